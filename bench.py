@@ -1,0 +1,296 @@
+#!/usr/bin/env python3
+"""Benchmark: singlephase D3Q19 permeability lattice update, MLUPS on one GB300.
+
+Workload (one bench "step" = one LBM time step over the whole lattice):
+  256^3 lattice of overlapping solid spheres (seeded; lognormal radii, mean 8, sd 2
+  voxels) added until porosity 0.22, isolated pores removed; body force 1e-6 along z;
+  tau = 1 (nu = 1/6); MRT preset 1; periodic in x, y, z; FP64 storage and collision
+  (the plain drop-in form).  MLUPS counts fluid nodes only, as the reference's
+  benchmark does (singlephase_3D/0.src/Main.F90:471).
+
+  value : device-resident timed region (CUDA events), K steps.  The PDF state
+          (2.5 GB) is far larger than L2, so no flush is needed between steps.
+  e2e   : the same metric through the C ABI with host buffers: each timed round
+          uploads the full state from pinned host memory, runs R steps, and reads the
+          monitor result (per-slice flow rate) back to the host.
+  --impl reference : the reference algorithm's CPU implementation (the C++
+          restatement, all host threads) on the same workload, bounded sample.
+Under torchrun (N>1) every rank runs an independent replica (the lattice is not
+sharded); value = total fluid-node updates of all ranks / max time over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for sub in ("mf-lbm_gb300", "oracle"):
+    sys.path.insert(0, os.path.join(ROOT, sub))
+
+import numpy as np  # noqa: E402
+
+METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
+BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1}
+DTYPE = {0: "f64", 1: "f32", 2: "f16"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="lattice edge")
+    ap.add_argument("--porosity", type=float, default=0.22)
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
+    ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
+    ap.add_argument("--cpu-sample-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(n, porosity, precision, device=0):
+    from mflbm import geometry
+    from mflbm.solver import make_params
+    p = make_params(multiphase=0, nx=n, ny=n, nz=n, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
+                    wall_y_min=0, wall_y_max=0, wall_z_min=0, wall_z_max=0, inlet_bc=0, outlet_bc=0, mrt=1,
+                    la_nu1=1.0 / 6.0, force_z=1e-6, precision=precision, strict_fp=0, device=device)
+    wg = geometry.sphere_packing((n, n, n), porosity, mean_r=8.0, sd_r=2.0, seed=2024)
+    walls, pore, _ = geometry.set_walls(p, wg)
+    return p, walls, pore
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(p, walls, pore, steps):
+    """The CPU restatement of the reference (all host threads) on the same workload."""
+    import pyoracle
+    threads = os.cpu_count() or 1
+    o = pyoracle.Oracle(p, variant="fast", threads=threads)
+    o.set_geometry(walls)
+    o.init_equilibrium()
+    o.run(1, 2)  # first-touch and warm-up
+    t0 = time.perf_counter()
+    o.run(3, steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": pore * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the full {p.nx}x{p.ny}x{p.nz} workload ({pore} fluid nodes), "
+                      f"C++ restatement -O3, OpenMP {threads} threads, {dt:.2f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    p, walls, pore = workload(args.n, args.porosity, 0)
+    steps = max(1, min(args.steps, args.cpu_sample_steps))
+    import pyoracle
+    threads = os.cpu_count() or 1
+    o = pyoracle.Oracle(p, variant="fast", threads=threads)
+    o.set_geometry(walls)
+    o.init_equilibrium()
+    o.run(1, max(args.warmup, 0) and 2)
+    t0 = time.perf_counter()
+    o.run(3, steps)
+    dt = time.perf_counter() - t0
+    v = pore * steps / dt / 1e6
+    line = {"metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity}, "
+                                   "periodic xyz, F_z=1e-6, tau=1, MRT preset 1", "fluid_nodes": pore},
+            "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+                             "sample": f"{steps} steps of the full workload; the Fortran reference cannot be built "
+                                       "(no Fortran compiler or MPI), so its C++ restatement runs instead"},
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    world, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from mflbm import Solver
+    p, walls, pore = workload(args.n, args.porosity, args.precision, device=local)
+    sim = Solver(p)
+    sim.set_geometry(walls)
+    sim.init_equilibrium()
+    # warm-up (graph capture, first touch)
+    sim.run(1, max(args.warmup, 3))
+    sim.synchronize()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region: per-step launches with CUDA events around every
+    # collision sweep (profiling mode), the region bracketed by events on the same stream
+    barrier()
+    sim.set_profiling(True)
+    with ClockSampler(local) as clk:
+        sim.run(args.warmup + 1, args.steps)
+        prof = sim.get_profile()   # synchronises the context stream
+    total_s = prof["region_ms"] / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * pore * args.steps / total_s / 1e6
+
+    # ---- graph-replayed region (the production path, no per-kernel events)
+    barrier()
+    sim.set_profiling(False)
+    sim.run(args.warmup + 1 + args.steps, args.steps)
+    gprof = sim.get_profile()
+    graph_mlups = pore * args.steps / (gprof["region_ms"] / 1e3) / 1e6
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    try:
+        rs = args.e2e_round
+        state = sim.download_state()
+        f_host = torch.from_numpy(state["f"]).pin_memory().numpy()
+        barrier()
+        t0 = time.perf_counter()
+        nround = max(1, args.steps // rs)
+        for r in range(nround):
+            sim.upload_state(f_host)
+            sim.run(2, rs)
+            prof_z, scal, status = sim.monitor()
+        e2e_s = time.perf_counter() - t0
+        h2d = f_host.nbytes
+        d2h = 2 * p.nz * 8 + 3 * 8 + 4
+        e2e = {"value": world * pore * rs * nround / e2e_s / 1e6, "unit": "MLUPS",
+               "h2d_bytes_per_step": h2d / rs, "d2h_bytes_per_step": d2h / rs,
+               "round": f"upload full state (pinned) + {rs} steps + monitor readback"}
+    except Exception as exc:  # keep the device-timed number even if e2e fails
+        e2e = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
+
+    collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
+    bpl = BYTES_PER_LU[args.precision]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = pore * bpl / collide_avg_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "sp_collide_traffic.json")
+    if os.path.exists(tf):
+        try:
+            t = json.load(open(tf))
+            traffic = t["bytes_per_fluid_node"] * pore
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(p, walls, pore, args.cpu_sample_steps)
+        except Exception as exc:
+            cpu = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
+            "config": {"workload": f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity} "
+                                   "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, "
+                                   "F_z=1e-6, tau=1, MRT preset 1",
+                       "lattice": [args.n] * 3, "fluid_nodes": pore, "replicas": world,
+                       "l2": f"state {19 * 8 * (args.n + 2) ** 3 / 1e9:.1f} GB >> 129 MB L2, no flush needed",
+                       "timed_path": "per-step launches with events around each collision sweep",
+                       "graph_replay_mlups": graph_mlups},
+            "e2e": e2e,
+            "gpu_launches": prof["kernel_launches"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic, "bytes_per_lu": bpl, "peak_source": "measured (MEASURED_PEAKS.json)",
+                         "kernel": "k_sp_step", "avg_launch_ms": collide_avg_s * 1e3},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,222 @@
+/*
+ * mflbm.h -- C ABI of the GB300 lattice-Boltzmann step library (libmflbm.so).
+ *
+ * The library replaces the per-time-step device work of MF-LBM's two Fortran
+ * programs, multiphase_3D and singlephase_3D, on one GPU:
+ *
+ *   - the OpenACC data region and the per-step kernels it encloses
+ *     (multiphase_3D/0.src/Main_multiphase.F90:104-115, 120-122, 167, 325;
+ *      singlephase_3D/0.src/Main.F90:98-103, 140, 278),
+ *   - main_iteration_kernel (Main_multiphase.F90:341-486; Main.F90:291-422),
+ *     including the inlet/outlet/porous-plate boundary conditions and the
+ *     single-rank periodic halo exchange that the reference performs through
+ *     MPI messages to itself (multiphase_3D/0.src/Mpi.F90:101-867),
+ *   - color_gradient (multiphase_3D/0.src/Phase_gradient.F90:5-265),
+ *   - compute_macro_vars (multiphase_3D/0.src/Misc.F90:372-430;
+ *     singlephase_3D/0.src/Misc.F90:368-423) and the device-side reductions of
+ *     monitor / cal_saturation (multiphase_3D/0.src/Monitor.F90:5-85, 512-550;
+ *     singlephase_3D/0.src/Monitor.F90:4-59).
+ *
+ * The Fortran host keeps deck parsing, geometry preprocessing, initialisation,
+ * file I/O and the time loop, and calls these entry points through
+ * ISO_C_BINDING (the mechanism the reference already uses for gethostid,
+ * multiphase_3D/0.src/Misc.F90:442-447).
+ *
+ * Conventions
+ *   - Every array crossing the ABI uses the reference's halo'd Fortran layout
+ *     (column-major, i fastest):
+ *       PDFs f_q, g_q, curv, u, v, w, rho : (1-1:n+1) in x, y, z  (halo 1)
+ *       phi                               : (1-4:n+4)             (halo 4)
+ *       cn_x, cn_y, cn_z, c_norm, walls   : (1-2:n+2)             (halo 2)
+ *       w_in, phi_convec_bc               : (0:nx+1, 0:ny+1)
+ *       f_convec_bc, g_convec_bc          : (0:nx+1, 0:ny+1, 0:18)
+ *   - All functions return MFLBM_OK (0) on success or a negative MFLBM_E* code;
+ *     mflbm_last_error() then holds a one-line message.
+ *   - One host thread per context; calls on one context are not thread-safe.
+ *     mflbm_step / mflbm_run are asynchronous on the context's CUDA stream;
+ *     every call that returns data to the host synchronises first.
+ *   - Host pointers are only read or written during the call.
+ *   - ntime keeps the reference's meaning: even = in-place collision, odd =
+ *     streaming collision (AA pattern); the state is in natural order only
+ *     after even steps (multiphase_3D/0.src/Init_multiphase.F90:155-159).
+ */
+#ifndef MFLBM_H
+#define MFLBM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFLBM_ABI_VERSION 1
+
+/* status codes */
+#define MFLBM_OK        0
+#define MFLBM_EINVAL   -1   /* invalid argument or parameter combination            */
+#define MFLBM_ECUDA    -2   /* CUDA runtime error (message in mflbm_last_error)     */
+#define MFLBM_ENOMEM   -3   /* device allocation failed                             */
+#define MFLBM_ESTATE   -4   /* call out of order (e.g. step before set_geometry)    */
+#define MFLBM_ETIMEOUT -5   /* a bounded device-side wait gave up                   */
+#define MFLBM_ENODEV   -6   /* no usable CUDA device                                */
+#define MFLBM_ERANGE   -7   /* a size exceeds a documented limit                    */
+
+/* simulation_end_indicator values reported by mflbm_monitor
+ * (multiphase_3D/0.src/Monitor.F90:253-259) */
+#define MFLBM_RUNNING 0
+#define MFLBM_FAILED  3
+
+/* PDF storage precision */
+#define MFLBM_FP64 0   /* plain drop-in: FP64 storage, FP64 collision               */
+#define MFLBM_FP32 1   /* FP32 storage, FP32 collision                              */
+#define MFLBM_FP16 2   /* FP16 storage of f_q - w_q*rho0, FP32 collision            */
+
+/* Run parameters: the subset of simulation_control.txt that the per-step path
+ * reads, after the reference's own host-side derivations
+ * (multiphase_3D/0.src/Init_multiphase.F90:116-150, IO_multiphase.F90:467-468;
+ *  singlephase_3D/0.src/Initialization.F90:80-129). */
+typedef struct mflbm_params {
+    int32_t abi_version;      /* must be MFLBM_ABI_VERSION                                 */
+    int32_t multiphase;       /* 1: multiphase_3D colour-gradient model, 0: singlephase_3D */
+    int32_t nx, ny, nz;       /* lattice_dimensions (one device holds the whole domain)    */
+    int32_t iper, jper, kper; /* periodic_indicator; iper=1 is an extension (singlephase)  */
+    int32_t wall_x_min, wall_x_max;   /* domain_wall_status_x                             */
+    int32_t wall_y_min, wall_y_max;   /* domain_wall_status_y                             */
+    int32_t wall_z_min, wall_z_max;   /* domain_wall_status_z                             */
+    int32_t inlet_bc;         /* 1 velocity (bounce-back), 2 Zou-He pressure               */
+    int32_t outlet_bc;        /* 1 convective, 2 Zou-He pressure                           */
+    int32_t mrt;              /* multiphase: the compile-time `mrt` switch (1..4, ref. 2)
+                                 singlephase: MRT_collision_parameter_preset               */
+    int32_t porous_plate_cmd; /* 0 none, 1 block fluid 1, 2 block fluid 2                  */
+    int32_t z_porous_plate;   /* plane index of the porous plate                           */
+    int32_t precision;        /* MFLBM_FP64 / MFLBM_FP32 / MFLBM_FP16                      */
+    int32_t strict_fp;        /* 1: no FMA contraction (bit-identical to an IEEE restatement) */
+    int32_t device;           /* CUDA device ordinal                                       */
+    double  la_nu1;           /* fluid1_viscosity (singlephase: fluid_viscosity)           */
+    double  la_nu2;           /* fluid2_viscosity                                          */
+    double  gamma;            /* surface_tension                                           */
+    double  beta;             /* RK_beta                                                   */
+    double  sa_inject;        /* saturation_injection (phi_inlet = 2*sa_inject-1)          */
+    double  force_z;          /* effective body force along z (force_Z)                    */
+    double  uin_avg;          /* average inlet velocity; convective outlet speed           */
+    double  rho_in;           /* inlet density for inlet_bc=2                              */
+    double  rho_out;          /* outlet density for outlet_bc=2 (reference: 1)             */
+    double  relaxation;       /* `relaxation` (reference: 1)                               */
+} mflbm_params;
+
+/* One solid-boundary node: the Fortran derived type indirect_solid_boundary_nodes
+ * (multiphase_3D/0.src/Module.F90:90-94), 96 bytes, local halo'd coordinates. */
+typedef struct mflbm_solid_bnd {
+    int32_t ix, iy, iz, i_fluid_num;
+    int32_t neighbor_list[18];   /* D3Q19 direction indices 1..18 of fluid neighbours */
+    double  la_weight;
+} mflbm_solid_bnd;
+
+/* One fluid-boundary node: indirect_fluid_boundary_nodes
+ * (multiphase_3D/0.src/Module.F90:98-101), 48 bytes; theta in radians after the
+ * reference's (180-theta)*pi/180 transform (IO_multiphase.F90:467-468). */
+typedef struct mflbm_fluid_bnd {
+    int32_t ix, iy, iz, _pad;
+    double  nwx, nwy, nwz, theta;
+} mflbm_fluid_bnd;
+
+typedef struct mflbm_ctx mflbm_ctx;
+
+/* Library ABI version (MFLBM_ABI_VERSION). */
+int32_t mflbm_version(void);
+
+/* Allocate a context and its device arrays.  Replaces MemAllocate_multi /
+ * MemAllocate (Init_multiphase.F90:583-828; singlephase Initialization.F90:380-516)
+ * plus the `!$acc data` region entry (Main_multiphase.F90:104-115).
+ * Validates the parameter combinations the reference rejects
+ * (IO_multiphase.F90:471-541). */
+int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out);
+
+/* Free all device memory (the `!$acc end data` at Main_multiphase.F90:325). */
+void mflbm_destroy(mflbm_ctx *ctx);
+
+/* Last error message of ctx, or of the last failed mflbm_create when ctx is NULL. */
+const char *mflbm_last_error(const mflbm_ctx *ctx);
+
+/* Upload the geometry: walls (int8, halo 2, after set_walls' halo transport,
+ * multiphase_3D/0.src/Misc.F90:6-210), the solid/fluid boundary lists from
+ * geometry_preprocessing_new/_load (Geometry_preprocessing.F90:9-685; ignored
+ * for singlephase, may be NULL/0) and the inlet profile w_in (nullable when the
+ * inlet is not a velocity inlet). */
+int32_t mflbm_set_geometry(mflbm_ctx *ctx, const int8_t *walls,
+                           const mflbm_solid_bnd *solid, int32_t n_solid,
+                           const mflbm_fluid_bnd *fluid, int32_t n_fluid,
+                           const double *w_in);
+
+/* Upload the full halo'd state (copyin of the `!$acc data` region).
+ * f[19] / g[19] are arrays of 19 pointers; g, phi and the convective arrays are
+ * NULL for singlephase; the convective arrays are required when outlet_bc==1. */
+int32_t mflbm_upload_state(mflbm_ctx *ctx, const double *const *f, const double *const *g,
+                           const double *phi, const double *f_convec,
+                           const double *g_convec, const double *phi_convec);
+
+/* Download the full halo'd state (the `!$acc update host` of save_checkpoint,
+ * IO_multiphase.F90:568-571).  NULL pointers are skipped. */
+int32_t mflbm_download_state(mflbm_ctx *ctx, double *const *f, double *const *g, double *phi,
+                             double *f_convec, double *g_convec, double *phi_convec);
+
+/* Device-side initialisation_new_multi_pdf / initialization_new_pdf with
+ * u=v=w=0, rho=1 over the halo'd box, plus the convective-outlet memory
+ * (Init_multiphase.F90:357-470; singlephase Initialization.F90:240-309).
+ * phi (halo 4) is required for multiphase and ignored for singlephase. */
+int32_t mflbm_init_equilibrium(mflbm_ctx *ctx, const double *phi);
+
+/* One main_iteration_kernel for time step ntime (asynchronous). */
+int32_t mflbm_step(mflbm_ctx *ctx, int32_t ntime);
+
+/* nsteps consecutive steps ntime0 .. ntime0+nsteps-1, replayed from a captured
+ * CUDA graph of one even+odd pair (asynchronous). */
+int32_t mflbm_run(mflbm_ctx *ctx, int32_t ntime0, int32_t nsteps);
+
+/* color_gradient (multiphase only): phi extrapolation, normals, wetting,
+ * normal extrapolation, curvature.  Called once after upload, as
+ * Main_multiphase.F90:120 does. */
+int32_t mflbm_color_gradient(mflbm_ctx *ctx);
+
+/* Download cn_x, cn_y, cn_z, c_norm (halo 2) and curv (halo 1); NULL skips. */
+int32_t mflbm_get_gradient(mflbm_ctx *ctx, double *cn_x, double *cn_y, double *cn_z,
+                           double *c_norm, double *curv);
+
+/* compute_macro_vars, then download u, v, w, rho (halo 1, NULL skips) and,
+ * for multiphase, phi (halo 4, NULL skips).  Like the reference this zeroes
+ * phi at wall nodes.  Valid after even steps only. */
+int32_t mflbm_macro(mflbm_ctx *ctx, double *u, double *v, double *w, double *rho,
+                    double *phi);
+
+/* compute_macro_vars + the device reductions of monitor.
+ * multiphase: profiles[7*nz] = fl1, fl2, vol1, vol2, mass1, mass2, pre (per z slice);
+ *             scalars[3]     = umax^2, usq1, usq2.
+ * singlephase: profiles[2*nz] = fl, pre;  scalars[3] = umax^2, 0, 0.
+ * *status = MFLBM_FAILED when a sum is NaN or sqrt(umax^2) > 0.5, else MFLBM_RUNNING.
+ * Sums accumulate in FP64 in every precision mode. */
+int32_t mflbm_monitor(mflbm_ctx *ctx, double *profiles, double *scalars, int32_t *status);
+
+/* cal_saturation (multiphase_3D/0.src/Monitor.F90:512-550): vol1, vol2 sums. */
+int32_t mflbm_saturation(mflbm_ctx *ctx, double *vol1, double *vol2);
+
+/* Wait for all work queued on the context's stream. */
+int32_t mflbm_synchronize(mflbm_ctx *ctx);
+
+/* Diagnostics for benchmarking; no counterpart in the reference.
+ * Starts a measurement region: records a CUDA event on the context's stream and
+ * resets the counters below.  enable=1 also makes mflbm_step / mflbm_run launch step
+ * by step (no graph replay) with CUDA events around every collision sweep. */
+int32_t mflbm_set_profiling(mflbm_ctx *ctx, int32_t enable);
+
+/* Ends the region: device time (ms) since mflbm_set_profiling on the context's
+ * stream, the time and number of the timed collision sweeps (profiling mode), and
+ * the number of kernels launched by mflbm_step / mflbm_run (graph replays included).
+ * Synchronises. */
+int32_t mflbm_get_profile(mflbm_ctx *ctx, double *region_ms, double *collide_ms, int64_t *collide_launches,
+                          int64_t *kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MFLBM_H */

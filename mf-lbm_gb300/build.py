@@ -1,0 +1,78 @@
+"""Build libmflbm.so (sm_103a) in-tree.
+
+Three translation units are compiled in parallel and linked into
+mf-lbm_gb300/mflbm/lib/libmflbm.so:
+
+  csrc/api.cu             C ABI, context, step ordering, CUDA graphs
+  csrc/kernels_fast.cu    kernels with nvcc's default FMA contraction
+  csrc/kernels_strict.cu  the same kernels with --fmad=false (bit-identical to an IEEE
+                          restatement that keeps the reference's operation order)
+
+Only one -gencode (sm_103a) is built.  nvcc cross-compiles without a GPU, so this runs
+on the CPU build host and on the GPU host alike.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "mflbm", "lib")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libmflbm.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          "--expt-relaxed-constexpr"]
+UNITS = {
+    "api.o": ("api.cu", []),
+    "kernels_fast.o": ("kernels_fast.cu", []),
+    "kernels_strict.o": ("kernels_strict.cu", ["--fmad=false"]),
+}
+
+
+def nvcc():
+    exe = shutil.which("nvcc")
+    if exe is None:
+        cand = "/usr/local/cuda/bin/nvcc"
+        if os.path.exists(cand):
+            return cand
+        raise RuntimeError("nvcc not found")
+    return exe
+
+
+def _sources_mtime():
+    m = 0.0
+    for root in (CSRC, os.path.join(HERE, "..", "include")):
+        for name in os.listdir(root):
+            m = max(m, os.path.getmtime(os.path.join(root, name)))
+    return m
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+        return LIB
+    exe = nvcc()
+    procs = []
+    for obj, (src, extra) in UNITS.items():
+        cmd = [exe, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", os.path.join(BUILD_DIR, obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((subprocess.Popen(cmd), obj))
+    failed = [obj for p, obj in procs if p.wait() != 0]
+    if failed:
+        raise RuntimeError(f"nvcc failed for {failed}")
+    tmp = LIB + ".tmp"
+    cmd = [exe, *ARCH, "-shared", "-o", tmp, *[os.path.join(BUILD_DIR, o) for o in UNITS]]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,679 @@
+// api.cu -- the C ABI of libmflbm.so (declared in include/mflbm.h).
+//
+// One mflbm_ctx owns one CUDA stream and every device array of one simulation.  The
+// ordering of a time step follows main_iteration_kernel
+// (multiphase_3D/0.src/Main_multiphase.F90:341-486; singlephase_3D/0.src/Main.F90:291-422):
+//   collision sweep (even: in place, odd: AA streaming)
+//   -> periodic halo exchange (pull after even, push after odd; phi after both)
+//   -> inlet/outlet BCs (_before_odd after even, _after_odd after odd) and porous plate
+//   -> color_gradient (multiphase)
+// mflbm_run replays the same launches from CUDA graphs captured once per context.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/mflbm.h"
+#include "kernels_api.h"
+
+using namespace mflbm;
+
+struct mflbm_ctx {
+    mflbm_params p{};
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    const KernelTable *kt = nullptr;
+    DevState st{};
+    size_t elt = 8;
+    std::vector<void *> allocs;
+    bool have_geometry = false;
+    bool open_z = false;
+    // graphs of whole even+odd step pairs
+    cudaGraphExec_t g_pair = nullptr, g_block = nullptr;
+    int block_pairs = 8;
+    std::vector<double> h_mon;
+    std::string err;
+    // diagnostics: kernel launch count; optional CUDA-event timing of collision sweeps
+    int64_t launches = 0;
+    int64_t pair_launches = 0, block_launches = 0;  // kernels per captured graph
+    bool profiling = false;
+    cudaEvent_t region0 = nullptr, region1 = nullptr;  // bracket the region since set_profiling
+    std::vector<cudaEvent_t> ev;   // 2 * kEventRing, pairs around each collision sweep
+    int ev_used = 0;
+    double collide_ms = 0.0;
+    int64_t collide_count = 0;
+};
+
+static const int kEventRing = 512;
+
+static thread_local std::string g_last_create_error;
+
+namespace {
+
+int fail(mflbm_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg; else g_last_create_error = msg;
+    return code;
+}
+
+int cuda_fail(mflbm_ctx *c, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(c, e == cudaErrorMemoryAllocation ? MFLBM_ENOMEM : MFLBM_ECUDA, m);
+}
+
+#define CK(ctx, expr)                                             \
+    do {                                                          \
+        cudaError_t e_ = (expr);                                  \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #expr); \
+    } while (0)
+
+int64_t n1(const mflbm_params &p) { return (int64_t)(p.nx + 2) * (p.ny + 2) * (p.nz + 2); }
+int64_t n2(const mflbm_params &p) { return (int64_t)(p.nx + 4) * (p.ny + 4) * (p.nz + 4); }
+int64_t n4(const mflbm_params &p) { return (int64_t)(p.nx + 8) * (p.ny + 8) * (p.nz + 8); }
+int64_t nplane(const mflbm_params &p) { return (int64_t)(p.nx + 2) * (p.ny + 2); }
+
+// parameter checks of read_parameter_multi / read_parameter
+// (multiphase_3D/0.src/IO_multiphase.F90:471-541; singlephase_3D/0.src/IO.F90:393-451)
+int validate(const mflbm_params *p, std::string &err) {
+    if (!p) { err = "params is NULL"; return MFLBM_EINVAL; }
+    if (p->abi_version != MFLBM_ABI_VERSION) { err = "abi_version mismatch"; return MFLBM_EINVAL; }
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3) { err = "lattice dimensions must be >= 3"; return MFLBM_EINVAL; }
+    if ((int64_t)p->nx * p->ny > ((int64_t)1 << 30) || p->nz > 65000 || p->ny > 65000) {
+        err = "lattice dimensions exceed the launch-grid limits"; return MFLBM_ERANGE;
+    }
+    if (p->multiphase) {
+        if (p->iper == 1 || p->wall_x_max == 0 || p->wall_x_min == 0) {
+            err = "X direction periodic BC enabled or non-slip BC not applied at x = xmin or x = xmax";
+            return MFLBM_EINVAL;
+        }
+        if (p->mrt < 1 || p->mrt > 4) { err = "mrt must be 1..4"; return MFLBM_EINVAL; }
+        if (p->precision != MFLBM_FP64) { err = "multiphase supports MFLBM_FP64 storage only"; return MFLBM_EINVAL; }
+        if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
+    } else {
+        if (p->iper == 1 && (p->wall_x_max == 1 || p->wall_x_min == 1)) {
+            err = "non-slip BC applied at x = xmin or x = xmax while x direction periodic BC enabled";
+            return MFLBM_EINVAL;
+        }
+        if (p->iper == 0 && (p->wall_x_max == 0 || p->wall_x_min == 0)) {
+            err = "non-slip BC not applied at x = xmin or x = xmax while x direction periodic BC not enabled";
+            return MFLBM_EINVAL;
+        }
+    }
+    if (p->jper == 0 && (p->wall_y_max == 0 || p->wall_y_min == 0)) {
+        err = "non-slip BC not applied at y = ymin or y = ymax while y direction periodic BC not enabled";
+        return MFLBM_EINVAL;
+    }
+    if (p->jper == 1 && (p->wall_y_max == 1 || p->wall_y_min == 1)) {
+        err = "non-slip BC applied at y = ymin or y = ymax while y direction periodic BC enabled";
+        return MFLBM_EINVAL;
+    }
+    if (p->kper == 1 && (p->wall_z_max == 1 || p->wall_z_min == 1)) {
+        err = "non-slip BC applied at z = zmin or z = zmax while z direction periodic BC enabled";
+        return MFLBM_EINVAL;
+    }
+    if (p->outlet_bc == 1 && p->inlet_bc == 2) {
+        err = "Inlet pressure + outlet convective BC is not supported";
+        return MFLBM_EINVAL;
+    }
+    if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FP16) { err = "unknown precision"; return MFLBM_EINVAL; }
+    if (p->la_nu1 <= 0.0) { err = "la_nu1 must be positive"; return MFLBM_EINVAL; }
+    return MFLBM_OK;
+}
+
+template <class T> int dalloc(mflbm_ctx *c, T **ptr, int64_t count) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (size_t)count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    c->allocs.push_back(p);
+    e = cudaMemsetAsync(p, 0, (size_t)count * sizeof(T), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync");
+    *ptr = reinterpret_cast<T *>(p);
+    return MFLBM_OK;
+}
+
+void drop_graphs(mflbm_ctx *c) {
+    if (c->g_pair) cudaGraphExecDestroy(c->g_pair);
+    if (c->g_block) cudaGraphExecDestroy(c->g_block);
+    c->g_pair = c->g_block = nullptr;
+}
+
+// fold the recorded event pairs into the running totals
+int drain_events(mflbm_ctx *c) {
+    if (c->ev_used == 0) return MFLBM_OK;
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int t = 0; t < c->ev_used; ++t) {
+        float ms = 0.f;
+        CK(c, cudaEventElapsedTime(&ms, c->ev[2 * t], c->ev[2 * t + 1]));
+        c->collide_ms += ms;
+    }
+    c->collide_count += c->ev_used;
+    c->ev_used = 0;
+    return MFLBM_OK;
+}
+
+// launches of one main_iteration_kernel; no synchronisation, capturable unless
+// profiling (which brackets the collision sweep with events); returns kernels launched
+int enqueue_step(mflbm_ctx *c, int32_t ntime) {
+    const bool even = (ntime % 2) == 0;
+    int n = 0;
+    const bool timed = c->profiling;
+    if (timed) {
+        if (c->ev_used == kEventRing && drain_events(c)) return -1;
+        cudaEventRecord(c->ev[2 * c->ev_used], c->stream);
+    }
+    n += c->kt->collide(c->st, !even, c->stream);
+    if (timed) {
+        cudaEventRecord(c->ev[2 * c->ev_used + 1], c->stream);
+        ++c->ev_used;
+    }
+    n += c->kt->wrap(c->st, even, c->stream);
+    n += c->kt->boundary(c->st, even, c->p.inlet_bc, c->p.outlet_bc, c->open_z, c->stream);
+    if (c->p.multiphase) n += c->kt->color_gradient(c->st, c->stream);
+    return n;
+}
+
+int capture(mflbm_ctx *c, int pairs, cudaGraphExec_t *out, int64_t *nkernels) {
+    cudaGraph_t graph = nullptr;
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int64_t n = 0;
+    for (int t = 0; t < pairs; ++t) {
+        n += enqueue_step(c, 0);
+        n += enqueue_step(c, 1);
+    }
+    *nkernels = n;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+    return MFLBM_OK;
+}
+
+int ready(mflbm_ctx *c) {
+    if (!c) return MFLBM_EINVAL;
+    if (!c->have_geometry) return fail(c, MFLBM_ESTATE, "mflbm_set_geometry must be called first");
+    return MFLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mflbm_version(void) { return MFLBM_ABI_VERSION; }
+
+const char *mflbm_last_error(const mflbm_ctx *ctx) {
+    return ctx ? ctx->err.c_str() : g_last_create_error.c_str();
+}
+
+int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
+    if (!out) return fail(nullptr, MFLBM_EINVAL, "out is NULL");
+    *out = nullptr;
+    std::string err;
+    int rc = validate(params, err);
+    if (rc) return fail(nullptr, rc, err);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= 0)
+        return fail(nullptr, MFLBM_ENODEV, std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+    if (params->device < 0 || params->device >= ndev) return fail(nullptr, MFLBM_ENODEV, "device ordinal out of range");
+    e = cudaSetDevice(params->device);
+    if (e != cudaSuccess) return fail(nullptr, MFLBM_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+
+    mflbm_ctx *c = new mflbm_ctx();
+    c->p = *params;
+    c->dev = params->device;
+    const mflbm_params &p = c->p;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        g_last_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+        delete c;
+        return MFLBM_ECUDA;
+    }
+    c->kt = p.strict_fp ? kernels_strict() : kernels_fast();
+    c->open_z = p.kper == 0 && p.wall_z_min == 0 && p.wall_z_max == 0;
+    c->elt = p.precision == MFLBM_FP32 ? 4 : (p.precision == MFLBM_FP16 ? 2 : 8);
+
+    // padded PDF layout: i=1 on a 32-byte boundary, rows multiple of 32 bytes
+    Layout &L = c->st.L;
+    const int A = (int)(32 / c->elt);
+    L.nx = p.nx; L.ny = p.ny; L.nz = p.nz;
+    L.xo = A - 1;
+    L.pitch = ((int64_t)L.xo + p.nx + 2 + A - 1) / A * A;
+    L.pz = L.pitch * (p.ny + 2);
+    L.qs = L.pz * (p.nz + 2);
+    L.h1x = p.nx + 2; L.h1xy = (int64_t)(p.nx + 2) * (p.ny + 2);
+    L.h2x = p.nx + 4; L.h2xy = (int64_t)(p.nx + 4) * (p.ny + 4);
+    L.h4x = p.nx + 8; L.h4xy = (int64_t)(p.nx + 8) * (p.ny + 8);
+
+    // derived parameters (Init_multiphase.F90:116-128; singlephase Initialization.F90:80-112)
+    StepParams &P = c->st.P;
+    P.force_z = p.force_z;
+    P.gamma = p.gamma;
+    P.beta = p.beta;
+    P.la_nui1 = 1.0 / p.la_nu1;
+    P.la_nui2 = p.multiphase ? 1.0 / p.la_nu2 : 0.0;
+    P.sa_inject = p.sa_inject;
+    P.phi_inlet = 2.0 * p.sa_inject - 1.0;
+    P.uin_avg = p.uin_avg;
+    P.rho_in = p.rho_in;
+    P.rho_out = p.rho_out;
+    P.relaxation = p.relaxation;
+    P.mrt = p.mrt;
+    P.porous_plate_cmd = p.porous_plate_cmd;
+    P.z_porous_plate = p.z_porous_plate;
+    P.iper = p.iper; P.jper = p.jper; P.kper = p.kper;
+    {
+        const double omega = 1.0 / (3.0 * p.la_nu1 + 0.5);
+        P.s_nu = omega;
+        if (p.mrt == 1) {
+            P.s_e = omega; P.s_e2 = omega; P.s_pi = omega;
+            P.s_q = 8.0 * (2.0 - omega) / (8.0 - omega);
+            P.s_t = P.s_q;
+        } else {
+            // the reference tests `== 1` twice (Initialization.F90:91-98): other presets are SRT
+            P.s_e = omega; P.s_e2 = omega; P.s_pi = omega; P.s_q = omega; P.s_t = omega;
+        }
+    }
+    c->st.multiphase = p.multiphase;
+    c->st.prec = p.precision;
+    c->st.ref = 1.0f;
+    c->st.scale = 4096.0f;
+    c->st.rk_weight2 = 1.0 / std::sqrt(2.0) / 36.0;
+
+    // device arrays (MemAllocate_multi, Init_multiphase.F90:583-828)
+    const int nsp = p.multiphase ? 2 : 1;
+    int r = MFLBM_OK;
+    {
+        void *pdf = nullptr;
+        const size_t bytes = (size_t)nsp * 19 * (size_t)L.qs * c->elt;
+        e = cudaMalloc(&pdf, bytes);
+        if (e != cudaSuccess) { r = cuda_fail(c, e, "cudaMalloc(PDF)"); goto fail_create; }
+        c->allocs.push_back(pdf);
+        e = cudaMemsetAsync(pdf, 0, bytes, c->stream);
+        if (e != cudaSuccess) { r = cuda_fail(c, e, "cudaMemsetAsync(PDF)"); goto fail_create; }
+        c->st.f = pdf;
+        c->st.g = p.multiphase ? (void *)((char *)pdf + (size_t)19 * L.qs * c->elt) : nullptr;
+    }
+    if ((r = dalloc(c, &c->st.walls, n2(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.w_in, nplane(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.fconv, nplane(p) * 19))) goto fail_create;
+    if ((r = dalloc(c, &c->st.u, n1(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.v, n1(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.w, n1(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.rho, n1(p)))) goto fail_create;
+    if ((r = dalloc(c, &c->st.mon, (int64_t)kMonNQ * p.nz))) goto fail_create;
+    if (p.precision != MFLBM_FP64 && (r = dalloc(c, &c->st.stage, n1(p)))) goto fail_create;
+    if (p.multiphase) {
+        if ((r = dalloc(c, &c->st.phi, n4(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.cnx, n2(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.cny, n2(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.cnz, n2(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.cnorm, n2(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.curv, n1(p)))) goto fail_create;
+        if ((r = dalloc(c, &c->st.gconv, nplane(p) * 19))) goto fail_create;
+        if ((r = dalloc(c, &c->st.phiconv, nplane(p)))) goto fail_create;
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { r = cuda_fail(c, e, "cudaStreamSynchronize"); goto fail_create; }
+    c->h_mon.assign((size_t)kMonNQ * p.nz, 0.0);
+    *out = c;
+    return MFLBM_OK;
+
+fail_create:
+    g_last_create_error = c->err;
+    mflbm_destroy(c);
+    return r;
+}
+
+void mflbm_destroy(mflbm_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->dev);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+    if (c->region0) cudaEventDestroy(c->region0);
+    if (c->region1) cudaEventDestroy(c->region1);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid,
+                           const mflbm_fluid_bnd *fluid, int32_t n_fluid, const double *w_in) {
+    if (!c) return MFLBM_EINVAL;
+    if (!walls) return fail(c, MFLBM_EINVAL, "walls is NULL");
+    if (n_solid < 0 || n_fluid < 0) return fail(c, MFLBM_EINVAL, "negative list length");
+    if ((n_solid > 0 && !solid) || (n_fluid > 0 && !fluid)) return fail(c, MFLBM_EINVAL, "list pointer is NULL");
+    const mflbm_params &p = c->p;
+    CK(c, cudaSetDevice(c->dev));
+    if (!p.multiphase) { n_solid = 0; n_fluid = 0; }
+    // every list entry must stay inside the arrays it touches: solid nodes inside
+    // [-2, n+3] (their neighbours reach the phi halo [-3, n+4]); fluid nodes inside
+    // [-1, n+2] (Geometry_preprocessing.F90:429-507)
+    for (int32_t t = 0; t < n_solid; ++t) {
+        const mflbm_solid_bnd &s = solid[t];
+        if (s.ix < -2 || s.ix > p.nx + 3 || s.iy < -2 || s.iy > p.ny + 3 || s.iz < -2 || s.iz > p.nz + 3)
+            return fail(c, MFLBM_EINVAL, "solid boundary node " + std::to_string(t) + " outside [-2, n+3]");
+        if (s.i_fluid_num < 0 || s.i_fluid_num > 18)
+            return fail(c, MFLBM_EINVAL, "solid boundary node " + std::to_string(t) + ": i_fluid_num outside 0..18");
+        for (int n = 0; n < s.i_fluid_num; ++n)
+            if (s.neighbor_list[n] < 1 || s.neighbor_list[n] > 18)
+                return fail(c, MFLBM_EINVAL, "solid boundary node " + std::to_string(t) + ": neighbour outside 1..18");
+    }
+    std::vector<FluidBnd> fb((size_t)n_fluid);
+    for (int32_t t = 0; t < n_fluid; ++t) {
+        const mflbm_fluid_bnd &f = fluid[t];
+        if (f.ix < -1 || f.ix > p.nx + 2 || f.iy < -1 || f.iy > p.ny + 2 || f.iz < -1 || f.iz > p.nz + 2)
+            return fail(c, MFLBM_EINVAL, "fluid boundary node " + std::to_string(t) + " outside [-1, n+2]");
+        fb[t] = FluidBnd{f.ix, f.iy, f.iz, 0, f.nwx, f.nwy, f.nwz, std::cos(f.theta), std::sin(f.theta)};
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    drop_graphs(c);
+    CK(c, cudaMemcpy(c->st.walls, walls, (size_t)n2(p), cudaMemcpyHostToDevice));
+    if (w_in) CK(c, cudaMemcpy(c->st.w_in, w_in, sizeof(double) * nplane(p), cudaMemcpyHostToDevice));
+    else CK(c, cudaMemset(c->st.w_in, 0, sizeof(double) * nplane(p)));
+    // lists: reallocate when they grow
+    static_assert(sizeof(SolidBnd) == sizeof(mflbm_solid_bnd), "solid boundary ABI");
+    if (n_solid > c->st.ns || (n_solid > 0 && !c->st.sb)) {
+        SolidBnd *sb = nullptr;
+        int r = dalloc(c, &sb, n_solid);
+        if (r) return r;
+        c->st.sb = sb;
+    }
+    if (n_fluid > c->st.nf || (n_fluid > 0 && !c->st.fb)) {
+        FluidBnd *fbd = nullptr;
+        int r = dalloc(c, &fbd, n_fluid);
+        if (r) return r;
+        c->st.fb = fbd;
+    }
+    if (n_solid) CK(c, cudaMemcpy((void *)c->st.sb, solid, sizeof(SolidBnd) * n_solid, cudaMemcpyHostToDevice));
+    if (n_fluid) CK(c, cudaMemcpy((void *)c->st.fb, fb.data(), sizeof(FluidBnd) * n_fluid, cudaMemcpyHostToDevice));
+    c->st.ns = n_solid;
+    c->st.nf = n_fluid;
+    CK(c, cudaDeviceSynchronize());
+    c->have_geometry = true;
+    return MFLBM_OK;
+}
+
+int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *const *g, const double *phi,
+                           const double *f_convec, const double *g_convec, const double *phi_convec) {
+    if (!c) return MFLBM_EINVAL;
+    const mflbm_params &p = c->p;
+    if (!f) return fail(c, MFLBM_EINVAL, "f is NULL");
+    for (int q = 0; q < 19; ++q) if (!f[q]) return fail(c, MFLBM_EINVAL, "f[q] is NULL");
+    if (p.multiphase) {
+        if (!g || !phi) return fail(c, MFLBM_EINVAL, "g and phi are required for multiphase");
+        for (int q = 0; q < 19; ++q) if (!g[q]) return fail(c, MFLBM_EINVAL, "g[q] is NULL");
+    }
+    if (p.outlet_bc == 1 && c->open_z && (!f_convec || (p.multiphase && (!g_convec || !phi_convec))))
+        return fail(c, MFLBM_EINVAL, "convective outlet memory arrays are required when outlet_bc == 1");
+    CK(c, cudaSetDevice(c->dev));
+    const Layout &L = c->st.L;
+    const int nsp = p.multiphase ? 2 : 1;
+    for (int s = 0; s < nsp; ++s) {
+        const double *const *src = s == 0 ? f : g;
+        char *base = (char *)(s == 0 ? c->st.f : c->st.g);
+        for (int q = 0; q < 19; ++q) {
+            if (p.precision == MFLBM_FP64) {
+                char *dst = base + ((size_t)q * L.qs + L.xo) * c->elt;
+                CK(c, cudaMemcpy2DAsync(dst, (size_t)L.pitch * 8, src[q], (size_t)(p.nx + 2) * 8, (size_t)(p.nx + 2) * 8,
+                                        (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyHostToDevice, c->stream));
+            } else {
+                CK(c, cudaMemcpyAsync(c->st.stage, src[q], sizeof(double) * n1(p), cudaMemcpyHostToDevice, c->stream));
+                c->kt->convert_in(c->st, s, q, c->stream);
+                CK(c, cudaPeekAtLastError());
+            }
+        }
+    }
+    if (p.multiphase) CK(c, cudaMemcpyAsync(c->st.phi, phi, sizeof(double) * n4(p), cudaMemcpyHostToDevice, c->stream));
+    if (f_convec) CK(c, cudaMemcpyAsync(c->st.fconv, f_convec, sizeof(double) * nplane(p) * 19, cudaMemcpyHostToDevice, c->stream));
+    if (p.multiphase && g_convec)
+        CK(c, cudaMemcpyAsync(c->st.gconv, g_convec, sizeof(double) * nplane(p) * 19, cudaMemcpyHostToDevice, c->stream));
+    if (p.multiphase && phi_convec)
+        CK(c, cudaMemcpyAsync(c->st.phiconv, phi_convec, sizeof(double) * nplane(p), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, double *phi, double *f_convec,
+                             double *g_convec, double *phi_convec) {
+    if (!c) return MFLBM_EINVAL;
+    const mflbm_params &p = c->p;
+    CK(c, cudaSetDevice(c->dev));
+    const Layout &L = c->st.L;
+    const int nsp = p.multiphase ? 2 : 1;
+    for (int s = 0; s < nsp; ++s) {
+        double *const *dstv = s == 0 ? f : g;
+        if (!dstv) continue;
+        const char *base = (const char *)(s == 0 ? c->st.f : c->st.g);
+        for (int q = 0; q < 19; ++q) {
+            if (!dstv[q]) continue;
+            if (p.precision == MFLBM_FP64) {
+                const char *src = base + ((size_t)q * L.qs + L.xo) * c->elt;
+                CK(c, cudaMemcpy2DAsync(dstv[q], (size_t)(p.nx + 2) * 8, src, (size_t)L.pitch * 8, (size_t)(p.nx + 2) * 8,
+                                        (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyDeviceToHost, c->stream));
+            } else {
+                c->kt->convert_out(c->st, s, q, c->stream);
+                CK(c, cudaPeekAtLastError());
+                CK(c, cudaMemcpyAsync(dstv[q], c->st.stage, sizeof(double) * n1(p), cudaMemcpyDeviceToHost, c->stream));
+            }
+        }
+    }
+    if (p.multiphase && phi) CK(c, cudaMemcpyAsync(phi, c->st.phi, sizeof(double) * n4(p), cudaMemcpyDeviceToHost, c->stream));
+    if (f_convec) CK(c, cudaMemcpyAsync(f_convec, c->st.fconv, sizeof(double) * nplane(p) * 19, cudaMemcpyDeviceToHost, c->stream));
+    if (p.multiphase && g_convec)
+        CK(c, cudaMemcpyAsync(g_convec, c->st.gconv, sizeof(double) * nplane(p) * 19, cudaMemcpyDeviceToHost, c->stream));
+    if (p.multiphase && phi_convec)
+        CK(c, cudaMemcpyAsync(phi_convec, c->st.phiconv, sizeof(double) * nplane(p), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_init_equilibrium(mflbm_ctx *c, const double *phi) {
+    if (!c) return MFLBM_EINVAL;
+    const mflbm_params &p = c->p;
+    if (p.multiphase && !phi) return fail(c, MFLBM_EINVAL, "phi is required for multiphase");
+    CK(c, cudaSetDevice(c->dev));
+    if (p.multiphase) CK(c, cudaMemcpyAsync(c->st.phi, phi, sizeof(double) * n4(p), cudaMemcpyHostToDevice, c->stream));
+    c->kt->init_equilibrium(c->st, p.outlet_bc == 1, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_step(mflbm_ctx *c, int32_t ntime) {
+    int r = ready(c);
+    if (r) return r;
+    if (ntime < 0) return fail(c, MFLBM_EINVAL, "ntime must be >= 0");
+    CK(c, cudaSetDevice(c->dev));
+    const int n = enqueue_step(c, ntime);
+    if (n < 0) return MFLBM_ECUDA;
+    c->launches += n;
+    CK(c, cudaPeekAtLastError());
+    return MFLBM_OK;
+}
+
+int32_t mflbm_run(mflbm_ctx *c, int32_t ntime0, int32_t nsteps) {
+    int r = ready(c);
+    if (r) return r;
+    if (ntime0 < 0 || nsteps < 0) return fail(c, MFLBM_EINVAL, "ntime0 and nsteps must be >= 0");
+    CK(c, cudaSetDevice(c->dev));
+    int32_t t = ntime0, left = nsteps;
+    if (c->profiling) {  // step by step, so every collision sweep is bracketed by events
+        for (; left > 0; ++t, --left) {
+            const int n = enqueue_step(c, t);
+            if (n < 0) return MFLBM_ECUDA;
+            c->launches += n;
+        }
+        CK(c, cudaPeekAtLastError());
+        return MFLBM_OK;
+    }
+    if (left > 0 && (t % 2) != 0) {  // graphs start on an even step
+        c->launches += enqueue_step(c, t);
+        ++t; --left;
+    }
+    if (left >= 2 && !c->g_pair) {
+        if ((r = capture(c, 1, &c->g_pair, &c->pair_launches))) return r;
+    }
+    if (left >= 2 * c->block_pairs && !c->g_block) {
+        if ((r = capture(c, c->block_pairs, &c->g_block, &c->block_launches))) return r;
+    }
+    while (left >= 2 * c->block_pairs) {
+        CK(c, cudaGraphLaunch(c->g_block, c->stream));
+        c->launches += c->block_launches;
+        t += 2 * c->block_pairs; left -= 2 * c->block_pairs;
+    }
+    while (left >= 2) {
+        CK(c, cudaGraphLaunch(c->g_pair, c->stream));
+        c->launches += c->pair_launches;
+        t += 2; left -= 2;
+    }
+    if (left == 1) c->launches += enqueue_step(c, t);
+    CK(c, cudaPeekAtLastError());
+    return MFLBM_OK;
+}
+
+int32_t mflbm_set_profiling(mflbm_ctx *c, int32_t enable) {
+    if (!c) return MFLBM_EINVAL;
+    CK(c, cudaSetDevice(c->dev));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (enable && c->ev.empty()) {
+        c->ev.resize(2 * kEventRing);
+        for (auto &e : c->ev) CK(c, cudaEventCreate(&e));
+    }
+    if (!c->region0) {
+        CK(c, cudaEventCreate(&c->region0));
+        CK(c, cudaEventCreate(&c->region1));
+    }
+    c->profiling = enable != 0;
+    c->ev_used = 0;
+    c->collide_ms = 0.0;
+    c->collide_count = 0;
+    c->launches = 0;
+    CK(c, cudaEventRecord(c->region0, c->stream));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_get_profile(mflbm_ctx *c, double *region_ms, double *collide_ms, int64_t *collide_launches,
+                          int64_t *kernel_launches) {
+    if (!c) return MFLBM_EINVAL;
+    if (!c->region0) return fail(c, MFLBM_ESTATE, "mflbm_set_profiling was not called");
+    CK(c, cudaSetDevice(c->dev));
+    CK(c, cudaEventRecord(c->region1, c->stream));
+    int r = drain_events(c);
+    if (r) return r;
+    CK(c, cudaEventSynchronize(c->region1));
+    float rms = 0.f;
+    CK(c, cudaEventElapsedTime(&rms, c->region0, c->region1));
+    if (region_ms) *region_ms = rms;
+    if (collide_ms) *collide_ms = c->collide_ms;
+    if (collide_launches) *collide_launches = c->collide_count;
+    if (kernel_launches) *kernel_launches = c->launches;
+    return MFLBM_OK;
+}
+
+int32_t mflbm_color_gradient(mflbm_ctx *c) {
+    int r = ready(c);
+    if (r) return r;
+    if (!c->p.multiphase) return fail(c, MFLBM_EINVAL, "color_gradient is multiphase only");
+    CK(c, cudaSetDevice(c->dev));
+    c->kt->color_gradient(c->st, c->stream);
+    CK(c, cudaPeekAtLastError());
+    return MFLBM_OK;
+}
+
+int32_t mflbm_get_gradient(mflbm_ctx *c, double *cn_x, double *cn_y, double *cn_z, double *c_norm, double *curv) {
+    if (!c) return MFLBM_EINVAL;
+    if (!c->p.multiphase) return fail(c, MFLBM_EINVAL, "multiphase only");
+    const mflbm_params &p = c->p;
+    CK(c, cudaSetDevice(c->dev));
+    CK(c, cudaStreamSynchronize(c->stream));
+    const size_t b2 = sizeof(double) * n2(p);
+    if (cn_x) CK(c, cudaMemcpy(cn_x, c->st.cnx, b2, cudaMemcpyDeviceToHost));
+    if (cn_y) CK(c, cudaMemcpy(cn_y, c->st.cny, b2, cudaMemcpyDeviceToHost));
+    if (cn_z) CK(c, cudaMemcpy(cn_z, c->st.cnz, b2, cudaMemcpyDeviceToHost));
+    if (c_norm) CK(c, cudaMemcpy(c_norm, c->st.cnorm, b2, cudaMemcpyDeviceToHost));
+    if (curv) CK(c, cudaMemcpy(curv, c->st.curv, sizeof(double) * n1(p), cudaMemcpyDeviceToHost));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_macro(mflbm_ctx *c, double *u, double *v, double *w, double *rho, double *phi) {
+    int r = ready(c);
+    if (r) return r;
+    const mflbm_params &p = c->p;
+    CK(c, cudaSetDevice(c->dev));
+    c->kt->monitor(c->st, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaStreamSynchronize(c->stream));
+    const size_t b1 = sizeof(double) * n1(p);
+    if (u) CK(c, cudaMemcpy(u, c->st.u, b1, cudaMemcpyDeviceToHost));
+    if (v) CK(c, cudaMemcpy(v, c->st.v, b1, cudaMemcpyDeviceToHost));
+    if (w) CK(c, cudaMemcpy(w, c->st.w, b1, cudaMemcpyDeviceToHost));
+    if (rho) CK(c, cudaMemcpy(rho, c->st.rho, b1, cudaMemcpyDeviceToHost));
+    if (phi && p.multiphase) CK(c, cudaMemcpy(phi, c->st.phi, sizeof(double) * n4(p), cudaMemcpyDeviceToHost));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_monitor(mflbm_ctx *c, double *profiles, double *scalars, int32_t *status) {
+    int r = ready(c);
+    if (r) return r;
+    const mflbm_params &p = c->p;
+    CK(c, cudaSetDevice(c->dev));
+    c->kt->monitor(c->st, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaMemcpyAsync(c->h_mon.data(), c->st.mon, sizeof(double) * kMonNQ * p.nz, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    const int nz = p.nz;
+    const double *m = c->h_mon.data();
+    bool bad = false;
+    if (profiles) {
+        if (p.multiphase) {
+            for (int q = 0; q < 7; ++q)
+                for (int k = 0; k < nz; ++k) profiles[q * nz + k] = m[q * nz + k];
+        } else {
+            for (int k = 0; k < nz; ++k) { profiles[k] = m[k]; profiles[nz + k] = m[6 * nz + k]; }
+        }
+    }
+    const int nq = 7;
+    for (int q = 0; q < nq; ++q)
+        for (int k = 0; k < nz; ++k)
+            if (std::isnan(m[q * nz + k])) bad = true;
+    double umax = 0.0, usq1 = 0.0, usq2 = 0.0;
+    for (int k = 0; k < nz; ++k) {
+        const double t = m[7 * nz + k];
+        if (umax < t) umax = t;
+        usq1 += m[8 * nz + k];
+        usq2 += m[9 * nz + k];
+    }
+    if (scalars) { scalars[0] = umax; scalars[1] = usq1; scalars[2] = usq2; }
+    if (std::isnan(umax) || std::sqrt(umax) > 0.5) bad = true;
+    if (status) *status = bad ? MFLBM_FAILED : MFLBM_RUNNING;
+    return MFLBM_OK;
+}
+
+int32_t mflbm_saturation(mflbm_ctx *c, double *vol1, double *vol2) {
+    int r = ready(c);
+    if (r) return r;
+    if (!c->p.multiphase) return fail(c, MFLBM_EINVAL, "multiphase only");
+    const int nz = c->p.nz;
+    CK(c, cudaSetDevice(c->dev));
+    c->kt->saturation(c->st, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaMemcpyAsync(c->h_mon.data(), c->st.mon, sizeof(double) * 2 * nz, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nz; ++k) { a += c->h_mon[k]; b += c->h_mon[nz + k]; }
+    if (vol1) *vol1 = a;
+    if (vol2) *vol2 = b;
+    return MFLBM_OK;
+}
+
+int32_t mflbm_synchronize(mflbm_ctx *c) {
+    if (!c) return MFLBM_EINVAL;
+    CK(c, cudaSetDevice(c->dev));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// common.cuh -- device-side data layout shared by the kernels and the C-ABI layer.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+namespace mflbm {
+
+// D3Q19 lattice, multiphase_3D/0.src/Module.F90:111-114.  Used with compile-time q
+// (fully unrolled loops), so every call folds to a constant.
+__host__ __device__ constexpr int EX(int q) {
+    return (q == 1 || q == 7 || q == 9 || q == 11 || q == 13) ? 1
+         : (q == 2 || q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int EY(int q) {
+    return (q == 3 || q == 7 || q == 8 || q == 15 || q == 17) ? 1
+         : (q == 4 || q == 9 || q == 10 || q == 16 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int EZ(int q) {
+    return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
+         : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
+}
+// opposite direction (opc, Module.F90:114)
+__host__ __device__ constexpr int OPP(int q) {
+    return q == 1 ? 2 : q == 2 ? 1 : q == 3 ? 4 : q == 4 ? 3 : q == 5 ? 6 : q == 6 ? 5
+         : q == 7 ? 10 : q == 8 ? 9 : q == 9 ? 8 : q == 10 ? 7
+         : q == 11 ? 14 : q == 12 ? 13 : q == 13 ? 12 : q == 14 ? 11
+         : q == 15 ? 18 : q == 16 ? 17 : q == 17 ? 16 : q == 18 ? 15 : 0;
+}
+static_assert(OPP(9) == 8 && OPP(17) == 16 && OPP(0) == 0, "opposite table");
+static_assert(EX(OPP(13)) == -EX(13) && EZ(OPP(13)) == -EZ(13), "opposite table");
+
+// Device layout of the PDF arrays.
+// Each direction q is one SoA plane over the halo-1 box i,j,k in [0, n+1].  Rows are
+// padded so that interior node i=1 starts on a 32-byte boundary for every storage type:
+//   element(q,i,j,k) = q*qs + (i + xo) + pitch*j + pz*k,   pz = pitch*(ny+2)
+struct Layout {
+    int nx, ny, nz;
+    int xo;          // element offset of i=0 inside a row
+    int64_t pitch;   // row pitch in elements
+    int64_t pz;      // plane pitch in elements
+    int64_t qs;      // direction stride in elements
+    // Fortran-layout strides of the auxiliary arrays
+    int64_t h1x, h1xy;   // halo 1:  (nx+2), (nx+2)(ny+2)
+    int64_t h2x, h2xy;   // halo 2:  (nx+4), (nx+4)(ny+4)
+    int64_t h4x, h4xy;   // halo 4:  (nx+8), (nx+8)(ny+8)
+
+    __host__ __device__ __forceinline__ int64_t cell(int i, int j, int k) const {
+        return (int64_t)(i + xo) + pitch * j + pz * k;
+    }
+    __host__ __device__ __forceinline__ int64_t i1(int i, int j, int k) const { return (int64_t)i + h1x * j + h1xy * k; }
+    __host__ __device__ __forceinline__ int64_t i2(int i, int j, int k) const {
+        return (int64_t)(i + 1) + h2x * (j + 1) + h2xy * (k + 1);
+    }
+    __host__ __device__ __forceinline__ int64_t i4(int i, int j, int k) const {
+        return (int64_t)(i + 3) + h4x * (j + 3) + h4xy * (k + 3);
+    }
+    __host__ __device__ __forceinline__ int64_t ip(int i, int j) const { return (int64_t)i + h1x * j; }
+    __host__ __device__ __forceinline__ int64_t ic(int i, int j, int q) const { return (int64_t)i + h1x * j + h1xy * q; }
+};
+
+// Parameters read by the per-step kernels.
+struct StepParams {
+    double force_z;
+    double gamma, beta;
+    double la_nui1, la_nui2;
+    double sa_inject, phi_inlet;
+    double uin_avg, rho_in, rho_out, relaxation;
+    double s_e, s_e2, s_q, s_nu, s_pi, s_t;  // singlephase MRT rates
+    int mrt;                                 // multiphase `mrt` switch
+    int porous_plate_cmd, z_porous_plate;
+    int iper, jper, kper;
+};
+
+// One fluid-boundary node on the device: the host evaluates cos/sin of the local
+// contact angle once, so every step reuses them.
+struct FluidBnd {
+    int ix, iy, iz, pad;
+    double nwx, nwy, nwz, cos_t, sin_t;
+};
+
+struct SolidBnd {  // identical to mflbm_solid_bnd (96 bytes)
+    int ix, iy, iz, i_fluid_num;
+    int nbr[18];
+    double la_weight;
+};
+
+// FP16 deviation storage: value = w_q * ref + half_value * scale, ref = the rest
+// density of the species.
+template <class S> struct StoreTraits;
+template <> struct StoreTraits<double> { static constexpr int bytes = 8; };
+template <> struct StoreTraits<float> { static constexpr int bytes = 4; };
+template <> struct StoreTraits<__half> { static constexpr int bytes = 2; };
+
+}  // namespace mflbm

@@ -1,0 +1,1121 @@
+// kernels.cuh -- sm_103a kernels of the per-step lattice update.
+//
+// This header is compiled twice, once per floating-point flavour, inside namespace
+// mflbm::MFLBM_NS:
+//   kernels_fast.cu    (MFLBM_NS = fast)   default nvcc contraction of a*b+c into FMA
+//   kernels_strict.cu  (MFLBM_NS = strict) --fmad=false: every operation rounds on its
+//                      own, in the reference's written order, so results are
+//                      bit-identical to an IEEE FP64 restatement of the Fortran.
+// The host layer picks the flavour per context (mflbm_params.strict_fp).
+#pragma once
+#include "common.cuh"
+#include "kernels_api.h"
+
+namespace mflbm {
+namespace MFLBM_NS {
+
+// ---------------------------------------------------------------------------------
+// constants (multiphase_3D/0.src/Module.F90:116-131, 225-227)
+// ---------------------------------------------------------------------------------
+constexpr double mrt_coef1 = 1.0 / 19.0;
+constexpr double mrt_coef2 = 1.0 / 2394.0;
+constexpr double mrt_coef3 = 1.0 / 252.0;
+constexpr double mrt_coef4 = 1.0 / 72.0;
+constexpr double mrt_e2_coef1 = 0.0;
+constexpr double mrt_e2_coef2 = -475.0 / 63.0;
+constexpr double mrt_omega_xx = 0.0;
+constexpr double w_equ_0 = 1.0 / 3.0;
+constexpr double w_equ_1 = 1.0 / 18.0;
+constexpr double w_equ_2 = 1.0 / 36.0;
+constexpr double ISO4_1 = 1.0 / 6.0;
+constexpr double ISO4_2 = 1.0 / 12.0;
+
+__host__ __device__ constexpr double WEQ(int q) { return q == 0 ? w_equ_0 : (q <= 6 ? w_equ_1 : w_equ_2); }
+// Rest state of the reference MRT (its equilibrium energy-square moment is 0, so the
+// rest distribution is 4/21, 13/126, 1/63 rather than the BGK weights).  FP16 storage
+// keeps deviations from this state so that a fluid at rest stores zeros.
+__host__ __device__ constexpr double WREST(int q) { return q == 0 ? 4.0 / 21.0 : (q <= 6 ? 13.0 / 126.0 : 1.0 / 63.0); }
+
+// neighbour offset of direction q in the padded PDF layout
+__device__ __forceinline__ int64_t qoff(const Layout &L, int q) {
+    return (int64_t)EX(q) + (int64_t)EY(q) * L.pitch + (int64_t)EZ(q) * L.pz;
+}
+
+// ---------------------------------------------------------------------------------
+// PDF storage types.  FP64 and FP32 store the value; FP16 stores
+// (f_q - w_q * ref) * scale, i.e. a scaled deviation from the lattice weight.
+// ---------------------------------------------------------------------------------
+template <class S> struct Store;
+template <> struct Store<double> {
+    using R = double;
+    __device__ __forceinline__ static R ld(const double *p, int64_t o, R, R) { return p[o]; }
+    __device__ __forceinline__ static void st(double *p, int64_t o, R v, R, R) { p[o] = v; }
+};
+template <> struct Store<float> {
+    using R = float;
+    __device__ __forceinline__ static R ld(const float *p, int64_t o, R, R) { return p[o]; }
+    __device__ __forceinline__ static void st(float *p, int64_t o, R v, R, R) { p[o] = v; }
+};
+template <> struct Store<__half> {
+    using R = float;
+    // w_ref = w_q * ref density; sc = scale (store) / 1/scale (load)
+    __device__ __forceinline__ static R ld(const __half *p, int64_t o, R w_ref, R inv_scale) {
+        return w_ref + __half2float(p[o]) * inv_scale;
+    }
+    __device__ __forceinline__ static void st(__half *p, int64_t o, R v, R w_ref, R scale) {
+        p[o] = __float2half_rn((v - w_ref) * scale);
+    }
+};
+
+// ---------------------------------------------------------------------------------
+// MRT collision, the "MRT kernel, repeated part" of the reference
+// (multiphase_3D/0.src/Kernel_multiphase.F90:158-267, singlephase Kernel.F90:60-169),
+// in the written operation order.
+// ---------------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void mrt_collide(R (&ft)[19], R den, R fx, R fy, R fz, R s_e, R s_e2, R s_q, R s_nu, R s_pi,
+                                            R s_t) {
+    const R ux = ft[1] - ft[2] + ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14] + R(0.5) * fx;
+    const R uy = ft[3] - ft[4] + ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18] + R(0.5) * fy;
+    const R uz = ft[5] - ft[6] + ft[11] + ft[12] - ft[13] - ft[14] + ft[15] + ft[16] - ft[17] - ft[18] + R(0.5) * fz;
+    const R u2 = ux * ux + uy * uy + uz * uz;
+
+    R sum1 = ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6];
+    R sum2 = ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+    R sum3 = ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14];
+    R sum4 = ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18];
+    R sum5 = ft[11] + ft[12] - ft[13] - ft[14] + ft[15] + ft[16] - ft[17] - ft[18];
+    R sum6 = R(2.0) * (ft[1] + ft[2]) - ft[3] - ft[4] - ft[5] - ft[6];
+    R sum7 = ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] + ft[13] + ft[14] - R(2.0) * (ft[15] + ft[16] + ft[17] + ft[18]);
+    R sum8 = ft[3] + ft[4] - ft[5] - ft[6];
+    R sum9 = ft[7] + ft[8] + ft[9] + ft[10] - ft[11] - ft[12] - ft[13] - ft[14];
+
+    R m_rho = den;
+    R m_e = R(-30.0) * ft[0] - R(11.0) * sum1 + R(8.0) * sum2;
+    R m_e2 = R(12.0) * ft[0] - R(4.0) * sum1 + sum2;
+    R m_jx = ft[1] - ft[2] + sum3;
+    R m_qx = R(-4.0) * (ft[1] - ft[2]) + sum3;
+    R m_jy = ft[3] - ft[4] + sum4;
+    R m_qy = R(-4.0) * (ft[3] - ft[4]) + sum4;
+    R m_jz = ft[5] - ft[6] + sum5;
+    R m_qz = R(-4.0) * (ft[5] - ft[6]) + sum5;
+    R m_3pxx = sum6 + sum7;
+    R m_3pixx = R(-2.0) * sum6 + sum7;
+    R m_pww = sum8 + sum9;
+    R m_piww = R(-2.0) * sum8 + sum9;
+    R m_pxy = ft[7] - ft[8] - ft[9] + ft[10];
+    R m_pyz = ft[15] - ft[16] - ft[17] + ft[18];
+    R m_pzx = ft[11] - ft[12] - ft[13] + ft[14];
+    R m_tx = ft[7] - ft[8] + ft[9] - ft[10] - ft[11] + ft[12] - ft[13] + ft[14];
+    R m_ty = -ft[7] - ft[8] + ft[9] + ft[10] + ft[15] - ft[16] + ft[17] - ft[18];
+    R m_tz = ft[11] + ft[12] - ft[13] - ft[14] - ft[15] - ft[16] + ft[17] + ft[18];
+
+    const R c23 = R(-0.666666666666666667);
+    const R c13 = R(0.333333333333333333);
+    m_e = m_e - s_e * (m_e - (R(-11.0) * den + R(19.0) * u2)) + (R(38.0) - R(19.0) * s_e) * (fx * ux + fy * uy + fz * uz);
+    m_e2 = m_e2 - s_e2 * (m_e2 - (R(mrt_e2_coef1) * den + R(mrt_e2_coef2) * u2)) +
+           (R(-11.0) + R(5.5) * s_e2) * (fx * ux + fy * uy + fz * uz);
+    m_jx = m_jx + fx;
+    m_qx = m_qx - s_q * (m_qx - (c23 * ux)) + (c23 + c13 * s_q) * fx;
+    m_jy = m_jy + fy;
+    m_qy = m_qy - s_q * (m_qy - (c23 * uy)) + (c23 + c13 * s_q) * fy;
+    m_jz = m_jz + fz;
+    m_qz = m_qz - s_q * (m_qz - (c23 * uz)) + (c23 + c13 * s_q) * fz;
+
+    m_3pxx = m_3pxx - s_nu * (m_3pxx - (R(3.0) * ux * ux - u2)) + (R(2.0) - s_nu) * (R(2.0) * fx * ux - fy * uy - fz * uz);
+    m_3pixx = m_3pixx - s_pi * (m_3pixx - R(mrt_omega_xx) * (R(3.0) * ux * ux - u2)) +
+              (R(1.0) - R(0.5) * s_pi) * (R(-2.0) * fx * ux + fy * uy + fz * uz);
+    m_pww = m_pww - s_nu * (m_pww - (uy * uy - uz * uz)) + (R(2.0) - s_nu) * (fy * uy - fz * uz);
+    m_piww = m_piww - s_pi * (m_piww - R(mrt_omega_xx) * (uy * uy - uz * uz)) + (R(1.0) - R(0.5) * s_pi) * (-fy * uy + fz * uz);
+    m_pxy = m_pxy - s_nu * (m_pxy - (ux * uy)) + (R(1.0) - R(0.5) * s_nu) * (fx * uy + fy * ux);
+    m_pyz = m_pyz - s_nu * (m_pyz - (uy * uz)) + (R(1.0) - R(0.5) * s_nu) * (fy * uz + fz * uy);
+    m_pzx = m_pzx - s_nu * (m_pzx - (ux * uz)) + (R(1.0) - R(0.5) * s_nu) * (fx * uz + fz * ux);
+    m_tx = m_tx - s_t * (m_tx);
+    m_ty = m_ty - s_t * (m_ty);
+    m_tz = m_tz - s_t * (m_tz);
+
+    m_rho = R(mrt_coef1) * m_rho;
+    m_e = R(mrt_coef2) * m_e;
+    m_e2 = R(mrt_coef3) * m_e2;
+    m_jx = R(0.1) * m_jx;
+    m_qx = R(0.025) * m_qx;
+    m_jy = R(0.1) * m_jy;
+    m_qy = R(0.025) * m_qy;
+    m_jz = R(0.1) * m_jz;
+    m_qz = R(0.025) * m_qz;
+    m_3pxx = R(2.0 * mrt_coef4) * m_3pxx;
+    m_3pixx = R(mrt_coef4) * m_3pixx;
+    m_pww = R(6.0 * mrt_coef4) * m_pww;
+    m_piww = R(3.0 * mrt_coef4) * m_piww;
+    m_pxy = R(0.25) * m_pxy;
+    m_pyz = R(0.25) * m_pyz;
+    m_pzx = R(0.25) * m_pzx;
+    m_tx = R(0.125) * m_tx;
+    m_ty = R(0.125) * m_ty;
+    m_tz = R(0.125) * m_tz;
+    sum1 = m_rho - R(11.0) * m_e - R(4.0) * m_e2;
+    sum2 = R(2.0) * m_3pxx - R(4.0) * m_3pixx;
+    sum3 = m_pww - R(2.0) * m_piww;
+    sum4 = m_rho + R(8.0) * m_e + m_e2;
+    sum5 = m_jx + m_qx;
+    sum6 = m_jy + m_qy;
+    sum7 = m_jz + m_qz;
+    sum8 = m_3pxx + m_3pixx;
+    sum9 = m_pww + m_piww;
+
+    ft[0] = m_rho - R(30.0) * m_e + R(12.0) * m_e2;
+    ft[1] = sum1 + m_jx - R(4.0) * m_qx + sum2;
+    ft[2] = sum1 - m_jx + R(4.0) * m_qx + sum2;
+    ft[3] = sum1 + m_jy - R(4.0) * m_qy - R(0.5) * sum2 + sum3;
+    ft[4] = sum1 - m_jy + R(4.0) * m_qy - R(0.5) * sum2 + sum3;
+    ft[5] = sum1 + m_jz - R(4.0) * m_qz - R(0.5) * sum2 - sum3;
+    ft[6] = sum1 - m_jz + R(4.0) * m_qz - R(0.5) * sum2 - sum3;
+    ft[7] = sum4 + sum5 + sum6 + sum8 + sum9 + m_pxy + m_tx - m_ty;
+    ft[8] = sum4 - sum5 + sum6 + sum8 + sum9 - m_pxy - m_tx - m_ty;
+    ft[9] = sum4 + sum5 - sum6 + sum8 + sum9 - m_pxy + m_tx + m_ty;
+    ft[10] = sum4 - sum5 - sum6 + sum8 + sum9 + m_pxy - m_tx + m_ty;
+    ft[11] = sum4 + sum5 + sum7 + sum8 - sum9 + m_pzx - m_tx + m_tz;
+    ft[12] = sum4 - sum5 + sum7 + sum8 - sum9 - m_pzx + m_tx + m_tz;
+    ft[13] = sum4 + sum5 - sum7 + sum8 - sum9 - m_pzx - m_tx - m_tz;
+    ft[14] = sum4 - sum5 - sum7 + sum8 - sum9 + m_pzx + m_tx - m_tz;
+    ft[15] = sum4 + sum6 + sum7 - sum8 * R(2.0) + m_pyz + m_ty - m_tz;
+    ft[16] = sum4 - sum6 + sum7 - sum8 * R(2.0) - m_pyz - m_ty - m_tz;
+    ft[17] = sum4 + sum6 - sum7 - sum8 * R(2.0) - m_pyz + m_ty + m_tz;
+    ft[18] = sum4 - sum6 - sum7 - sum8 * R(2.0) + m_pyz - m_ty + m_tz;
+}
+
+// ---------------------------------------------------------------------------------
+// singlephase kernel_even / kernel_odd (singlephase_3D/0.src/Kernel.F90:5-400).
+// One thread per interior node; solid nodes are skipped, so their slots carry the
+// implicit full-way bounce-back of the AA pattern.
+// odd : ft_q <- f_q(x - e_q) ... f_opp(q)(x + e_q) <- ft_q
+// even: ft_q <- f_opp(q)(x)  ... f_q(x) <- ft_q
+// ---------------------------------------------------------------------------------
+template <class S, bool ODD>
+__global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int8_t *__restrict__ walls, const Layout L,
+                                                 const StepParams P, const float ref, const float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > L.nx || j > L.ny) return;
+    if (walls[L.i2(i, j, k)] != 0) return;
+    const int64_t c = L.cell(i, j, k);
+    const R inv_scale = R(1.0f / scale);
+    R ft[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        if (ODD)
+            ft[q] = St::ld(f, (int64_t)q * L.qs + c - qoff(L, q), R(WREST(q) * ref), inv_scale);
+        else
+            ft[q] = St::ld(f, (int64_t)OPP(q) * L.qs + c, R(WREST(q) * ref), inv_scale);
+    }
+    const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
+                  ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+    mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
+    const R sc = R(scale);
+    if (ODD) {
+        St::st(f, c, ft[0], R(WREST(0) * ref), sc);
+#pragma unroll
+        for (int q = 1; q < 19; ++q) St::st(f, (int64_t)OPP(q) * L.qs + c + qoff(L, q), ft[q], R(WREST(q) * ref), sc);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) St::st(f, (int64_t)q * L.qs + c, ft[q], R(WREST(q) * ref), sc);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// multiphase kernel_even_color / kernel_odd_color
+// (multiphase_3D/0.src/Kernel_multiphase.F90:6-725): total-PDF MRT collision with the
+// CSF force, viscosity interpolation in 1/nu, R-K recolouring into f (fluid 1) and
+// g (fluid 2), phi written for the gradient pass.
+// ---------------------------------------------------------------------------------
+template <bool ODD>
+__global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double *__restrict__ g, double *__restrict__ phi,
+                                                 const double *__restrict__ cnx, const double *__restrict__ cny,
+                                                 const double *__restrict__ cnz, const double *__restrict__ cnorm,
+                                                 const double *__restrict__ curv, const int8_t *__restrict__ walls,
+                                                 const Layout L, const StepParams P, const double rk_weight2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > L.nx || j > L.ny) return;
+    const int64_t w2 = L.i2(i, j, k);
+    if (walls[w2] != 0) return;
+    const int64_t c = L.cell(i, j, k);
+    double ft[19];
+    double rho1, rho2;
+    // pull (odd) or local swapped read (even); rho1/rho2 accumulate in the written order
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const double a = ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c];
+        ft[q] = a;
+        rho1 = q == 0 ? a : rho1 + a;
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const double b = ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c];
+        ft[q] = ft[q] + b;
+        rho2 = q == 0 ? b : rho2 + b;
+    }
+    const double ph = (rho1 - rho2) / (rho1 + rho2);
+    phi[L.i4(i, j, k)] = ph;
+    const double cx = cnx[w2], cy = cny[w2], cz = cnz[w2];
+    double tmp = 0.5 * P.gamma * curv[L.i1(i, j, k)] * cnorm[w2];
+    const double fx = tmp * cx;
+    const double fy = tmp * cy;
+    const double fz = tmp * cz + P.force_z;
+    const double omega = 1.0 / (6.0 / ((1.0 + ph) * P.la_nui1 + (1.0 - ph) * P.la_nui2) + 0.5);
+    double s_e, s_e2, s_pi, s_q, s_t;
+    if (P.mrt == 1) {
+        s_e = omega; s_e2 = omega; s_pi = omega;
+        s_q = 8.0 * (2.0 - omega) / (8.0 - omega);
+        s_t = s_q;
+    } else if (P.mrt == 3) {
+        s_e = omega; s_e2 = omega; s_pi = omega; s_q = omega; s_t = omega;
+    } else if (P.mrt == 4) {
+        s_e = omega; s_e2 = omega; s_pi = omega;
+        s_q = (6.0 - 3.0 * omega) / (3.0 - omega);
+        s_t = omega;
+    } else {
+        s_e = 1.19; s_e2 = 1.4; s_pi = 1.4; s_q = 1.2; s_t = 1.98;
+    }
+    const double den = rho1 + rho2;
+    mrt_collide<double>(ft, den, fx, fy, fz, s_e, s_e2, s_q, omega, s_pi, s_t);
+    // recolouring (Kernel_multiphase.F90:272-315)
+    const double tmp1 = rho1 / den;
+    tmp = rho1 * rho2 * P.beta / den;
+    const double a0 = tmp1 * ft[0];
+    const double b0 = ft[0] * (1.0 - tmp1);
+    f[c] = a0;
+    g[c] = b0;
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        const double ex = (double)EX(q), ey = (double)EY(q), ez = (double)EZ(q);
+        double proj;
+        // the reference writes each projection as a signed sum of the two non-zero
+        // components in x, y, z order, e.g. (-cnx + cny)
+        if (q <= 6)
+            proj = EX(q) != 0 ? ex * cx : (EY(q) != 0 ? ey * cy : ez * cz);
+        else if (EZ(q) == 0)
+            proj = ex * cx + ey * cy;
+        else if (EY(q) == 0)
+            proj = ex * cx + ez * cz;
+        else
+            proj = ey * cy + ez * cz;
+        const double wq = q <= 6 ? w_equ_1 : rk_weight2;
+        const double a = tmp1 * ft[q] + wq * tmp * (proj);
+        const double b = ft[q] - a;
+        const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
+        f[o] = a;
+        g[o] = b;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Periodic halo exchange (single-device form of Mpi.F90:101-598).  Faces copy the five
+// PDFs that cross the face over the interior tangential range; the edge kernel then
+// copies the one PDF per edge, and must run after the faces (it overrides four slots
+// that two face copies also write in the push direction, Mpi.F90:417-431).
+// ---------------------------------------------------------------------------------
+__device__ __constant__ int c_plus[3][5] = {{1, 7, 9, 11, 13}, {3, 7, 8, 15, 17}, {5, 11, 12, 15, 16}};
+__device__ __constant__ int c_minus[3][5] = {{2, 8, 10, 12, 14}, {4, 10, 9, 16, 18}, {6, 14, 13, 18, 17}};
+
+// one thread per (face cell, species); dim 0=x, 1=y, 2=z
+template <class S>
+__global__ void k_wrap_faces(S *__restrict__ f, int nspecies, const Layout L, int dim, int pull) {
+    const int64_t n1 = dim == 0 ? L.ny : L.nx;  // fastest tangential extent
+    const int64_t n2 = dim == 2 ? L.ny : L.nz;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2 * nspecies) return;
+    const int s = (int)(t / (n1 * n2));
+    const int64_t r = t % (n1 * n2);
+    const int a = (int)(r % n1) + 1, b = (int)(r / n1) + 1;
+    S *A = f + (int64_t)s * 19 * L.qs;
+    const int n = dim == 0 ? L.nx : (dim == 1 ? L.ny : L.nz);
+    auto cell = [&](int layer) -> int64_t {
+        if (dim == 0) return L.cell(layer, a, b);
+        if (dim == 1) return L.cell(a, layer, b);
+        return L.cell(a, b, layer);
+    };
+    if (pull) {
+        // ghost 0 <- interior n for the + set; ghost n+1 <- interior 1 for the - set
+        const int64_t g0 = cell(0), in_n = cell(n), g1 = cell(n + 1), in_1 = cell(1);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            const int qp = c_plus[dim][m], qm = c_minus[dim][m];
+            A[(int64_t)qp * L.qs + g0] = A[(int64_t)qp * L.qs + in_n];
+            A[(int64_t)qm * L.qs + g1] = A[(int64_t)qm * L.qs + in_1];
+        }
+    } else {
+        // interior 1 <- ghost n+1 for the - set; interior n <- ghost 0 for the + set
+        const int64_t g0 = cell(0), in_n = cell(n), g1 = cell(n + 1), in_1 = cell(1);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            const int qp = c_plus[dim][m], qm = c_minus[dim][m];
+            A[(int64_t)qm * L.qs + in_1] = A[(int64_t)qm * L.qs + g1];
+            A[(int64_t)qp * L.qs + in_n] = A[(int64_t)qp * L.qs + g0];
+        }
+    }
+}
+
+// edges: along x when y and z are periodic (the reference's case), along y (x,z) and
+// along z (x,y) for the x-periodic extension.  One thread per edge cell and species.
+template <class S>
+__global__ void k_wrap_edges(S *__restrict__ f, int nspecies, const Layout L, int axis, int pull) {
+    const int n = axis == 0 ? L.nx : (axis == 1 ? L.ny : L.nz);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n * nspecies) return;
+    const int s = (int)(t / n);
+    const int a = (int)(t % n) + 1;
+    S *A = f + (int64_t)s * 19 * L.qs;
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    auto X = [&](int q, int i, int j, int k) -> S & { return A[(int64_t)q * L.qs + L.cell(i, j, k)]; };
+    if (axis == 0) {  // y,z periodic; i = a
+        const int i = a;
+        if (pull) {
+            X(18, i, ny + 1, nz + 1) = X(18, i, 1, 1);
+            X(16, i, ny + 1, 0) = X(16, i, 1, nz);
+            X(17, i, 0, nz + 1) = X(17, i, ny, 1);
+            X(15, i, 0, 0) = X(15, i, ny, nz);
+        } else {
+            X(15, i, ny, nz) = X(15, i, 0, 0);
+            X(17, i, ny, 1) = X(17, i, 0, nz + 1);
+            X(16, i, 1, nz) = X(16, i, ny + 1, 0);
+            X(18, i, 1, 1) = X(18, i, ny + 1, nz + 1);
+        }
+    } else if (axis == 1) {  // x,z periodic; j = a
+        const int j = a;
+        if (pull) {
+            X(11, 0, j, 0) = X(11, nx, j, nz);
+            X(12, nx + 1, j, 0) = X(12, 1, j, nz);
+            X(13, 0, j, nz + 1) = X(13, nx, j, 1);
+            X(14, nx + 1, j, nz + 1) = X(14, 1, j, 1);
+        } else {
+            X(11, nx, j, nz) = X(11, 0, j, 0);
+            X(12, 1, j, nz) = X(12, nx + 1, j, 0);
+            X(13, nx, j, 1) = X(13, 0, j, nz + 1);
+            X(14, 1, j, 1) = X(14, nx + 1, j, nz + 1);
+        }
+    } else {  // x,y periodic; k = a
+        const int k = a;
+        if (pull) {
+            X(7, 0, 0, k) = X(7, nx, ny, k);
+            X(8, nx + 1, 0, k) = X(8, 1, ny, k);
+            X(9, 0, ny + 1, k) = X(9, nx, 1, k);
+            X(10, nx + 1, ny + 1, k) = X(10, 1, 1, k);
+        } else {
+            X(7, nx, ny, k) = X(7, 0, 0, k);
+            X(8, 1, ny, k) = X(8, nx + 1, 0, k);
+            X(9, nx, 1, k) = X(9, 0, ny + 1, k);
+            X(10, 1, 1, k) = X(10, nx + 1, ny + 1, k);
+        }
+    }
+}
+
+// phi halo, 4 layers (MPI_phi_async_pack / MPI_phi_sync_update, Mpi.F90:608-867):
+// z faces (i,j interior), y faces (i,k interior), x-edges; sources are all interior.
+__global__ void k_wrap_phi(double *__restrict__ phi, const Layout L, int py, int pz) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    const int64_t nzf = pz ? (int64_t)4 * nx * ny : 0;
+    const int64_t nyf = py ? (int64_t)4 * nx * nz : 0;
+    const int64_t ned = (py && pz) ? (int64_t)16 * nx : 0;
+    if (t < nzf) {
+        const int i = (int)(t % nx) + 1;
+        const int j = (int)((t / nx) % ny) + 1;
+        const int k = (int)(t / ((int64_t)nx * ny)) + 1;
+        phi[L.i4(i, j, k - 4)] = phi[L.i4(i, j, nz + k - 4)];
+        phi[L.i4(i, j, k + nz)] = phi[L.i4(i, j, k)];
+        return;
+    }
+    int64_t u = t - nzf;
+    if (u < nyf) {
+        const int i = (int)(u % nx) + 1;
+        const int j = (int)((u / nx) % 4) + 1;
+        const int k = (int)(u / ((int64_t)nx * 4)) + 1;
+        phi[L.i4(i, j - 4, k)] = phi[L.i4(i, ny + j - 4, k)];
+        phi[L.i4(i, j + ny, k)] = phi[L.i4(i, j, k)];
+        return;
+    }
+    u -= nyf;
+    if (u < ned) {
+        const int i = (int)(u % nx) + 1;
+        const int j = (int)((u / nx) % 4) + 1;
+        const int k = (int)(u / ((int64_t)nx * 4)) + 1;
+        phi[L.i4(i, j - 4, k - 4)] = phi[L.i4(i, ny + j - 4, nz + k - 4)];
+        phi[L.i4(i, j + ny, k - 4)] = phi[L.i4(i, j, nz + k - 4)];
+        phi[L.i4(i, j + ny, k + nz)] = phi[L.i4(i, j, k)];
+        phi[L.i4(i, j - 4, k + nz)] = phi[L.i4(i, ny + j - 4, k)];
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Inlet / outlet boundary conditions on the z planes; one thread per (i,j).
+// The reference's masking x*(1-w) + y*w is kept literally.
+// ---------------------------------------------------------------------------------
+template <class R> __device__ __forceinline__ R sel(R x, R y, int w) { return x * (R)(1 - w) + y * (R)w; }
+
+// velocity inlet (Boundary_multiphase_inlet.F90:6-102; singlephase Boundary.F90:5-73)
+template <class S>
+__global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+                                 const int8_t *__restrict__ walls, const double *__restrict__ w_in, const Layout L,
+                                 const StepParams P, int before_odd, int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1;
+    if (i > L.nx) return;
+    const int wi = walls[L.i2(i, j, 1)];
+    if (multiphase) {
+        const double p0 = P.phi_inlet * (double)(1 - wi) + phi[L.i4(i, j, 0)] * (double)wi;
+        phi[L.i4(i, j, 0)] = p0;
+        phi[L.i4(i, j, -1)] = p0;
+        phi[L.i4(i, j, -2)] = p0;
+        phi[L.i4(i, j, -3)] = p0;
+    }
+    double tmp2 = w_in[L.ip(i, j)] * P.relaxation;
+    double tmp1;
+    if (multiphase) {
+        tmp1 = tmp2 * P.sa_inject;
+        tmp2 = tmp2 - tmp1;
+    } else {
+        tmp1 = tmp2;
+    }
+    const R inv = R(1.0f / scale), sc = R(scale);
+    for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
+        S *A = s == 0 ? f : g;
+        const R t = R(s == 0 ? tmp1 : tmp2);
+        const float rf = ref;
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        const R c1 = R(6.0 * w_equ_1), c2 = R(6.0 * w_equ_2);
+        if (before_odd) {
+            st(5, i, j, 0, sel<R>(ld(6, i, j, 1) + c1 * t, ld(5, i, j, 0), wi));
+            st(11, i - 1, j, 0, sel<R>(ld(14, i, j, 1) + c2 * t, ld(11, i - 1, j, 0), wi));
+            st(12, i + 1, j, 0, sel<R>(ld(13, i, j, 1) + c2 * t, ld(12, i + 1, j, 0), wi));
+            st(15, i, j - 1, 0, sel<R>(ld(18, i, j, 1) + c2 * t, ld(15, i, j - 1, 0), wi));
+            st(16, i, j + 1, 0, sel<R>(ld(17, i, j, 1) + c2 * t, ld(16, i, j + 1, 0), wi));
+        } else {
+            st(6, i, j, 1, sel<R>(ld(5, i, j, 0) + c1 * t, ld(6, i, j, 1), wi));
+            st(13, i, j, 1, sel<R>(ld(12, i + 1, j, 0) + c2 * t, ld(13, i, j, 1), wi));
+            st(14, i, j, 1, sel<R>(ld(11, i - 1, j, 0) + c2 * t, ld(14, i, j, 1), wi));
+            st(17, i, j, 1, sel<R>(ld(16, i, j + 1, 0) + c2 * t, ld(17, i, j, 1), wi));
+            st(18, i, j, 1, sel<R>(ld(15, i, j - 1, 0) + c2 * t, ld(18, i, j, 1), wi));
+        }
+    }
+}
+
+// Zou-He pressure inlet (Boundary_multiphase_inlet.F90:115-294; Boundary.F90:80-187)
+template <class S>
+__global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+                              const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                              int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1;
+    if (i > L.nx) return;
+    const int wi = walls[L.i2(i, j, 1)];
+    double rhos[2];
+    if (multiphase) {
+        const double p0 = P.phi_inlet * (double)(1 - wi) + phi[L.i4(i, j, 0)] * (double)wi;
+        phi[L.i4(i, j, 0)] = p0;
+        phi[L.i4(i, j, -1)] = p0;
+        phi[L.i4(i, j, -2)] = p0;
+        phi[L.i4(i, j, -3)] = p0;
+        double tmpRho2 = P.rho_in;
+        const double tmpRho1 = P.rho_in * P.sa_inject;
+        tmpRho2 = tmpRho2 - tmpRho1;
+        rhos[0] = tmpRho1;
+        rhos[1] = tmpRho2;
+    } else {
+        rhos[0] = P.rho_in;
+        rhos[1] = 0.0;
+    }
+    const R inv = R(1.0f / scale), sc = R(scale);
+    for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
+        S *A = s == 0 ? f : g;
+        const float rf = ref;
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        const R c3 = R(0.333333333333333333), c6 = R(0.166666666666666667);
+        if (before_odd) {
+            const R t = (R(rhos[s]) - (ld(0, i, j, 1) + ld(1, i - 1, j, 1) + ld(2, i + 1, j, 1) + ld(3, i, j - 1, 1) +
+                                       ld(4, i, j + 1, 1) + ld(7, i - 1, j - 1, 1) + ld(8, i + 1, j - 1, 1) +
+                                       ld(9, i - 1, j + 1, 1) + ld(10, i + 1, j + 1, 1) +
+                                       R(2.0) * (ld(6, i, j, 2) + ld(14, i + 1, j, 2) + ld(13, i - 1, j, 2) +
+                                                 ld(18, i, j + 1, 2) + ld(17, i, j - 1, 2)))) *
+                        R(P.relaxation);
+            const R tnx = R(0.5) * (ld(1, i - 1, j, 1) + ld(7, i - 1, j - 1, 1) + ld(9, i - 1, j + 1, 1) -
+                                    (ld(2, i + 1, j, 1) + ld(8, i + 1, j - 1, 1) + ld(10, i + 1, j + 1, 1)));
+            const R tny = R(0.5) * (ld(3, i, j - 1, 1) + ld(7, i - 1, j - 1, 1) + ld(8, i + 1, j - 1, 1) -
+                                    (ld(4, i, j + 1, 1) + ld(10, i + 1, j + 1, 1) + ld(9, i - 1, j + 1, 1)));
+            st(5, i, j, 0, sel<R>(ld(6, i, j, 2) + c3 * t, ld(5, i, j, 0), wi));
+            st(11, i - 1, j, 0, sel<R>(ld(14, i + 1, j, 2) + c6 * t - tnx, ld(11, i - 1, j, 0), wi));
+            st(12, i + 1, j, 0, sel<R>(ld(13, i - 1, j, 2) + c6 * t + tnx, ld(12, i + 1, j, 0), wi));
+            st(15, i, j - 1, 0, sel<R>(ld(18, i, j + 1, 2) + c6 * t - tny, ld(15, i, j - 1, 0), wi));
+            st(16, i, j + 1, 0, sel<R>(ld(17, i, j - 1, 2) + c6 * t + tny, ld(16, i, j + 1, 0), wi));
+        } else {
+            const R t = (R(rhos[s]) - (ld(0, i, j, 1) + ld(2, i, j, 1) + ld(1, i, j, 1) + ld(4, i, j, 1) + ld(3, i, j, 1) +
+                                       ld(8, i, j, 1) + ld(7, i, j, 1) + ld(10, i, j, 1) + ld(9, i, j, 1) +
+                                       R(2.0) * (ld(5, i, j, 1) + ld(11, i, j, 1) + ld(12, i, j, 1) + ld(15, i, j, 1) +
+                                                 ld(16, i, j, 1)))) *
+                        R(P.relaxation);
+            const R tnx = R(0.5) * (ld(2, i, j, 1) + ld(8, i, j, 1) + ld(10, i, j, 1) - (ld(1, i, j, 1) + ld(7, i, j, 1) + ld(9, i, j, 1)));
+            const R tny = R(0.5) * (ld(4, i, j, 1) + ld(9, i, j, 1) + ld(10, i, j, 1) - (ld(3, i, j, 1) + ld(8, i, j, 1) + ld(7, i, j, 1)));
+            st(6, i, j, 1, sel<R>(ld(5, i, j, 1) + c3 * t, ld(6, i, j, 1), wi));
+            st(13, i, j, 1, sel<R>(ld(12, i, j, 1) + c6 * t + tnx, ld(13, i, j, 1), wi));
+            st(14, i, j, 1, sel<R>(ld(11, i, j, 1) + c6 * t - tnx, ld(14, i, j, 1), wi));
+            st(17, i, j, 1, sel<R>(ld(16, i, j, 1) + c6 * t + tny, ld(17, i, j, 1), wi));
+            st(18, i, j, 1, sel<R>(ld(15, i, j, 1) + c6 * t - tny, ld(18, i, j, 1), wi));
+        }
+    }
+}
+
+// convective outlet (Boundary_multiphase_outlet.F90:7-127; Boundary.F90:196-276)
+template <class S>
+__global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+                                    double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
+                                    const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                                    int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1;
+    if (i > L.nx) return;
+    const int nz = L.nz;
+    const int wi = walls[L.i2(i, j, nz)];
+    const double u_convec = P.uin_avg;
+    const double temp = 1.0 / (1.0 + u_convec);
+    if (multiphase) {
+        const double p1 = ((phiconv[L.ip(i, j)] + u_convec * phi[L.i4(i, j, nz)]) * temp) * (double)(1 - wi) +
+                          phi[L.i4(i, j, nz + 1)] * (double)wi;
+        phi[L.i4(i, j, nz + 1)] = p1;
+        phiconv[L.ip(i, j)] = p1;
+        phi[L.i4(i, j, nz + 2)] = p1;
+        phi[L.i4(i, j, nz + 3)] = p1;
+        phi[L.i4(i, j, nz + 4)] = p1;
+    }
+    const R inv = R(1.0f / scale), sc = R(scale);
+    const R uc = R(u_convec), tp = R(temp);
+    for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
+        S *A = s == 0 ? f : g;
+        double *C = s == 0 ? fconv : gconv;
+        const float rf = ref;
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        auto cv = [&](int q) -> double & { return C[L.ic(i, j, q)]; };
+        if (before_odd) {
+            st(6, i, j, nz + 1, sel<R>((R(cv(6)) + uc * ld(6, i, j, nz)) * tp, ld(6, i, j, nz + 1), wi));
+            st(13, i - 1, j, nz + 1, sel<R>((R(cv(13)) + uc * ld(13, i - 1, j, nz)) * tp, ld(13, i - 1, j, nz + 1), wi));
+            st(14, i + 1, j, nz + 1, sel<R>((R(cv(14)) + uc * ld(14, i + 1, j, nz)) * tp, ld(14, i + 1, j, nz + 1), wi));
+            st(17, i, j - 1, nz + 1, sel<R>((R(cv(17)) + uc * ld(17, i, j - 1, nz)) * tp, ld(17, i, j - 1, nz + 1), wi));
+            st(18, i, j + 1, nz + 1, sel<R>((R(cv(18)) + uc * ld(18, i, j + 1, nz)) * tp, ld(18, i, j + 1, nz + 1), wi));
+            cv(6) = ld(6, i, j, nz + 1);
+            cv(13) = ld(13, i - 1, j, nz + 1);
+            cv(14) = ld(14, i + 1, j, nz + 1);
+            cv(17) = ld(17, i, j - 1, nz + 1);
+            cv(18) = ld(18, i, j + 1, nz + 1);
+        } else {
+            st(5, i, j, nz, sel<R>((R(cv(6)) + uc * ld(5, i, j, nz - 1)) * tp, ld(5, i, j, nz), wi));
+            st(11, i, j, nz, sel<R>((R(cv(14)) + uc * ld(11, i, j, nz - 1)) * tp, ld(11, i, j, nz), wi));
+            st(12, i, j, nz, sel<R>((R(cv(13)) + uc * ld(12, i, j, nz - 1)) * tp, ld(12, i, j, nz), wi));
+            st(15, i, j, nz, sel<R>((R(cv(18)) + uc * ld(15, i, j, nz - 1)) * tp, ld(15, i, j, nz), wi));
+            st(16, i, j, nz, sel<R>((R(cv(17)) + uc * ld(16, i, j, nz - 1)) * tp, ld(16, i, j, nz), wi));
+            cv(6) = ld(5, i, j, nz);
+            cv(14) = ld(11, i, j, nz);
+            cv(13) = ld(12, i, j, nz);
+            cv(18) = ld(15, i, j, nz);
+            cv(17) = ld(16, i, j, nz);
+        }
+    }
+}
+
+// Zou-He pressure outlet (Boundary_multiphase_outlet.F90:139-311; Boundary.F90:284-389)
+template <class S>
+__global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+                               const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                               int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1;
+    if (i > L.nx) return;
+    const int nz = L.nz;
+    const int wi = walls[L.i2(i, j, nz)];
+    double phin = 0.0;
+    if (multiphase) {
+        phin = phi[L.i4(i, j, nz)];
+        phi[L.i4(i, j, nz + 1)] = phin;
+        phi[L.i4(i, j, nz + 2)] = phin;
+        phi[L.i4(i, j, nz + 3)] = phin;
+        phi[L.i4(i, j, nz + 4)] = phin;
+    }
+    const R inv = R(1.0f / scale), sc = R(scale);
+    const float rf = ref;
+    auto LD = [&](S *A, int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
+    R t1;
+    for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
+        S *A = s == 0 ? f : g;
+        auto ld = [&](int q, int ii, int jj, int kk) { return LD(A, q, ii, jj, kk); };
+        if (before_odd) {
+            const R part = ld(0, i, j, nz) + ld(1, i - 1, j, nz) + ld(2, i + 1, j, nz) + ld(3, i, j - 1, nz);
+            // keep one left-to-right chain across both species, as the reference writes it
+            R acc = s == 0 ? part : t1 + ld(0, i, j, nz) + ld(1, i - 1, j, nz) + ld(2, i + 1, j, nz) + ld(3, i, j - 1, nz);
+            acc = acc + ld(4, i, j + 1, nz) + ld(7, i - 1, j - 1, nz) + ld(8, i + 1, j - 1, nz) + ld(9, i - 1, j + 1, nz) +
+                  ld(10, i + 1, j + 1, nz) +
+                  R(2.0) * (ld(5, i, j, nz - 1) + ld(11, i - 1, j, nz - 1) + ld(12, i + 1, j, nz - 1) +
+                            ld(15, i, j - 1, nz - 1) + ld(16, i, j + 1, nz - 1));
+            t1 = acc;
+        } else {
+            const R part = ld(0, i, j, nz) + ld(2, i, j, nz) + ld(1, i, j, nz) + ld(4, i, j, nz);
+            R acc = s == 0 ? part : t1 + ld(0, i, j, nz) + ld(2, i, j, nz) + ld(1, i, j, nz) + ld(4, i, j, nz);
+            acc = acc + ld(3, i, j, nz) + ld(8, i, j, nz) + ld(7, i, j, nz) + ld(10, i, j, nz) + ld(9, i, j, nz) +
+                  R(2.0) * (ld(6, i, j, nz) + ld(14, i, j, nz) + ld(13, i, j, nz) + ld(18, i, j, nz) + ld(17, i, j, nz));
+            t1 = acc;
+        }
+    }
+    t1 = t1 - R(P.rho_out);
+    R t2 = R(0.0);
+    if (multiphase) {
+        t2 = t1 * R(0.5) * (R(1.0) - R(phin));
+        t1 = t1 - t2;
+    }
+    const R c3 = R(0.333333333333333333), c6 = R(0.166666666666666667);
+    const R w1 = R(1.0) - (R)wi, w0 = (R)wi;
+    for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
+        S *A = s == 0 ? f : g;
+        const R t = s == 0 ? t1 : t2;
+        auto ld = [&](int q, int ii, int jj, int kk) { return LD(A, q, ii, jj, kk); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        if (before_odd) {
+            const R tnx = R(0.5) * (ld(1, i - 1, j, nz) + ld(7, i - 1, j - 1, nz) + ld(9, i - 1, j + 1, nz) -
+                                    (ld(2, i + 1, j, nz) + ld(8, i + 1, j - 1, nz) + ld(10, i + 1, j + 1, nz)));
+            const R tny = R(0.5) * (ld(3, i, j - 1, nz) + ld(7, i - 1, j - 1, nz) + ld(8, i + 1, j - 1, nz) -
+                                    (ld(4, i, j + 1, nz) + ld(10, i + 1, j + 1, nz) + ld(9, i - 1, j + 1, nz)));
+            st(6, i, j, nz + 1, (ld(5, i, j, nz - 1) - c3 * t) * w1 + ld(6, i, j, nz + 1) * w0);
+            st(13, i - 1, j, nz + 1, (ld(12, i + 1, j, nz - 1) - c6 * t - tnx) * w1 + ld(13, i - 1, j, nz + 1) * w0);
+            st(14, i + 1, j, nz + 1, (ld(11, i - 1, j, nz - 1) - c6 * t + tnx) * w1 + ld(14, i + 1, j, nz + 1) * w0);
+            st(17, i, j - 1, nz + 1, (ld(16, i, j + 1, nz - 1) - c6 * t - tny) * w1 + ld(17, i, j - 1, nz + 1) * w0);
+            st(18, i, j + 1, nz + 1, (ld(15, i, j - 1, nz - 1) - c6 * t + tny) * w1 + ld(18, i, j + 1, nz + 1) * w0);
+        } else {
+            const R tnx = R(0.5) * (ld(2, i, j, nz) + ld(8, i, j, nz) + ld(10, i, j, nz) - (ld(1, i, j, nz) + ld(7, i, j, nz) + ld(9, i, j, nz)));
+            const R tny = R(0.5) * (ld(4, i, j, nz) + ld(10, i, j, nz) + ld(9, i, j, nz) - (ld(3, i, j, nz) + ld(7, i, j, nz) + ld(8, i, j, nz)));
+            st(5, i, j, nz, (ld(6, i, j, nz) - c3 * t) * w1 + ld(5, i, j, nz) * w0);
+            st(11, i, j, nz, (ld(14, i, j, nz) - c6 * t + tnx) * w1 + ld(11, i, j, nz) * w0);
+            st(12, i, j, nz, (ld(13, i, j, nz) - c6 * t - tnx) * w1 + ld(12, i, j, nz) * w0);
+            st(15, i, j, nz, (ld(18, i, j, nz) - c6 * t + tny) * w1 + ld(15, i, j, nz) * w0);
+            st(16, i, j, nz, (ld(17, i, j, nz) - c6 * t - tny) * w1 + ld(16, i, j, nz) * w0);
+        }
+    }
+}
+
+// porous plate (Boundary_multiphase_other.F90:8-184); blocked = the species that is
+// reflected, passing = the species copied across.
+__global__ void k_porous_plate(double *__restrict__ blocked, double *__restrict__ passing, const Layout L, int z,
+                               int before_odd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1;
+    if (i > L.nx) return;
+    auto b = [&](int q, int ii, int jj, int kk) -> double & { return blocked[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
+    auto c = [&](int q, int ii, int jj, int kk) -> double & { return passing[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
+    if (before_odd) {
+        b(6, i, j, z) = b(5, i, j, z - 1);
+        b(13, i - 1, j, z) = b(12, i, j, z - 1);
+        b(14, i + 1, j, z) = b(11, i, j, z - 1);
+        b(17, i, j - 1, z) = b(16, i, j, z - 1);
+        b(18, i, j + 1, z) = b(15, i, j, z - 1);
+        b(5, i, j, z) = b(6, i, j, z + 1);
+        b(12, i + 1, j, z) = b(13, i, j, z + 1);
+        b(11, i - 1, j, z) = b(14, i, j, z + 1);
+        b(16, i, j + 1, z) = b(17, i, j, z + 1);
+        b(15, i, j - 1, z) = b(18, i, j, z + 1);
+        c(6, i, j, z) = c(6, i, j, z + 1);
+        c(13, i, j, z) = c(13, i, j, z + 1);
+        c(14, i, j, z) = c(14, i, j, z + 1);
+        c(17, i, j, z) = c(17, i, j, z + 1);
+        c(18, i, j, z) = c(18, i, j, z + 1);
+        c(5, i, j, z) = c(5, i, j, z - 1);
+        c(12, i, j, z) = c(12, i, j, z - 1);
+        c(11, i, j, z) = c(11, i, j, z - 1);
+        c(16, i, j, z) = c(16, i, j, z - 1);
+        c(15, i, j, z) = c(15, i, j, z - 1);
+    } else {
+        b(5, i, j, z - 1) = b(6, i, j, z);
+        b(11, i, j, z - 1) = b(14, i + 1, j, z);
+        b(12, i, j, z - 1) = b(13, i - 1, j, z);
+        b(15, i, j, z - 1) = b(18, i, j + 1, z);
+        b(16, i, j, z - 1) = b(17, i, j - 1, z);
+        b(6, i, j, z + 1) = b(5, i, j, z);
+        b(14, i, j, z + 1) = b(11, i - 1, j, z);
+        b(13, i, j, z + 1) = b(12, i + 1, j, z);
+        b(18, i, j, z + 1) = b(15, i, j - 1, z);
+        b(17, i, j, z + 1) = b(16, i, j + 1, z);
+        c(5, i, j, z - 1) = c(5, i, j, z);
+        c(11, i, j, z - 1) = c(11, i, j, z);
+        c(12, i, j, z - 1) = c(12, i, j, z);
+        c(15, i, j, z - 1) = c(15, i, j, z);
+        c(16, i, j, z - 1) = c(16, i, j, z);
+        c(6, i, j, z + 1) = c(6, i, j, z);
+        c(14, i, j, z + 1) = c(14, i, j, z);
+        c(13, i, j, z + 1) = c(13, i, j, z);
+        c(18, i, j, z + 1) = c(18, i, j, z);
+        c(17, i, j, z + 1) = c(17, i, j, z);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// color_gradient (Phase_gradient.F90:5-265)
+// ---------------------------------------------------------------------------------
+// phi extrapolation to the solid-boundary list (:13-30)
+__global__ void k_extrap_phi(double *__restrict__ phi, const SolidBnd *__restrict__ sb, int ns, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    const SolidBnd s = sb[t];
+    double acc = 0.0;
+    for (int n = 0; n < s.i_fluid_num; ++n) {
+        const int ie = s.nbr[n];
+        int dx = 0, dy = 0, dz = 0;
+        double w = 0.0;
+#pragma unroll
+        for (int q = 1; q < 19; ++q)
+            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = WEQ(q); }
+        acc = acc + phi[L.i4(s.ix + dx, s.iy + dy, s.iz + dz)] * w;
+    }
+    phi[L.i4(s.ix, s.iy, s.iz)] = acc / s.la_weight;
+}
+
+// ISO4 gradient and unit normal over [1-2, n+2]^3 (:33-79)
+__global__ void __launch_bounds__(256) k_normals(const double *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                 double *__restrict__ cnx, double *__restrict__ cny,
+                                                 double *__restrict__ cnz, double *__restrict__ cnorm, const Layout L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > L.nx + 2 || j > L.ny + 2) return;
+    auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
+    double gx = ISO4_1 * (P(1, 0, 0) - P(-1, 0, 0)) +
+                ISO4_2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
+    double gy = ISO4_1 * (P(0, 1, 0) - P(0, -1, 0)) +
+                ISO4_2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
+    double gz = ISO4_1 * (P(0, 0, 1) - P(0, 0, -1)) +
+                ISO4_2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
+    double cn = sqrt(gx * gx + gy * gy + gz * gz);
+    const int64_t id = L.i2(i, j, k);
+    if (cn < 1e-6 || walls[id] == 1) {
+        gx = 0.0; gy = 0.0; gz = 0.0; cn = 0.0;
+    } else {
+        gx = gx / cn; gy = gy / cn; gz = gz / cn;
+    }
+    cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
+}
+
+// geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
+__global__ void k_wetting(double *__restrict__ cnx, double *__restrict__ cny, double *__restrict__ cnz,
+                          const double *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf) return;
+    const FluidBnd b = fb[t];
+    const int64_t id = L.i2(b.ix, b.iy, b.iz);
+    if (cnorm[id] > 1e-6) {
+        const double cnx0 = cnx[id], cny0 = cny[id], cnz0 = cnz[id];
+        const double tmpCos = b.cos_t;
+        const double tmp1 = b.nwx * cnx0 + b.nwy * cny0 + b.nwz * cnz0;
+        const double tmp2 = 1.0 / sqrt(1.0 - tmp1 * tmp1);
+        const double coe1 = b.sin_t * tmp1 * tmp2;
+        const double coe2 = b.sin_t * tmp2;
+        const double cnxp = (tmpCos - coe1) * b.nwx + coe2 * cnx0;
+        const double cnyp = (tmpCos - coe1) * b.nwy + coe2 * cny0;
+        const double cnzp = (tmpCos - coe1) * b.nwz + coe2 * cnz0;
+        const double cnxm = (tmpCos + coe1) * b.nwx - coe2 * cnx0;
+        const double cnym = (tmpCos + coe1) * b.nwy - coe2 * cny0;
+        const double cnzm = (tmpCos + coe1) * b.nwz - coe2 * cnz0;
+        const double distP = (cnxp - cnx0) * (cnxp - cnx0) + (cnyp - cny0) * (cnyp - cny0) + (cnzp - cnz0) * (cnzp - cnz0);
+        const double distM = (cnxm - cnx0) * (cnxm - cnx0) + (cnym - cny0) * (cnym - cny0) + (cnzm - cnz0) * (cnzm - cnz0);
+        if (distP <= distM) {
+            cnx[id] = cnxp; cny[id] = cnyp; cnz[id] = cnzp;
+        } else {
+            cnx[id] = cnxm; cny[id] = cnym; cnz[id] = cnzm;
+        }
+    }
+}
+
+// normal extrapolation to solid-boundary nodes inside [0, n+1]^3 (:85-110)
+__global__ void k_extrap_normals(double *__restrict__ cnx, double *__restrict__ cny, double *__restrict__ cnz,
+                                 const SolidBnd *__restrict__ sb, int ns, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    const SolidBnd s = sb[t];
+    if (!(s.ix >= 0 && s.ix <= L.nx + 1 && s.iy >= 0 && s.iy <= L.ny + 1 && s.iz >= 0 && s.iz <= L.nz + 1)) return;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int n = 0; n < s.i_fluid_num; ++n) {
+        const int ie = s.nbr[n];
+        int dx = 0, dy = 0, dz = 0;
+        double w = 0.0;
+#pragma unroll
+        for (int q = 1; q < 19; ++q)
+            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = WEQ(q); }
+        const int64_t nb = L.i2(s.ix + dx, s.iy + dy, s.iz + dz);
+        ax = ax + cnx[nb] * w;
+        ay = ay + cny[nb] * w;
+        az = az + cnz[nb] * w;
+    }
+    const int64_t id = L.i2(s.ix, s.iy, s.iz);
+    cnx[id] = ax / s.la_weight;
+    cny[id] = ay / s.la_weight;
+    cnz[id] = az / s.la_weight;
+}
+
+// curvature over [1, n]^3 (:113-201)
+__global__ void __launch_bounds__(256) k_curvature(const double *__restrict__ cnx, const double *__restrict__ cny,
+                                                   const double *__restrict__ cnz, double *__restrict__ curv, const Layout L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > L.nx || j > L.ny) return;
+    auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
+    auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
+    auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };
+    const double kxx = ISO4_1 * (X(1, 0, 0) - X(-1, 0, 0)) +
+                       ISO4_2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
+    const double kyy = ISO4_1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
+                       ISO4_2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(-1, 1, 0) - Y(1, -1, 0) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, 1, -1) - Y(0, -1, 1));
+    const double kzz = ISO4_1 * (Z(0, 0, 1) - Z(0, 0, -1)) +
+                       ISO4_2 * (Z(1, 0, 1) - Z(-1, 0, -1) + Z(-1, 0, 1) - Z(1, 0, -1) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, -1, 1) - Z(0, 1, -1));
+    const double kxy = ISO4_1 * (X(0, 1, 0) - X(0, -1, 0)) +
+                       ISO4_2 * (X(1, 1, 0) - X(-1, -1, 0) + X(-1, 1, 0) - X(1, -1, 0) + X(0, 1, 1) - X(0, -1, -1) + X(0, 1, -1) - X(0, -1, 1));
+    const double kxz = ISO4_1 * (X(0, 0, 1) - X(0, 0, -1)) +
+                       ISO4_2 * (X(1, 0, 1) - X(-1, 0, -1) + X(-1, 0, 1) - X(1, 0, -1) + X(0, 1, 1) - X(0, -1, -1) + X(0, -1, 1) - X(0, 1, -1));
+    const double kyx = ISO4_1 * (Y(1, 0, 0) - Y(-1, 0, 0)) +
+                       ISO4_2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(1, -1, 0) - Y(-1, 1, 0) + Y(1, 0, 1) - Y(-1, 0, -1) + Y(1, 0, -1) - Y(-1, 0, 1));
+    const double kyz = ISO4_1 * (Y(0, 0, 1) - Y(0, 0, -1)) +
+                       ISO4_2 * (Y(1, 0, 1) - Y(-1, 0, -1) + Y(-1, 0, 1) - Y(1, 0, -1) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, -1, 1) - Y(0, 1, -1));
+    const double kzx = ISO4_1 * (Z(1, 0, 0) - Z(-1, 0, 0)) +
+                       ISO4_2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(1, -1, 0) - Z(-1, 1, 0) + Z(1, 0, 1) - Z(-1, 0, -1) + Z(1, 0, -1) - Z(-1, 0, 1));
+    const double kzy = ISO4_1 * (Z(0, 1, 0) - Z(0, -1, 0)) +
+                       ISO4_2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(-1, 1, 0) - Z(1, -1, 0) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, 1, -1) - Z(0, -1, 1));
+    const double cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
+    curv[L.i1(i, j, k)] = (cx * cx - 1.0) * kxx + (cy * cy - 1.0) * kyy + (cz * cz - 1.0) * kzz + cx * cy * (kxy + kyx) +
+                          cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz);
+}
+
+// ---------------------------------------------------------------------------------
+// compute_macro_vars fused with the per-slice monitor reductions
+// (Misc.F90:372-430; Monitor.F90:27-85; singlephase Misc.F90:368-423, Monitor.F90:18-59).
+// One block per z slice.  Each block writes its slice sums and its umax/usq partials to
+// out[nq][nz]; the host finishes the global max/sums in slice order, so the result is
+// independent of scheduling.  Accumulation is FP64 for every storage type.
+// ---------------------------------------------------------------------------------
+constexpr int MON_THREADS = 256;
+constexpr int MON_NQ = 10;  // fl1 fl2 vol1 vol2 mass1 mass2 pre | umax usq1 usq2
+
+template <class S>
+__global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f, const S *__restrict__ g,
+                                                         double *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                         const double *__restrict__ cnx, const double *__restrict__ cny,
+                                                         const double *__restrict__ cnz, const double *__restrict__ cnorm,
+                                                         const double *__restrict__ curv, double *__restrict__ u,
+                                                         double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho,
+                                                         double *__restrict__ out, const Layout L, const StepParams P,
+                                                         int multiphase, int write_fields, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int k = blockIdx.x + 1;
+    const int64_t n = (int64_t)L.nx * L.ny;
+    double acc[MON_NQ];
+#pragma unroll
+    for (int m = 0; m < MON_NQ; ++m) acc[m] = 0.0;
+    const R inv = R(1.0f / scale);
+    for (int64_t t = threadIdx.x; t < n; t += MON_THREADS) {
+        const int i = (int)(t % L.nx) + 1, j = (int)(t / L.nx) + 1;
+        const int wi = walls[L.i2(i, j, k)];
+        const int64_t c = L.cell(i, j, k);
+        double ft[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            double a = (double)St::ld(f, (int64_t)q * L.qs + c, R(WREST(q) * ref), inv);
+            if (multiphase) a = a + (double)St::ld(g, (int64_t)q * L.qs + c, R(WREST(q) * ref), inv);
+            ft[q] = a;
+        }
+        const double m = (double)(1 - wi);
+        const double rr = (ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
+                           ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18]) * m;
+        double fx = 0.0, fy = 0.0, fz = P.force_z;
+        const int64_t i1 = L.i1(i, j, k);
+        if (multiphase) {
+            const int64_t i2 = L.i2(i, j, k);
+            const double tmp = 0.5 * P.gamma * curv[i1] * cnorm[i2];
+            fx = tmp * cnx[i2];
+            fy = tmp * cny[i2];
+            fz = tmp * cnz[i2] + P.force_z;
+        }
+        const double uu = (ft[1] - ft[2] + ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14] - 0.5 * fx) * m;
+        const double vv = (ft[3] - ft[4] + ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18] - 0.5 * fy) * m;
+        const double ww = (ft[5] - ft[6] + ft[11] + ft[12] - ft[13] - ft[14] + ft[15] + ft[16] - ft[17] - ft[18] - 0.5 * fz) * m;
+        if (write_fields) { u[i1] = uu; v[i1] = vv; w[i1] = ww; rho[i1] = rr; }
+        const double temp = multiphase ? (uu * uu + vv * vv + ww * ww) * m : uu * uu + vv * vv + ww * ww;
+        acc[7] = (acc[7] < temp) ? temp : acc[7];
+        if (multiphase) {
+            const int64_t i4 = L.i4(i, j, k);
+            const double ph = 0.0 * (double)wi + phi[i4] * m;
+            phi[i4] = ph;
+            if (ph > 0.999) acc[8] += temp;
+            else if (ph < -0.999) acc[9] += temp;
+            acc[2] += 0.5 * (1.0 + ph) * m;
+            acc[3] += 0.5 * (1.0 - ph) * m;
+            acc[4] += rr * 0.5 * (1.0 + ph) * m;
+            acc[5] += rr * 0.5 * (1.0 - ph) * m;
+            acc[0] += ww * 0.5 * (1.0 + ph) * m;
+            acc[1] += ww * 0.5 * (1.0 - ph) * m;
+            acc[6] += rr * m;
+        } else {
+            acc[0] += ww;
+            acc[6] += rr;
+        }
+    }
+    // warp shuffle, then shared memory across warps (fixed order -> deterministic)
+    __shared__ double red[MON_THREADS / 32][MON_NQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int m = 0; m < MON_NQ; ++m) {
+        double x = acc[m];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = m == 7 ? ((x < y) ? y : x) : x + y;
+        }
+        if (lane == 0) red[wid][m] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < MON_NQ) {
+        const int m = threadIdx.x;
+        double x = red[0][m];
+        for (int q = 1; q < MON_THREADS / 32; ++q) x = m == 7 ? ((x < red[q][m]) ? red[q][m] : x) : x + red[q][m];
+        out[(int64_t)m * L.nz + (k - 1)] = x;
+    }
+}
+
+// cal_saturation partial sums per slice (Monitor.F90:512-550)
+__global__ void __launch_bounds__(MON_THREADS) k_saturation(const double *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                            double *__restrict__ out, const Layout L) {
+    const int k = blockIdx.x + 1;
+    const int64_t n = (int64_t)L.nx * L.ny;
+    double v1 = 0.0, v2 = 0.0;
+    for (int64_t t = threadIdx.x; t < n; t += MON_THREADS) {
+        const int i = (int)(t % L.nx) + 1, j = (int)(t / L.nx) + 1;
+        const double m = (double)(1 - walls[L.i2(i, j, k)]);
+        const double ph = phi[L.i4(i, j, k)];
+        v1 += 0.5 * (1.0 + ph) * m;
+        v2 += 0.5 * (1.0 - ph) * m;
+    }
+    __shared__ double red[2][MON_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        v2 += __shfl_down_sync(0xffffffffu, v2, o);
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = v1; red[1][threadIdx.x >> 5] = v2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < MON_THREADS / 32; ++q) { a += red[0][q]; b += red[1][q]; }
+        out[k - 1] = a;
+        out[L.nz + k - 1] = b;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// initialisation: equilibrium PDFs at rest, rho = 1 (Init_multiphase.F90:366-415;
+// singlephase Initialization.F90:248-276), and the convective-outlet memory (:418-467)
+// ---------------------------------------------------------------------------------
+template <class S>
+__global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const double *__restrict__ phi, double *__restrict__ u,
+                          double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho, const Layout L,
+                          int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb) return;
+    const int i = (int)(t % (L.nx + 2));
+    const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
+    const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    const int64_t c = L.cell(i, j, k);
+    // t enumerates the halo-1 box in Fortran order, so it is also the u/v/w/rho index
+    u[t] = 0.0;
+    v[t] = 0.0;
+    w[t] = 0.0;
+    rho[t] = 1.0;
+    const double usqrt = 0.0;
+    double r0, r1 = 0.0;
+    if (multiphase) {
+        const double ph = phi[L.i4(i, j, k)];
+        r0 = 1.0 * (1.0 + ph) * 0.5;
+        r1 = 1.0 * (1.0 - ph) * 0.5;
+    } else {
+        r0 = 1.0;
+    }
+    const R sc = R(scale);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const double wq = WEQ(q);
+        const double cu = 0.0;
+        const double a = q == 0 ? r0 * wq + r0 * wq * (-1.5 * usqrt) : r0 * wq + r0 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
+        St::st(f, (int64_t)q * L.qs + c, R(a), R(WREST(q) * ref), sc);
+        if (multiphase) {
+            const double b = q == 0 ? r1 * wq + r1 * wq * (-1.5 * usqrt) : r1 * wq + r1 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
+            St::st(g, (int64_t)q * L.qs + c, R(b), R(WREST(q) * ref), sc);
+        }
+    }
+}
+
+template <class S>
+__global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, const double *__restrict__ phi,
+                              double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
+                              const Layout L, int multiphase, float ref, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t np = (int64_t)(L.nx + 2) * (L.ny + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np) return;
+    const int i = (int)(t % (L.nx + 2)), j = (int)(t / (L.nx + 2));
+    const R inv = R(1.0f / scale);
+    for (int q = 0; q < 19; ++q) {
+        fconv[L.ic(i, j, q)] = (double)St::ld(f, (int64_t)q * L.qs + L.cell(i, j, L.nz), R(WREST(q) * ref), inv);
+        if (multiphase)
+            gconv[L.ic(i, j, q)] = (double)St::ld(g, (int64_t)q * L.qs + L.cell(i, j, L.nz), R(WREST(q) * ref), inv);
+    }
+    if (multiphase) phiconv[L.ip(i, j)] = phi[L.i4(i, j, L.nz)];
+}
+
+// FP64 <-> storage conversion of one direction plane (upload/download of FP32/FP16 state)
+template <class S>
+__global__ void k_convert_in(S *__restrict__ dst, const double *__restrict__ src, const Layout L, int q, float ref,
+                             float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb) return;
+    const int i = (int)(t % (L.nx + 2));
+    const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
+    const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    St::st(dst, L.cell(i, j, k), R(src[t]), R(WREST(q) * ref), R(scale));
+}
+
+template <class S>
+__global__ void k_convert_out(double *__restrict__ dst, const S *__restrict__ src, const Layout L, int q, float ref,
+                              float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb) return;
+    const int i = (int)(t % (L.nx + 2));
+    const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
+    const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    dst[t] = (double)St::ld(src, L.cell(i, j, k), R(WREST(q) * ref), R(1.0f / scale));
+}
+
+}  // namespace MFLBM_NS
+}  // namespace mflbm

@@ -1,0 +1,61 @@
+// kernels_api.h -- launch interface between the C-ABI layer (api.cu) and the kernel
+// translation units.  Each floating-point flavour (fast / strict) exports one
+// KernelTable; the ordering of one time step lives only in api.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace mflbm {
+
+// Everything a launcher needs: device pointers, layout and parameters.
+struct DevState {
+    Layout L;
+    StepParams P;
+    int multiphase;
+    int prec;              // MFLBM_FP64 / FP32 / FP16
+    float ref, scale;      // FP16 deviation storage: rest density and scale
+    double rk_weight2;     // 1/sqrt(2)/36 evaluated on the host
+    void *f;               // species 1 PDFs (19 planes)
+    void *g;               // species 2 PDFs (19 planes), multiphase only
+    double *phi;           // halo 4
+    double *cnx, *cny, *cnz, *cnorm;  // halo 2
+    double *curv, *u, *v, *w, *rho;   // halo 1
+    int8_t *walls;         // halo 2
+    double *w_in;          // (nx+2)(ny+2)
+    double *fconv, *gconv, *phiconv;
+    const SolidBnd *sb;
+    int ns;
+    const FluidBnd *fb;
+    int nf;
+    double *mon;           // MON_NQ * nz slice partials
+    double *stage;         // one FP64 plane of the halo-1 box (conversion staging)
+};
+
+struct KernelTable {
+    // every launcher returns the number of kernels it launched
+    // one collision+streaming sweep over the interior (kernel_even / kernel_odd)
+    int (*collide)(const DevState &, bool odd, cudaStream_t);
+    // periodic halo exchange after the sweep: pull after even, push after odd
+    int (*wrap)(const DevState &, bool pull, cudaStream_t);
+    // inlet/outlet/porous-plate boundary conditions
+    int (*boundary)(const DevState &, bool before_odd, int inlet_bc, int outlet_bc, bool open_z, cudaStream_t);
+    // color_gradient: extrapolation, normals, wetting, normal extrapolation, curvature
+    int (*color_gradient)(const DevState &, cudaStream_t);
+    // compute_macro_vars + per-slice reductions into st.mon
+    int (*monitor)(const DevState &, cudaStream_t);
+    // cal_saturation per-slice partials into st.mon (2*nz)
+    int (*saturation)(const DevState &, cudaStream_t);
+    // equilibrium at rest over the halo'd box, then the convective-outlet memory
+    int (*init_equilibrium)(const DevState &, bool convec, cudaStream_t);
+    // FP64 plane <-> storage plane (q of species s) through st.stage
+    int (*convert_in)(const DevState &, int species, int q, cudaStream_t);
+    int (*convert_out)(const DevState &, int species, int q, cudaStream_t);
+};
+
+const KernelTable *kernels_fast();
+const KernelTable *kernels_strict();
+
+constexpr int kMonNQ = 10;
+
+}  // namespace mflbm

@@ -1,0 +1,133 @@
+"""GPU parity of the multiphase colour-gradient path against the CPU oracle (C ABI).
+
+strict_fp=1: bit-identical PDFs, phi, normals, curvature on every slot after 1-3 and
+several steps (both AA parities, all boundary families).  Default (FMA) build: stated
+FP64 tolerances.  Monitor reductions: FP64 sums in a different order, rtol 1e-12.
+"""
+import numpy as np
+import pytest
+
+from cases import load_case, mp_case
+from mflbm import Solver
+from pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+MP_CASES = {
+    "periodic_yz": dict(per=(0, 1, 1)),
+    "periodic_y_velocity_inlet_convective": dict(per=(0, 1, 0), inlet=1, outlet=1),
+    "walled_velocity_inlet_convective": dict(per=(0, 0, 0), inlet=1, outlet=1, theta_deg=30.0),
+    "walled_pressure_bcs": dict(per=(0, 0, 0), inlet=2, outlet=2, sa_inject=0.0),
+    "velocity_inlet_pressure_outlet": dict(per=(0, 0, 0), inlet=1, outlet=2),
+    "periodic_z_only": dict(per=(0, 0, 1), force=1e-5),
+    "viscosity_ratio_mrt1": dict(per=(0, 1, 1), nu1=0.02, nu2=0.2, mrt=1),
+    "mrt3": dict(per=(0, 1, 1), mrt=3, theta_deg=120.0),
+    "mrt4": dict(per=(0, 1, 1), mrt=4, beta=0.7),
+    "porous_plate_blocks_fluid1": dict(per=(0, 1, 0), inlet=1, outlet=1, plate=1, zplate=8),
+    "porous_plate_blocks_fluid2": dict(per=(0, 1, 0), inlet=1, outlet=1, plate=2, zplate=6),
+    "ragged_sizes": dict(nx=9, ny=7, nz=11, per=(0, 1, 1), spheres=1),
+}
+
+FIELDS = ("f", "g", "phi", "f_convec", "g_convec", "phi_convec")
+
+
+def _pair(kw, strict=1):
+    case = mp_case(strict=strict, **kw)
+    gpu = Solver(case["params"])
+    orc = Oracle(case["params"])
+    load_case(gpu, case)
+    load_case(orc, case)
+    return case, gpu, orc
+
+
+def _same(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_initial_color_gradient_bit_identical():
+    case, gpu, orc = _pair(MP_CASES["walled_velocity_inlet_convective"])
+    ga, gb = gpu.get_gradient(), orc.get_gradient()
+    for k in ga:
+        assert _same(ga[k], gb[k]), k
+
+
+@pytest.mark.parametrize("name", list(MP_CASES))
+@pytest.mark.parametrize("steps", [1, 2, 3, 6])
+def test_strict_bit_identical(name, steps):
+    case, gpu, orc = _pair(MP_CASES[name])
+    for n in range(1, steps + 1):
+        gpu.step(n)
+        orc.step(n)
+    a, b = gpu.download_state(), orc.download_state()
+    for k in FIELDS:
+        if k in a:
+            assert _same(a[k], b[k]), (k, np.nanmax(np.abs(a[k] - b[k])))
+    ga, gb = gpu.get_gradient(), orc.get_gradient()
+    for k in ga:
+        assert _same(ga[k], gb[k]), k
+
+
+@pytest.mark.parametrize("name", ["periodic_yz", "walled_velocity_inlet_convective", "viscosity_ratio_mrt1"])
+def test_fma_build_within_tolerance(name):
+    case, gpu, orc = _pair(MP_CASES[name], strict=0)
+    gpu.run(1, 40)
+    orc.run(1, 40)
+    a, b = gpu.download_state(), orc.download_state()
+    assert np.abs(a["f"] - b["f"]).max() <= 1e-12
+    assert np.abs(a["g"] - b["g"]).max() <= 1e-12
+    assert np.abs(a["phi"] - b["phi"]).max() <= 1e-10
+
+
+def test_graph_run_equals_steps():
+    kw = MP_CASES["periodic_y_velocity_inlet_convective"]
+    _, g1, _ = _pair(kw)
+    _, g2, _ = _pair(kw)
+    for n in range(1, 1 + 21):
+        g1.step(n)
+    g2.run(1, 21)
+    a, b = g1.download_state(), g2.download_state()
+    for k in FIELDS:
+        assert _same(a[k], b[k]), k
+
+
+def test_monitor_saturation_macro():
+    case, gpu, orc = _pair(MP_CASES["walled_velocity_inlet_convective"])
+    gpu.run(1, 24)
+    orc.run(1, 24)
+    va, vb = gpu.saturation(), orc.saturation()
+    np.testing.assert_allclose(va, vb, rtol=1e-13)
+    pa, sa, st_a = gpu.monitor()
+    pb, sb, st_b = orc.monitor()
+    assert st_a == st_b == 0
+    np.testing.assert_allclose(pa, pb, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(sa, sb, rtol=1e-12, atol=1e-30)
+    ma, mb = gpu.macro(), orc.macro()
+    for k in ("u", "v", "w", "rho"):
+        assert _same(ma[k][1:-1, 1:-1, 1:-1], mb[k][1:-1, 1:-1, 1:-1]), k
+    assert _same(ma["phi"], mb["phi"])
+
+
+def test_init_equilibrium_matches_oracle():
+    case = mp_case(per=(0, 0, 0), inlet=1, outlet=1)
+    gpu, orc = Solver(case["params"]), Oracle(case["params"])
+    for s in (gpu, orc):
+        s.set_geometry(case["walls"], case["solid"], case["fluid"], case["w_in"])
+        s.init_equilibrium(case["phi"])
+    a, b = gpu.download_state(), orc.download_state()
+    for k in FIELDS:
+        assert _same(a[k], b[k]), k
+
+
+def test_list_outside_halo_rejected():
+    case = mp_case()
+    gpu = Solver(case["params"])
+    bad = case["solid"].copy()
+    bad["ix"][0] = case["params"].nx + 9
+    from mflbm import MflbmError
+    with pytest.raises(MflbmError):
+        gpu.set_geometry(case["walls"], bad, case["fluid"])
+    bad = case["solid"].copy()
+    bad["neighbor_list"][0, 0] = 19
+    bad["i_fluid_num"][0] = max(1, bad["i_fluid_num"][0])
+    with pytest.raises(MflbmError):
+        gpu.set_geometry(case["walls"], bad, case["fluid"])
