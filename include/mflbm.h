@@ -69,7 +69,7 @@ extern "C" {
 /* PDF storage precision */
 #define MFLBM_FP64 0   /* plain drop-in: FP64 storage, FP64 collision               */
 #define MFLBM_FP32 1   /* FP32 storage, FP32 collision                              */
-#define MFLBM_FP16 2   /* FP16 storage of f_q - w_q*rho0, FP32 collision            */
+#define MFLBM_FP16 2   /* FP16 storage of scaled deviations from the rest state, FP32 collision */
 
 /* Run parameters: the subset of simulation_control.txt that the per-step path
  * reads, after the reference's own host-side derivations
@@ -214,6 +214,7 @@ int32_t mflbm_set_profiling(mflbm_ctx *ctx, int32_t enable);
  * Synchronises. */
 int32_t mflbm_get_profile(mflbm_ctx *ctx, double *region_ms, double *collide_ms, int64_t *collide_launches,
                           int64_t *kernel_launches);
+
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,6 @@
 """Build libmflbm.so (sm_103a) in-tree.
 
-Three translation units are compiled in parallel and linked into
+The translation units are compiled in parallel and linked into
 mf-lbm_gb300/mflbm/lib/libmflbm.so:
 
   csrc/api.cu             C ABI, context, step ordering, CUDA graphs
