@@ -215,6 +215,23 @@ int32_t mflbm_set_profiling(mflbm_ctx *ctx, int32_t enable);
 int32_t mflbm_get_profile(mflbm_ctx *ctx, double *region_ms, double *collide_ms, int64_t *collide_launches,
                           int64_t *kernel_launches);
 
+/* Largest nz that mflbm_saturation_noalloc accepts: its scratch holds two doubles per
+ * z slice (256 KiB per device). */
+#define MFLBM_NOALLOC_MAX_NZ 16384
+
+/* cal_saturation without a context and without any allocation.  No counterpart in the
+ * reference: it is for callers that must not allocate device memory -- a Fortran host
+ * whose OpenACC data region owns every device array and passes `use_device` pointers,
+ * or a loop that cannot afford cudaMalloc's implicit device-wide synchronisation.
+ *   phi   device pointer, halo 4 layout; walls device pointer, halo 2 layout
+ *   vol   device pointer to 2 doubles, receives (vol1, vol2) as mflbm_saturation
+ *   stream  cudaStream_t to launch on (NULL: legacy default stream); asynchronous
+ * Scratch is a fixed __device__ array shared by every call; overlapping calls race.
+ * The first call on a device looks up the scratch address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  nz > MFLBM_NOALLOC_MAX_NZ returns
+ * MFLBM_ERANGE.  Errors are reported through mflbm_last_error(NULL). */
+int32_t mflbm_saturation_noalloc(const double *phi, const int8_t *walls, int32_t nx, int32_t ny, int32_t nz,
+                                 double *vol, void *stream);
 
 #ifdef __cplusplus
 }

@@ -7,6 +7,7 @@ mf-lbm_gb300/mflbm/lib/libmflbm.so:
   csrc/kernels_fast.cu    kernels with nvcc's default FMA contraction
   csrc/kernels_strict.cu  the same kernels with --fmad=false (bit-identical to an IEEE
                           restatement that keeps the reference's operation order)
+  csrc/noalloc.cu         mflbm_saturation_noalloc (fixed device scratch, no allocation)
 
 Only one -gencode (sm_103a) is built.  nvcc cross-compiles without a GPU, so this runs
 on the CPU build host and on the GPU host alike.
@@ -29,6 +30,7 @@ UNITS = {
     "api.o": ("api.cu", []),
     "kernels_fast.o": ("kernels_fast.cu", []),
     "kernels_strict.o": ("kernels_strict.cu", ["--fmad=false"]),
+    "noalloc.o": ("noalloc.cu", []),
 }
 
 

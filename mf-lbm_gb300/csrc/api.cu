@@ -50,6 +50,11 @@ static const int kEventRing = 512;
 
 static thread_local std::string g_last_create_error;
 
+namespace mflbm {
+// errors of calls that have no context land in the same slot as mflbm_create's
+void set_global_error(const std::string &msg) { g_last_create_error = msg; }
+}  // namespace mflbm
+
 namespace {
 
 int fail(mflbm_ctx *c, int code, const std::string &msg) {

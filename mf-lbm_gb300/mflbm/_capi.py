@@ -24,6 +24,7 @@ MFLBM_FAILED = 3
 MFLBM_FP64 = 0
 MFLBM_FP32 = 1
 MFLBM_FP16 = 2
+MFLBM_NOALLOC_MAX_NZ = 16384
 
 ERROR_NAMES = {
     MFLBM_EINVAL: "MFLBM_EINVAL", MFLBM_ECUDA: "MFLBM_ECUDA", MFLBM_ENOMEM: "MFLBM_ENOMEM",
@@ -94,6 +95,7 @@ SIGNATURES = {
     "mflbm_synchronize": (C.c_int32, [P]),
     "mflbm_set_profiling": (C.c_int32, [P, C.c_int32]),
     "mflbm_get_profile": (C.c_int32, [P, P, P, P, P]),
+    "mflbm_saturation_noalloc": (C.c_int32, [P, P, C.c_int32, C.c_int32, C.c_int32, P, P]),
 }
 
 _lib = None
