@@ -30,6 +30,7 @@ struct mflbm_ctx {
     std::vector<void *> allocs;
     bool have_geometry = false;
     bool open_z = false;
+    int64_t cells_cap = 0;
     // graphs of whole even+odd step pairs
     cudaGraphExec_t g_pair = nullptr, g_block = nullptr;
     int block_pairs = 8;
@@ -247,6 +248,12 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     L.pitch = ((int64_t)L.xo + p.nx + 2 + A - 1) / A * A;
     L.pz = L.pitch * (p.ny + 2);
     L.qs = L.pz * (p.nz + 2);
+    if (L.qs >= ((int64_t)1 << 31)) {
+        g_last_create_error = "lattice too large: one PDF plane exceeds 2^31 elements";
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return MFLBM_ERANGE;
+    }
     L.h1x = p.nx + 2; L.h1xy = (int64_t)(p.nx + 2) * (p.ny + 2);
     L.h2x = p.nx + 4; L.h2xy = (int64_t)(p.nx + 4) * (p.ny + 4);
     L.h4x = p.nx + 8; L.h4xy = (int64_t)(p.nx + 8) * (p.ny + 8);
@@ -280,6 +287,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
             P.s_e = omega; P.s_e2 = omega; P.s_pi = omega; P.s_q = omega; P.s_t = omega;
         }
     }
+    c->st.fold = fold_rates<double>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
     c->st.multiphase = p.multiphase;
     c->st.prec = p.precision;
     c->st.ref = 1.0f;
@@ -391,6 +399,27 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
         int r = dalloc(c, &fbd, n_fluid);
         if (r) return r;
         c->st.fb = fbd;
+    }
+    // sorted list of interior fluid nodes (walls == 0): the collision sweep runs one
+    // thread per entry, so no lane idles on a solid node
+    {
+        const Layout &L = c->st.L;
+        std::vector<int32_t> cells;
+        cells.reserve((size_t)p.nx * p.ny * p.nz / 4 + 1);
+        for (int k = 1; k <= p.nz; ++k)
+            for (int j = 1; j <= p.ny; ++j)
+                for (int i = 1; i <= p.nx; ++i)
+                    if (walls[L.i2(i, j, k)] == 0) cells.push_back((int32_t)L.cell(i, j, k));
+        if ((int64_t)cells.size() > c->cells_cap) {
+            int32_t *d = nullptr;
+            int r = dalloc(c, &d, (int64_t)cells.size());
+            if (r) return r;
+            c->st.cells = d;
+            c->cells_cap = (int64_t)cells.size();
+        }
+        if (!cells.empty())
+            CK(c, cudaMemcpy((void *)c->st.cells, cells.data(), sizeof(int32_t) * cells.size(), cudaMemcpyHostToDevice));
+        c->st.ncell = (int)cells.size();
     }
     if (n_solid) CK(c, cudaMemcpy((void *)c->st.sb, solid, sizeof(SolidBnd) * n_solid, cudaMemcpyHostToDevice));
     if (n_fluid) CK(c, cudaMemcpy((void *)c->st.fb, fb.data(), sizeof(FluidBnd) * n_fluid, cudaMemcpyHostToDevice));

@@ -85,6 +85,52 @@ struct SolidBnd {  // identical to mflbm_solid_bnd (96 bytes)
     double la_weight;
 };
 
+// Folded MRT coefficients (see mrt_collide_pairs in kernels.cuh): every post-collision
+// moment, already divided by its back-transform norm, is a linear combination of the
+// pre-collision moment, its equilibrium term and its forcing term.
+template <class R> struct MrtFold {
+    R e_m, e_den, e_u2, e_f;   // e'   (/2394)
+    R e2_m, e2_u2, e2_f;       // e2'  (/252)
+    R q_m, q_u, q_f;           // q'   (/40)
+    R x3_m, x3_eq, x3_f;       // 3pxx'  (/36)
+    R xi_m, xi_f;              // 3pixx' (/72)
+    R w_m, w_eq, w_f;          // pww'   (/12)
+    R wi_m, wi_f;              // piww'  (/24)
+    R o_m, o_eq, o_f;          // pxy', pyz', pzx' (/4)
+    R t_m;                     // t'     (/8)
+};
+
+template <class R>
+__host__ __device__ __forceinline__ MrtFold<R> fold_rates(double s_e, double s_e2, double s_q, double s_nu, double s_pi,
+                                                          double s_t) {
+    MrtFold<R> c;
+    c.e_m = R((1.0 - s_e) / 2394.0);
+    c.e_den = R(-11.0 * s_e / 2394.0);
+    c.e_u2 = R(19.0 * s_e / 2394.0);
+    c.e_f = R((38.0 - 19.0 * s_e) / 2394.0);
+    c.e2_m = R((1.0 - s_e2) / 252.0);
+    c.e2_u2 = R(s_e2 * (-475.0 / 63.0) / 252.0);
+    c.e2_f = R((-11.0 + 5.5 * s_e2) / 252.0);
+    c.q_m = R((1.0 - s_q) / 40.0);
+    c.q_u = R(s_q * (-2.0 / 3.0) / 40.0);
+    c.q_f = R((-2.0 / 3.0 + s_q / 3.0) / 40.0);
+    c.x3_m = R((1.0 - s_nu) / 36.0);
+    c.x3_eq = R(s_nu / 36.0);
+    c.x3_f = R((2.0 - s_nu) / 36.0);
+    c.xi_m = R((1.0 - s_pi) / 72.0);
+    c.xi_f = R((1.0 - 0.5 * s_pi) / 72.0);
+    c.w_m = R((1.0 - s_nu) / 12.0);
+    c.w_eq = R(s_nu / 12.0);
+    c.w_f = R((2.0 - s_nu) / 12.0);
+    c.wi_m = R((1.0 - s_pi) / 24.0);
+    c.wi_f = R((1.0 - 0.5 * s_pi) / 24.0);
+    c.o_m = R((1.0 - s_nu) / 4.0);
+    c.o_eq = R(s_nu / 4.0);
+    c.o_f = R((1.0 - 0.5 * s_nu) / 4.0);
+    c.t_m = R((1.0 - s_t) / 8.0);
+    return c;
+}
+
 // FP16 deviation storage: value = w_q * ref + half_value * scale, ref = the rest
 // density of the species.
 template <class S> struct StoreTraits;

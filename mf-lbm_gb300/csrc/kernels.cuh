@@ -185,6 +185,132 @@ __device__ __forceinline__ void mrt_collide(R (&ft)[19], R den, R fx, R fy, R fz
 }
 
 // ---------------------------------------------------------------------------------
+// The same MRT collision re-associated for fewer FP64 instructions (default build).
+//
+// Opposite directions form 9 pairs (q, q').  Every even-order moment of the D3Q19 basis
+// (rho, e, e2, 3pxx, 3pixx, pww, piww, pxy, pyz, pzx) depends only on f0 and the pair
+// sums p = f_q + f_q'; every odd-order moment (j, q, t) only on the pair differences
+// d = f_q - f_q'.  The back-transform likewise yields a symmetric part S and an
+// antisymmetric part A per pair, f_q = S + A, f_q' = S - A.  Relaxation, equilibrium,
+// forcing and the back-transform norms (1/19, 1/2394, ...) are folded into one
+// coefficient set (MrtFold).  Mathematically this is the reference's collision
+// (Kernel_multiphase.F90:158-267) with mrt_e2_coef1 = mrt_omega_xx = 0 substituted.
+// ---------------------------------------------------------------------------------
+// FXY = false: the force has only a z component (singlephase body force).
+// OWN_DEN = true: the density is the sum of the 19 PDFs (singlephase); otherwise the
+// caller supplies it (rho1 + rho2 of the colour model).
+template <class R, bool FXY, bool OWN_DEN>
+__device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R fy, R fz, const MrtFold<R> &c) {
+    const R f0 = ft[0];
+    const R p1 = ft[1] + ft[2], d1 = ft[1] - ft[2];
+    const R p2 = ft[3] + ft[4], d2 = ft[3] - ft[4];
+    const R p3 = ft[5] + ft[6], d3 = ft[5] - ft[6];
+    const R p4 = ft[7] + ft[10], d4 = ft[7] - ft[10];
+    const R p5 = ft[8] + ft[9], d5 = ft[8] - ft[9];
+    const R p6 = ft[11] + ft[14], d6 = ft[11] - ft[14];
+    const R p7 = ft[12] + ft[13], d7 = ft[12] - ft[13];
+    const R p8 = ft[15] + ft[18], d8 = ft[15] - ft[18];
+    const R p9 = ft[16] + ft[17], d9 = ft[16] - ft[17];
+    // momentum; velocity with the half-step force
+    const R jx = d1 + d4 - d5 + d6 - d7;
+    const R jy = d2 + d4 + d5 + d8 - d9;
+    const R jz = d3 + d6 + d7 + d8 + d9;
+    const R ux = FXY ? jx + R(0.5) * fx : jx;
+    const R uy = FXY ? jy + R(0.5) * fy : jy;
+    const R uz = jz + R(0.5) * fz;
+    const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+    const R u2 = uxx + uyy + uzz;
+    const R fux = FXY ? fx * ux : R(0.0);
+    const R fuy = FXY ? fy * uy : R(0.0);
+    const R fuz = fz * uz;
+    const R Fu = FXY ? fux + fuy + fuz : fuz;
+    // even-order moments from the pair sums
+    const R a = p1 + p2 + p3;
+    const R dxy = p4 + p5, dxz = p6 + p7, dyz = p8 + p9;
+    const R ds = dxy + dxz + dyz;
+    const R den = OWN_DEN ? f0 + a + ds : den_in;
+    const R m_e = R(-30.0) * f0 - R(11.0) * a + R(8.0) * ds;
+    const R m_e2 = R(12.0) * f0 - R(4.0) * a + ds;
+    const R s6 = R(2.0) * p1 - p2 - p3;
+    const R s7 = dxy + dxz - R(2.0) * dyz;
+    const R s8 = p2 - p3, s9 = dxy - dxz;
+    // odd-order non-conserved moments from the pair differences
+    const R qx = jx - R(5.0) * d1, qy = jy - R(5.0) * d2, qz = jz - R(5.0) * d3;
+    const R tx = d4 - d5 - d6 + d7;
+    const R ty = -d4 - d5 + d8 - d9;
+    const R tz = d6 + d7 - d8 - d9;
+    // relaxed, forced and scaled moments
+    const R rho_s = den * R(1.0 / 19.0);
+    const R e_s = c.e_m * m_e + c.e_den * den + c.e_u2 * u2 + c.e_f * Fu;
+    const R e2_s = c.e2_m * m_e2 + c.e2_u2 * u2 + c.e2_f * Fu;
+    const R jx_s = R(0.1) * (FXY ? jx + fx : jx);
+    const R jy_s = R(0.1) * (FXY ? jy + fy : jy);
+    const R jz_s = R(0.1) * (jz + fz);
+    const R qx_s = FXY ? c.q_m * qx + c.q_u * ux + c.q_f * fx : c.q_m * qx + c.q_u * ux;
+    const R qy_s = FXY ? c.q_m * qy + c.q_u * uy + c.q_f * fy : c.q_m * qy + c.q_u * uy;
+    const R qz_s = c.q_m * qz + c.q_u * uz + c.q_f * fz;
+    const R x3_s = c.x3_m * (s6 + s7) + c.x3_eq * (R(3.0) * uxx - u2) + c.x3_f * (R(2.0) * fux - fuy - fuz);
+    const R xi_s = c.xi_m * (R(-2.0) * s6 + s7) + c.xi_f * (R(-2.0) * fux + fuy + fuz);
+    const R w_s = c.w_m * (s8 + s9) + c.w_eq * (uyy - uzz) + c.w_f * (fuy - fuz);
+    const R wi_s = c.wi_m * (R(-2.0) * s8 + s9) + c.wi_f * (fuz - fuy);
+    const R xy_s = FXY ? c.o_m * (p4 - p5) + c.o_eq * (ux * uy) + c.o_f * (fx * uy + fy * ux) : c.o_m * (p4 - p5) + c.o_eq * (ux * uy);
+    const R yz_s = FXY ? c.o_m * (p8 - p9) + c.o_eq * (uy * uz) + c.o_f * (fy * uz + fz * uy)
+                       : c.o_m * (p8 - p9) + c.o_eq * (uy * uz) + c.o_f * (fz * uy);
+    const R zx_s = FXY ? c.o_m * (p6 - p7) + c.o_eq * (ux * uz) + c.o_f * (fx * uz + fz * ux)
+                       : c.o_m * (p6 - p7) + c.o_eq * (ux * uz) + c.o_f * (fz * ux);
+    const R tx_s = c.t_m * tx, ty_s = c.t_m * ty, tz_s = c.t_m * tz;
+    // back-transform
+    const R sum1 = rho_s - R(11.0) * e_s - R(4.0) * e2_s;
+    const R sum2 = R(2.0) * x3_s - R(4.0) * xi_s;
+    const R sum3 = w_s - R(2.0) * wi_s;
+    const R sum4 = rho_s + R(8.0) * e_s + e2_s;
+    const R sum5 = jx_s + qx_s, sum6 = jy_s + qy_s, sum7 = jz_s + qz_s;
+    const R sum8 = x3_s + xi_s, sum9 = w_s + wi_s;
+    ft[0] = rho_s - R(30.0) * e_s + R(12.0) * e2_s;
+    {
+        const R S = sum1 + sum2, A = jx_s - R(4.0) * qx_s;
+        ft[1] = S + A;
+        ft[2] = S - A;
+    }
+    {
+        const R Syz = sum1 - R(0.5) * sum2;
+        const R Sy = Syz + sum3, Ay = jy_s - R(4.0) * qy_s;
+        const R Sz = Syz - sum3, Az = jz_s - R(4.0) * qz_s;
+        ft[3] = Sy + Ay;
+        ft[4] = Sy - Ay;
+        ft[5] = Sz + Az;
+        ft[6] = Sz - Az;
+    }
+    {
+        const R b = sum4 + sum8 + sum9;
+        const R Sp = b + xy_s, Ap = sum5 + sum6 + tx_s - ty_s;
+        const R Sm = b - xy_s, Am = sum6 - sum5 - tx_s - ty_s;
+        ft[7] = Sp + Ap;
+        ft[10] = Sp - Ap;
+        ft[8] = Sm + Am;
+        ft[9] = Sm - Am;
+    }
+    {
+        const R b = sum4 + sum8 - sum9;
+        const R Sp = b + zx_s, Ap = sum5 + sum7 - tx_s + tz_s;
+        const R Sm = b - zx_s, Am = sum7 - sum5 + tx_s + tz_s;
+        ft[11] = Sp + Ap;
+        ft[14] = Sp - Ap;
+        ft[12] = Sm + Am;
+        ft[13] = Sm - Am;
+    }
+    {
+        const R b = sum4 - R(2.0) * sum8;
+        const R Sp = b + yz_s, Ap = sum6 + sum7 + ty_s - tz_s;
+        const R Sm = b - yz_s, Am = sum7 - sum6 - ty_s - tz_s;
+        ft[15] = Sp + Ap;
+        ft[18] = Sp - Ap;
+        ft[16] = Sm + Am;
+        ft[17] = Sm - Am;
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // singlephase kernel_even / kernel_odd (singlephase_3D/0.src/Kernel.F90:5-400).
 // One thread per interior node; solid nodes are skipped, so their slots carry the
 // implicit full-way bounce-back of the AA pattern.
@@ -192,16 +318,15 @@ __device__ __forceinline__ void mrt_collide(R (&ft)[19], R den, R fx, R fy, R fz
 // even: ft_q <- f_opp(q)(x)  ... f_q(x) <- ft_q
 // ---------------------------------------------------------------------------------
 template <class S, bool ODD>
-__global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int8_t *__restrict__ walls, const Layout L,
-                                                 const StepParams P, const float ref, const float scale) {
+__global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
+                                                 const Layout L, const StepParams P, const MrtFold<double> fold,
+                                                 const float ref, const float scale) {
     using St = Store<S>;
     using R = typename St::R;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > L.nx || j > L.ny) return;
-    if (walls[L.i2(i, j, k)] != 0) return;
-    const int64_t c = L.cell(i, j, k);
+    // one thread per fluid node: the sorted fluid-cell list keeps every lane busy
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    const int64_t c = cells[t];
     const R inv_scale = R(1.0f / scale);
     R ft[19];
 #pragma unroll
@@ -211,9 +336,23 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int8_t
         else
             ft[q] = St::ld(f, (int64_t)OPP(q) * L.qs + c, R(WREST(q) * ref), inv_scale);
     }
+#ifdef MFLBM_STRICT
     const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
                   ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
     mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
+#else
+    MrtFold<R> cf;
+    cf.e_m = R(fold.e_m); cf.e_den = R(fold.e_den); cf.e_u2 = R(fold.e_u2); cf.e_f = R(fold.e_f);
+    cf.e2_m = R(fold.e2_m); cf.e2_u2 = R(fold.e2_u2); cf.e2_f = R(fold.e2_f);
+    cf.q_m = R(fold.q_m); cf.q_u = R(fold.q_u); cf.q_f = R(fold.q_f);
+    cf.x3_m = R(fold.x3_m); cf.x3_eq = R(fold.x3_eq); cf.x3_f = R(fold.x3_f);
+    cf.xi_m = R(fold.xi_m); cf.xi_f = R(fold.xi_f);
+    cf.w_m = R(fold.w_m); cf.w_eq = R(fold.w_eq); cf.w_f = R(fold.w_f);
+    cf.wi_m = R(fold.wi_m); cf.wi_f = R(fold.wi_f);
+    cf.o_m = R(fold.o_m); cf.o_eq = R(fold.o_eq); cf.o_f = R(fold.o_f);
+    cf.t_m = R(fold.t_m);
+    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), R(P.force_z), cf);
+#endif
     const R sc = R(scale);
     if (ODD) {
         St::st(f, c, ft[0], R(WREST(0) * ref), sc);
@@ -235,17 +374,19 @@ template <bool ODD>
 __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double *__restrict__ g, double *__restrict__ phi,
                                                  const double *__restrict__ cnx, const double *__restrict__ cny,
                                                  const double *__restrict__ cnz, const double *__restrict__ cnorm,
-                                                 const double *__restrict__ curv, const int8_t *__restrict__ walls,
-                                                 const Layout L, const StepParams P, const double rk_weight2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > L.nx || j > L.ny) return;
+                                                 const double *__restrict__ curv, const int32_t *__restrict__ cells,
+                                                 const int ncell, const Layout L, const StepParams P, const double rk_weight2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    const int64_t c = cells[t];
+    // lattice coordinates of the cell, for the auxiliary arrays in Fortran layout
+    const int k = (int)(c / L.pz);
+    const int64_t r = c - (int64_t)k * L.pz;
+    const int j = (int)(r / L.pitch);
+    const int i = (int)(r - (int64_t)j * L.pitch) - L.xo;
     const int64_t w2 = L.i2(i, j, k);
-    if (walls[w2] != 0) return;
-    const int64_t c = L.cell(i, j, k);
     double ft[19];
-    double rho1, rho2;
+    double rho1 = 0.0, rho2 = 0.0;
     // pull (odd) or local swapped read (even); rho1/rho2 accumulate in the written order
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
@@ -282,14 +423,17 @@ __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double 
         s_e = 1.19; s_e2 = 1.4; s_pi = 1.4; s_q = 1.2; s_t = 1.98;
     }
     const double den = rho1 + rho2;
+#ifdef MFLBM_STRICT
     mrt_collide<double>(ft, den, fx, fy, fz, s_e, s_e2, s_q, omega, s_pi, s_t);
+#else
+    const MrtFold<double> cf = fold_rates<double>(s_e, s_e2, s_q, omega, s_pi, s_t);
+    mrt_collide_pairs<double, true, false>(ft, den, fx, fy, fz, cf);
+#endif
     // recolouring (Kernel_multiphase.F90:272-315)
     const double tmp1 = rho1 / den;
     tmp = rho1 * rho2 * P.beta / den;
-    const double a0 = tmp1 * ft[0];
-    const double b0 = ft[0] * (1.0 - tmp1);
-    f[c] = a0;
-    g[c] = b0;
+    f[c] = tmp1 * ft[0];
+    g[c] = ft[0] * (1.0 - tmp1);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
         const double ex = (double)EX(q), ey = (double)EY(q), ez = (double)EZ(q);

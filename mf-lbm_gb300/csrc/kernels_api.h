@@ -30,6 +30,9 @@ struct DevState {
     int nf;
     double *mon;           // MON_NQ * nz slice partials
     double *stage;         // one FP64 plane of the halo-1 box (conversion staging)
+    const int32_t *cells;  // padded-layout index of every interior fluid node, ascending
+    int ncell;
+    MrtFold<double> fold;  // singlephase MRT coefficients of the default build
 };
 
 struct KernelTable {

@@ -16,28 +16,26 @@ template <class S> S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g
 
 template <class S>
 int collide_t(const DevState &st, bool odd, cudaStream_t s) {
-    const Layout &L = st.L;
-    const dim3 b = row_block(L.nx);
-    const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
+    if (st.ncell == 0) return 0;
+    const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     if (odd)
-        k_sp_step<S, true><<<g, b, 0, s>>>(fs<S>(st), st.walls, L, st.P, st.ref, st.scale);
+        k_sp_step<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, st.fold, st.ref, st.scale);
     else
-        k_sp_step<S, false><<<g, b, 0, s>>>(fs<S>(st), st.walls, L, st.P, st.ref, st.scale);
+        k_sp_step<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, st.fold, st.ref, st.scale);
     return 1;
 }
 
 int collide(const DevState &st, bool odd, cudaStream_t s) {
     if (st.multiphase) {
-        const Layout &L = st.L;
-        const dim3 b = row_block(L.nx);
-        const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
+        if (st.ncell == 0) return 0;
+        const unsigned nb = (unsigned)((st.ncell + 127) / 128);
         double *f = fs<double>(st), *gg = gs<double>(st);
         if (odd)
-            k_mp_step<true><<<g, b, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.walls, L, st.P,
-                                            st.rk_weight2);
+            k_mp_step<true><<<nb, 128, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.cells, st.ncell,
+                                               st.L, st.P, st.rk_weight2);
         else
-            k_mp_step<false><<<g, b, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.walls, L, st.P,
-                                             st.rk_weight2);
+            k_mp_step<false><<<nb, 128, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.cells,
+                                                st.ncell, st.L, st.P, st.rk_weight2);
         return 1;
     }
     switch (st.prec) {
