@@ -35,6 +35,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
 BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1}
+# multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
+BYTES_PER_LU_MP = 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1
 DTYPE = {0: "f64", 1: "f32", 2: "f16"}
 
 
@@ -44,7 +46,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=256, help="lattice edge")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3"],
+                    help="c2: singlephase packing permeability (default); c1: multiphase tube drainage; "
+                         "c3: multiphase packing drainage")
+    ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
     ap.add_argument("--porosity", type=float, default=0.22)
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
@@ -60,15 +65,32 @@ def dist_env():
     return world, rank, local
 
 
-def workload(n, porosity, precision, device=0):
-    from mflbm import geometry
-    from mflbm.solver import make_params
-    p = make_params(multiphase=0, nx=n, ny=n, nz=n, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
-                    wall_y_min=0, wall_y_max=0, wall_z_min=0, wall_z_max=0, inlet_bc=0, outlet_bc=0, mrt=1,
-                    la_nu1=1.0 / 6.0, force_z=1e-6, precision=precision, strict_fp=0, device=device)
-    wg = geometry.sphere_packing((n, n, n), porosity, mean_r=8.0, sd_r=2.0, seed=2024)
-    walls, pore, _ = geometry.set_walls(p, wg)
-    return p, walls, pore
+def workload(args, device=0):
+    from mflbm import workloads
+    if args.workload == "c1":
+        case = workloads.tube_drainage(device=device)
+        desc = ("multiphase colour-gradient drainage, 64x64x160 tube (r=30) with a sphere (r=14), phi=+1 for z<28, "
+                "tau=1, gamma=0.01, theta=45, inlet velocity 1e-4, convective outlet, FP64")
+    elif args.workload == "c3":
+        case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, device=device)
+        desc = (f"multiphase drainage, {args.n}^2x{args.n} sphere packing porosity 0.22 + 32-layer buffers, "
+                "inlet velocity 5e-5, gamma=0.01, theta=30, FP64")
+    else:
+        case = workloads.packing_permeability(n=args.n, porosity=args.porosity, precision=args.precision,
+                                              device=device)
+        desc = (f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity} "
+                "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, F_z=1e-6, tau=1, "
+                "MRT preset 1")
+    return case, desc
+
+
+def setup(sim, case):
+    sim.set_geometry(case["walls"], case.get("solid"), case.get("fluid"), case.get("w_in"))
+    if case["params"].multiphase:
+        sim.init_equilibrium(case["phi"])
+        sim.color_gradient()
+    else:
+        sim.init_equilibrium()
 
 
 class ClockSampler:
@@ -125,13 +147,13 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(p, walls, pore, steps):
+def cpu_baseline(case, steps):
     """The CPU restatement of the reference (all host threads) on the same workload."""
     import pyoracle
+    p, pore = case["params"], case["pore"]
     threads = os.cpu_count() or 1
     o = pyoracle.Oracle(p, variant="fast", threads=threads)
-    o.set_geometry(walls)
-    o.init_equilibrium()
+    setup(o, case)
     o.run(1, 2)  # first-touch and warm-up
     t0 = time.perf_counter()
     o.run(3, steps)
@@ -146,14 +168,15 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    p, walls, pore = workload(args.n, args.porosity, 0)
+    args.precision = 0
+    case, desc = workload(args)
+    p, pore = case["params"], case["pore"]
     steps = max(1, min(args.steps, args.cpu_sample_steps))
     import pyoracle
     threads = os.cpu_count() or 1
     o = pyoracle.Oracle(p, variant="fast", threads=threads)
-    o.set_geometry(walls)
-    o.init_equilibrium()
-    o.run(1, max(args.warmup, 0) and 2)
+    setup(o, case)
+    o.run(1, 2)
     t0 = time.perf_counter()
     o.run(3, steps)
     dt = time.perf_counter() - t0
@@ -161,8 +184,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity}, "
-                                   "periodic xyz, F_z=1e-6, tau=1, MRT preset 1", "fluid_nodes": pore},
+            "config": {"workload": desc, "fluid_nodes": pore},
             "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
                              "sample": f"{steps} steps of the full workload; the Fortran reference cannot be built "
                                        "(no Fortran compiler or MPI), so its C++ restatement runs instead"},
@@ -184,10 +206,10 @@ def main():
         dist.init_process_group("nccl")
 
     from mflbm import Solver
-    p, walls, pore = workload(args.n, args.porosity, args.precision, device=local)
+    case, desc = workload(args, device=local)
+    p, pore = case["params"], case["pore"]
     sim = Solver(p)
-    sim.set_geometry(walls)
-    sim.init_equilibrium()
+    setup(sim, case)
     # warm-up (graph capture, first touch)
     sim.run(1, max(args.warmup, 3))
     sim.synchronize()
@@ -223,17 +245,18 @@ def main():
     try:
         rs = args.e2e_round
         state = sim.download_state()
-        f_host = torch.from_numpy(state["f"]).pin_memory().numpy()
+        pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy() for k, v in state.items()}
         barrier()
         t0 = time.perf_counter()
         nround = max(1, args.steps // rs)
         for r in range(nround):
-            sim.upload_state(f_host)
+            sim.upload_state(pinned["f"], pinned.get("g"), pinned.get("phi"), pinned.get("f_convec"),
+                             pinned.get("g_convec"), pinned.get("phi_convec"))
             sim.run(2, rs)
             prof_z, scal, status = sim.monitor()
         e2e_s = time.perf_counter() - t0
-        h2d = f_host.nbytes
-        d2h = 2 * p.nz * 8 + 3 * 8 + 4
+        h2d = sum(v.nbytes for k, v in pinned.items() if k != "f_convec" or p.outlet_bc == 1)
+        d2h = (7 if p.multiphase else 2) * p.nz * 8 + 3 * 8 + 4
         e2e = {"value": world * pore * rs * nround / e2e_s / 1e6, "unit": "MLUPS",
                "h2d_bytes_per_step": h2d / rs, "d2h_bytes_per_step": d2h / rs,
                "round": f"upload full state (pinned) + {rs} steps + monitor readback"}
@@ -241,7 +264,9 @@ def main():
         e2e = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
 
     collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
-    bpl = BYTES_PER_LU[args.precision]
+    elt = 8 if (p.multiphase or args.precision == 0) else (4 if args.precision == 1 else 2)
+    state_bytes = (2 if p.multiphase else 1) * 19 * elt * (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
+    bpl = BYTES_PER_LU_MP if p.multiphase else BYTES_PER_LU[args.precision]
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -261,7 +286,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(p, walls, pore, args.cpu_sample_steps)
+            cpu = cpu_baseline(case, args.cpu_sample_steps)
         except Exception as exc:
             cpu = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
 
@@ -269,19 +294,18 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
-            "config": {"workload": f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity} "
-                                   "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, "
-                                   "F_z=1e-6, tau=1, MRT preset 1",
-                       "lattice": [args.n] * 3, "fluid_nodes": pore, "replicas": world,
-                       "l2": f"state {19 * 8 * (args.n + 2) ** 3 / 1e9:.1f} GB >> 129 MB L2, no flush needed",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[0 if p.multiphase else args.precision],
+            "data": "synthetic",
+            "config": {"workload": desc, "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": pore, "replicas": world,
+                       "l2": f"state {state_bytes / 1e9:.2f} GB vs 129 MB L2"
+                             + (": no flush needed" if state_bytes > 4 * 129e6 else ": inputs smaller than L2"),
                        "timed_path": "per-step launches with events around each collision sweep",
                        "graph_replay_mlups": graph_mlups},
             "e2e": e2e,
             "gpu_launches": prof["kernel_launches"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "bytes_per_lu": bpl, "peak_source": "measured (MEASURED_PEAKS.json)",
-                         "kernel": "k_sp_step", "avg_launch_ms": collide_avg_s * 1e3},
+                         "kernel": "k_mp_step" if p.multiphase else "k_sp_step", "avg_launch_ms": collide_avg_s * 1e3},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -1,0 +1,69 @@
+"""The 64x64x160 tube-drainage case after 2000 steps: GPU against the oracle.
+
+strict build: bit-identical phi, PDFs and convective memory at ntime = 2000 (even).
+default (FMA) build: max|dphi| <= 1e-6, max|du| <= 1e-10, |dS|/S <= 1e-10 against the
+oracle, velocities from compute_macro_vars (valid after even steps).
+"""
+import numpy as np
+import pytest
+
+from mflbm import Solver
+from mflbm.workloads import tube_drainage
+from pyoracle import Oracle
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+STEPS = 2000
+
+
+def _setup(sim, case):
+    sim.set_geometry(case["walls"], case["solid"], case["fluid"], case["w_in"])
+    sim.init_equilibrium(case["phi"])
+    sim.color_gradient()
+
+
+@pytest.fixture(scope="module")
+def oracle_result():
+    case = tube_drainage(strict_fp=1)
+    orc = Oracle(case["params"])
+    _setup(orc, case)
+    orc.run(1, STEPS)
+    st = orc.download_state()
+    sat = orc.saturation()
+    mac = orc.macro()
+    orc.close()
+    return case, st, sat, mac
+
+
+def test_strict_bit_identical_after_2000_steps(oracle_result):
+    case, st, sat, _ = oracle_result
+    gpu = Solver(case["params"])
+    _setup(gpu, case)
+    gpu.run(1, STEPS)
+    a = gpu.download_state()
+    for k in ("phi", "f", "g", "f_convec", "g_convec", "phi_convec"):
+        assert np.array_equal(a[k], st[k]), (k, np.abs(a[k] - st[k]).max())
+    # identical state; the FP64 sums over ~5e5 nodes differ only in summation order
+    np.testing.assert_allclose(gpu.saturation(), sat, rtol=1e-11)
+    gpu.close()
+
+
+def test_fma_build_within_tolerance_after_2000_steps(oracle_result):
+    case, st, sat, mac = oracle_result
+    p = case["params"]
+    p.strict_fp = 0
+    gpu = Solver(p)
+    _setup(gpu, case)
+    gpu.run(1, STEPS)
+    a = gpu.download_state()
+    inner = (slice(4, -4),) * 3
+    dphi = np.abs(a["phi"][inner] - st["phi"][inner]).max()
+    m = gpu.macro()
+    du = max(np.abs(m[k][1:-1, 1:-1, 1:-1] - mac[k][1:-1, 1:-1, 1:-1]).max() for k in ("u", "v", "w"))
+    v1, v2 = gpu.saturation()
+    s_gpu, s_orc = v1 / (v1 + v2), sat[0] / (sat[0] + sat[1])
+    print(f"FMA build after {STEPS} steps: max|dphi|={dphi:.3e} max|du|={du:.3e} dS/S={abs(s_gpu - s_orc) / s_orc:.3e}")
+    assert dphi <= 1e-6
+    assert du <= 1e-10
+    assert abs(s_gpu - s_orc) / s_orc <= 1e-10
+    gpu.close()
