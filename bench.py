@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
     ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-convergence", action="store_true",
+                    help="skip the time-to-steady permeability study (singlephase workload only)")
+    ap.add_argument("--conv-tol", type=float, default=1e-7)
     return ap.parse_args()
 
 
@@ -164,6 +167,38 @@ def cpu_baseline(case, steps):
                       f"C++ restatement -O3, OpenMP {threads} threads, {dt:.2f} s"}
 
 
+def convergence_study(args, case, device):
+    """Time-to-steady permeability of each storage form on the same geometry.
+
+    Every form starts from rest and runs until |du|/u < tol between checks 100 steps
+    apart (the monitor_timer role); k = nu * u_mean / F_z.  Wall time is the host clock
+    around the whole loop (graph-replayed steps plus the FP64 monitor reductions and
+    their read-back).  Errors are relative to the FP64 form."""
+    import copy
+    from mflbm import Solver
+    from mflbm.permeability import run_to_steady
+    out = {"tol": args.conv_tol, "check_every": 100, "forms": {}}
+    base = None
+    for prec in (0, 1, 2):
+        p = copy.copy(case["params"])
+        p.precision = prec
+        with Solver(p) as sim:
+            sim.set_geometry(case["walls"])
+            sim.init_equilibrium()
+            sim.run(1, 100)          # graph capture outside the clock
+            sim.init_equilibrium()
+            sim.synchronize()
+            r = run_to_steady(sim, p, check_every=100, tol=args.conv_tol, max_steps=200000)
+        form = {"k": r.k, "steps": r.steps, "seconds": r.seconds, "converged": r.converged, "status": r.status}
+        if prec == 0:
+            base = r
+        else:
+            form["k_rel_err_vs_fp64"] = abs(r.k - base.k) / abs(base.k)
+            form["wall_time_ratio_fp64_over_form"] = base.seconds / r.seconds
+        out["forms"][DTYPE[prec]] = form
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -252,7 +287,7 @@ def main():
         for r in range(nround):
             sim.upload_state(pinned["f"], pinned.get("g"), pinned.get("phi"), pinned.get("f_convec"),
                              pinned.get("g_convec"), pinned.get("phi_convec"))
-            sim.run(2, rs)
+            sim.run(1, rs)           # the uploaded state follows an even step
             prof_z, scal, status = sim.monitor()
         e2e_s = time.perf_counter() - t0
         h2d = sum(v.nbytes for k, v in pinned.items() if k != "f_convec" or p.outlet_bc == 1)
@@ -279,7 +314,8 @@ def main():
     if os.path.exists(tf):
         try:
             t = json.load(open(tf))
-            traffic = t["bytes_per_fluid_node"] * pore
+            key = DTYPE[0 if p.multiphase else args.precision]
+            traffic = t[key] * pore if (key in t and not p.multiphase) else None
         except Exception:
             traffic = None
 
@@ -309,8 +345,14 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
-        print(json.dumps(line), flush=True)
     sim.close()
+    if rank == 0 and args.workload == "c2" and not args.no_convergence:
+        try:
+            line["convergence"] = convergence_study(args, case, local)
+        except Exception as exc:
+            line["convergence"] = {"error": str(exc)[:200]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0

@@ -288,6 +288,9 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
         }
     }
     c->st.fold = fold_rates<double>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
+    c->st.fold.fz = P.force_z;
+    c->st.fold32 = fold_rates<float>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
+    c->st.fold32.fz = (float)P.force_z;
     c->st.multiphase = p.multiphase;
     c->st.prec = p.precision;
     c->st.ref = 1.0f;

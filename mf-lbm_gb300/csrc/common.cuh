@@ -98,6 +98,7 @@ template <class R> struct MrtFold {
     R wi_m, wi_f;              // piww'  (/24)
     R o_m, o_eq, o_f;          // pxy', pyz', pzx' (/4)
     R t_m;                     // t'     (/8)
+    R fz;                      // body force along z (singlephase)
 };
 
 template <class R>
@@ -128,6 +129,7 @@ __host__ __device__ __forceinline__ MrtFold<R> fold_rates(double s_e, double s_e
     c.o_eq = R(s_nu / 4.0);
     c.o_f = R((1.0 - 0.5 * s_nu) / 4.0);
     c.t_m = R((1.0 - s_t) / 8.0);
+    c.fz = R(0.0);
     return c;
 }
 

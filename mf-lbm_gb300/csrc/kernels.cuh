@@ -319,8 +319,8 @@ __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R
 // ---------------------------------------------------------------------------------
 template <class S, bool ODD>
 __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
-                                                 const Layout L, const StepParams P, const MrtFold<double> fold,
-                                                 const float ref, const float scale) {
+                                                 const Layout L, const StepParams P,
+                                                 const MrtFold<typename Store<S>::R> cf, const float scale) {
     using St = Store<S>;
     using R = typename St::R;
     // one thread per fluid node: the sorted fluid-cell list keeps every lane busy
@@ -332,35 +332,26 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
         if (ODD)
-            ft[q] = St::ld(f, (int64_t)q * L.qs + c - qoff(L, q), R(WREST(q) * ref), inv_scale);
+            ft[q] = St::ld(f, (int64_t)q * L.qs + c - qoff(L, q), R(WREST(q)), inv_scale);
         else
-            ft[q] = St::ld(f, (int64_t)OPP(q) * L.qs + c, R(WREST(q) * ref), inv_scale);
+            ft[q] = St::ld(f, (int64_t)OPP(q) * L.qs + c, R(WREST(q)), inv_scale);
     }
 #ifdef MFLBM_STRICT
     const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
                   ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
     mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
 #else
-    MrtFold<R> cf;
-    cf.e_m = R(fold.e_m); cf.e_den = R(fold.e_den); cf.e_u2 = R(fold.e_u2); cf.e_f = R(fold.e_f);
-    cf.e2_m = R(fold.e2_m); cf.e2_u2 = R(fold.e2_u2); cf.e2_f = R(fold.e2_f);
-    cf.q_m = R(fold.q_m); cf.q_u = R(fold.q_u); cf.q_f = R(fold.q_f);
-    cf.x3_m = R(fold.x3_m); cf.x3_eq = R(fold.x3_eq); cf.x3_f = R(fold.x3_f);
-    cf.xi_m = R(fold.xi_m); cf.xi_f = R(fold.xi_f);
-    cf.w_m = R(fold.w_m); cf.w_eq = R(fold.w_eq); cf.w_f = R(fold.w_f);
-    cf.wi_m = R(fold.wi_m); cf.wi_f = R(fold.wi_f);
-    cf.o_m = R(fold.o_m); cf.o_eq = R(fold.o_eq); cf.o_f = R(fold.o_f);
-    cf.t_m = R(fold.t_m);
-    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), R(P.force_z), cf);
+    // force_z travels in the same coefficient set, already converted to R on the host
+    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
 #endif
     const R sc = R(scale);
     if (ODD) {
-        St::st(f, c, ft[0], R(WREST(0) * ref), sc);
+        St::st(f, c, ft[0], R(WREST(0)), sc);
 #pragma unroll
-        for (int q = 1; q < 19; ++q) St::st(f, (int64_t)OPP(q) * L.qs + c + qoff(L, q), ft[q], R(WREST(q) * ref), sc);
+        for (int q = 1; q < 19; ++q) St::st(f, (int64_t)OPP(q) * L.qs + c + qoff(L, q), ft[q], R(WREST(q)), sc);
     } else {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) St::st(f, (int64_t)q * L.qs + c, ft[q], R(WREST(q) * ref), sc);
+        for (int q = 0; q < 19; ++q) St::st(f, (int64_t)q * L.qs + c, ft[q], R(WREST(q)), sc);
     }
 }
 
@@ -400,14 +391,25 @@ __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double 
         ft[q] = ft[q] + b;
         rho2 = q == 0 ? b : rho2 + b;
     }
+#ifdef MFLBM_STRICT
     const double ph = (rho1 - rho2) / (rho1 + rho2);
+#else
+    const double inv_den = 1.0 / (rho1 + rho2);   // one division serves phi and the recolouring
+    const double ph = (rho1 - rho2) * inv_den;
+#endif
     phi[L.i4(i, j, k)] = ph;
     const double cx = cnx[w2], cy = cny[w2], cz = cnz[w2];
     double tmp = 0.5 * P.gamma * curv[L.i1(i, j, k)] * cnorm[w2];
     const double fx = tmp * cx;
     const double fy = tmp * cy;
     const double fz = tmp * cz + P.force_z;
+#ifdef MFLBM_STRICT
     const double omega = 1.0 / (6.0 / ((1.0 + ph) * P.la_nui1 + (1.0 - ph) * P.la_nui2) + 0.5);
+#else
+    // 1/(6/X + 1/2) = X / (6 + X/2): one division
+    const double visc = (1.0 + ph) * P.la_nui1 + (1.0 - ph) * P.la_nui2;
+    const double omega = visc / (6.0 + 0.5 * visc);
+#endif
     double s_e, s_e2, s_pi, s_q, s_t;
     if (P.mrt == 1) {
         s_e = omega; s_e2 = omega; s_pi = omega;
@@ -430,8 +432,13 @@ __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double 
     mrt_collide_pairs<double, true, false>(ft, den, fx, fy, fz, cf);
 #endif
     // recolouring (Kernel_multiphase.F90:272-315)
+#ifdef MFLBM_STRICT
     const double tmp1 = rho1 / den;
     tmp = rho1 * rho2 * P.beta / den;
+#else
+    const double tmp1 = rho1 * inv_den;
+    tmp = rho1 * rho2 * P.beta * inv_den;
+#endif
     f[c] = tmp1 * ft[0];
     g[c] = ft[0] * (1.0 - tmp1);
 #pragma unroll
@@ -939,6 +946,11 @@ __global__ void __launch_bounds__(256) k_normals(const double *__restrict__ phi,
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
     if (i > L.nx + 2 || j > L.ny + 2) return;
+    const int64_t id = L.i2(i, j, k);
+    if (walls[id] == 1) {  // the reference zeroes normals at wall nodes (Phase_gradient.F90:65-69)
+        cnx[id] = 0.0; cny[id] = 0.0; cnz[id] = 0.0; cnorm[id] = 0.0;
+        return;
+    }
     auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
     double gx = ISO4_1 * (P(1, 0, 0) - P(-1, 0, 0)) +
                 ISO4_2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
@@ -947,11 +959,15 @@ __global__ void __launch_bounds__(256) k_normals(const double *__restrict__ phi,
     double gz = ISO4_1 * (P(0, 0, 1) - P(0, 0, -1)) +
                 ISO4_2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
     double cn = sqrt(gx * gx + gy * gy + gz * gz);
-    const int64_t id = L.i2(i, j, k);
-    if (cn < 1e-6 || walls[id] == 1) {
+    if (cn < 1e-6) {
         gx = 0.0; gy = 0.0; gz = 0.0; cn = 0.0;
     } else {
+#ifdef MFLBM_STRICT
         gx = gx / cn; gy = gy / cn; gz = gz / cn;
+#else
+        const double inv = 1.0 / cn;
+        gx = gx * inv; gy = gy * inv; gz = gz * inv;
+#endif
     }
     cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
 }
@@ -1014,11 +1030,20 @@ __global__ void k_extrap_normals(double *__restrict__ cnx, double *__restrict__ 
 
 // curvature over [1, n]^3 (:113-201)
 __global__ void __launch_bounds__(256) k_curvature(const double *__restrict__ cnx, const double *__restrict__ cny,
-                                                   const double *__restrict__ cnz, double *__restrict__ curv, const Layout L) {
+                                                   const double *__restrict__ cnz, double *__restrict__ curv,
+                                                   const int8_t *__restrict__ walls, const Layout L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > L.nx || j > L.ny) return;
+#ifndef MFLBM_STRICT
+    // curv is read only at fluid nodes (collision, compute_macro_vars masks walls); the
+    // default build leaves 0 at wall nodes instead of the reference's unused value
+    if (walls[L.i2(i, j, k)] != 0) {
+        curv[L.i1(i, j, k)] = 0.0;
+        return;
+    }
+#endif
     auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
     auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
     auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };

@@ -32,7 +32,8 @@ struct DevState {
     double *stage;         // one FP64 plane of the halo-1 box (conversion staging)
     const int32_t *cells;  // padded-layout index of every interior fluid node, ascending
     int ncell;
-    MrtFold<double> fold;  // singlephase MRT coefficients of the default build
+    MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
+    MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
 };
 
 struct KernelTable {

@@ -14,14 +14,19 @@ inline dim3 row_block(int nx) {
 template <class S> S *fs(const DevState &st) { return reinterpret_cast<S *>(st.f); }
 template <class S> S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g); }
 
+template <class R> const MrtFold<R> &fold_of(const DevState &st);
+template <> const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
+template <> const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
+
 template <class S>
 int collide_t(const DevState &st, bool odd, cudaStream_t s) {
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
+    const auto &cf = fold_of<typename Store<S>::R>(st);
     if (odd)
-        k_sp_step<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, st.fold, st.ref, st.scale);
+        k_sp_step<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
     else
-        k_sp_step<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, st.fold, st.ref, st.scale);
+        k_sp_step<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
     return 1;
 }
 
@@ -153,7 +158,7 @@ int color_gradient(const DevState &st, cudaStream_t s) {
         const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
         const dim3 b(bx, 256 / bx);
         const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
-        k_curvature<<<g, b, 0, s>>>(st.cnx, st.cny, st.cnz, st.curv, L);
+        k_curvature<<<g, b, 0, s>>>(st.cnx, st.cny, st.cnz, st.curv, st.walls, L);
     }
     return n_launch;
 }
