@@ -36,7 +36,7 @@ import numpy as np  # noqa: E402
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
 BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
-BYTES_PER_LU_MP = 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1
+BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1}
 DTYPE = {0: "f64", 1: "f32", 2: "f16"}
 
 
@@ -46,9 +46,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"],
                     help="c2: singlephase packing permeability (default); c1: multiphase tube drainage; "
-                         "c3: multiphase packing drainage")
+                         "c3: multiphase packing drainage; c4: batched permeability ensemble to steady state")
+    ap.add_argument("--samples", type=int, default=256, help="c4: ensemble size")
+    ap.add_argument("--c4-fp64", action="store_true", help="c4: also run the FP64 ensemble for per-sample k errors")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
     ap.add_argument("--porosity", type=float, default=0.22)
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
@@ -58,6 +60,8 @@ def parse():
     ap.add_argument("--no-convergence", action="store_true",
                     help="skip the time-to-steady permeability study (singlephase workload only)")
     ap.add_argument("--conv-tol", type=float, default=1e-7)
+    ap.add_argument("--layout", type=int, default=0, choices=[0, 1, 2],
+                    help="singlephase storage: 0 auto (fluid list when possible), 1 dense, 2 fluid list")
     return ap.parse_args()
 
 
@@ -71,16 +75,17 @@ def dist_env():
 def workload(args, device=0):
     from mflbm import workloads
     if args.workload == "c1":
-        case = workloads.tube_drainage(device=device)
+        case = workloads.tube_drainage(device=device, precision=args.precision)
         desc = ("multiphase colour-gradient drainage, 64x64x160 tube (r=30) with a sphere (r=14), phi=+1 for z<28, "
-                "tau=1, gamma=0.01, theta=45, inlet velocity 1e-4, convective outlet, FP64")
+                f"tau=1, gamma=0.01, theta=45, inlet velocity 1e-4, convective outlet, {DTYPE[args.precision]}")
     elif args.workload == "c3":
-        case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, device=device)
+        case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, device=device, precision=args.precision)
         desc = (f"multiphase drainage, {args.n}^2x{args.n} sphere packing porosity 0.22 + 32-layer buffers, "
-                "inlet velocity 5e-5, gamma=0.01, theta=30, FP64")
+                f"inlet velocity 5e-5, gamma=0.01, theta=30, {DTYPE[args.precision]}")
     else:
         case = workloads.packing_permeability(n=args.n, porosity=args.porosity, precision=args.precision,
                                               device=device)
+        case["params"].layout = args.layout
         desc = (f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity} "
                 "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, F_z=1e-6, tau=1, "
                 "MRT preset 1")
@@ -228,10 +233,59 @@ def run_reference(args):
     return 0
 
 
+def ensemble_study(args):
+    """c4: every sample of the ensemble from rest to |du|/u < tol (checks every 100
+    steps), converged samples leaving the sweep; value = fluid-node updates per second,
+    samples/s in config.  With --c4-fp64 the FP64 ensemble of the same seeds gives the
+    per-sample permeability error of the storage form."""
+    import torch
+    from mflbm import workloads
+    from mflbm.ensemble import Ensemble, run_to_steady, tune_cached
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    prec = args.precision if args.precision else 1
+    t0 = time.perf_counter()
+    case = workloads.packing_ensemble(n_samples=args.samples, precision=prec, device=local)
+    gen_s = time.perf_counter() - t0
+    res = {}
+    for pr in ([prec, 0] if args.c4_fp64 else [prec]):
+        case["params"].precision = pr
+        with Ensemble(case["params"], case["samples"]) as ens:
+            tune = tune_cached(ens, None, steps=6)
+            ens.init()
+            torch.cuda.synchronize()
+            with ClockSampler(local) as clk:
+                r = run_to_steady(ens, case["nf"], check_every=100, tol=args.conv_tol, max_steps=200000)
+            res[pr] = (r, tune, clk.summary(), ens.info())
+    r, tune, clocks, info = res[prec]
+    line = {"metric": METRIC, "value": r.fluid_updates / r.seconds / 1e6, "unit": "MLUPS", "n_gpus": 1,
+            "steps": int(r.steps.max()), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec], "data": "synthetic",
+            "config": {"workload": f"batched permeability ensemble: {args.samples} sphere packings, edges U[48,160], "
+                                   "porosity U[0.15,0.35], F_z=1e-6, tau=1, MRT preset 1, periodic xyz, "
+                                   f"to |du|/u<{args.conv_tol} every 100 steps",
+                       "samples": args.samples, "samples_per_s": args.samples / r.seconds,
+                       "wall_s": r.seconds, "converged": int(r.converged.sum()),
+                       "total_nodes": int(sum(e ** 3 for e in case["edges"])), "fluid_nodes": int(case["nf"].sum()),
+                       "fluid_updates": r.fluid_updates, "generate_s": gen_s, "launch": tune.get("chosen"),
+                       "tuner": tune.get("candidates")},
+            "clocks": clocks, "gpu_launches": None}
+    if args.c4_fp64:
+        r64 = res[0][0]
+        err = np.abs(r.k - r64.k) / np.abs(r64.k)
+        line["config"]["k_rel_err_vs_fp64"] = {"max": float(err.max()), "median": float(np.median(err))}
+        line["config"]["fp64_wall_s"] = r64.seconds
+        line["config"]["fp64_samples_per_s"] = args.samples / r64.seconds
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "c4":
+        return ensemble_study(args)
     world, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -298,10 +352,11 @@ def main():
     except Exception as exc:  # keep the device-timed number even if e2e fails
         e2e = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
 
+    layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
     collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
-    elt = 8 if (p.multiphase or args.precision == 0) else (4 if args.precision == 1 else 2)
+    elt = 8 if args.precision == 0 else (4 if args.precision == 1 else 2)
     state_bytes = (2 if p.multiphase else 1) * 19 * elt * (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
-    bpl = BYTES_PER_LU_MP if p.multiphase else BYTES_PER_LU[args.precision]
+    bpl = BYTES_PER_LU_MP[args.precision] if p.multiphase else BYTES_PER_LU[args.precision]
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -314,7 +369,7 @@ def main():
     if os.path.exists(tf):
         try:
             t = json.load(open(tf))
-            key = DTYPE[0 if p.multiphase else args.precision]
+            key = f"{DTYPE[args.precision]}_{layout}"
             traffic = t[key] * pore if (key in t and not p.multiphase) else None
         except Exception:
             traffic = None
@@ -330,9 +385,10 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[0 if p.multiphase else args.precision],
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
             "data": "synthetic",
             "config": {"workload": desc, "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": pore, "replicas": world,
+                       "layout": layout,
                        "l2": f"state {state_bytes / 1e9:.2f} GB vs 129 MB L2"
                              + (": no flush needed" if state_bytes > 4 * 129e6 else ": inputs smaller than L2"),
                        "timed_path": "per-step launches with events around each collision sweep",
@@ -341,7 +397,8 @@ def main():
             "gpu_launches": prof["kernel_launches"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "bytes_per_lu": bpl, "peak_source": "measured (MEASURED_PEAKS.json)",
-                         "kernel": "k_mp_step" if p.multiphase else "k_sp_step", "avg_launch_ms": collide_avg_s * 1e3},
+                         "kernel": "k_mp_step" if p.multiphase else ("k_sp_list" if layout == "list" else "k_sp_step"),
+                         "avg_launch_ms": collide_avg_s * 1e3},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

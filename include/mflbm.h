@@ -49,7 +49,7 @@
 extern "C" {
 #endif
 
-#define MFLBM_ABI_VERSION 1
+#define MFLBM_ABI_VERSION 2
 
 /* status codes */
 #define MFLBM_OK        0
@@ -70,6 +70,16 @@ extern "C" {
 #define MFLBM_FP64 0   /* plain drop-in: FP64 storage, FP64 collision               */
 #define MFLBM_FP32 1   /* FP32 storage, FP32 collision                              */
 #define MFLBM_FP16 2   /* FP16 storage of scaled deviations from the rest state, FP32 collision */
+
+/* PDF storage layout (no counterpart in the reference, which stores every cell).
+ * DENSE: one plane per direction over the halo-1 box, as the reference's arrays.
+ * LIST:  only the fluid nodes plus one slot per solid bounce-back link, with an
+ *        18-entry neighbour table; singlephase samples that are periodic or walled in
+ *        every direction (no inlet/outlet).  Same update, same results.
+ * AUTO:  LIST when the geometry allows it, else DENSE (decided by mflbm_set_geometry). */
+#define MFLBM_LAYOUT_AUTO  0
+#define MFLBM_LAYOUT_DENSE 1
+#define MFLBM_LAYOUT_LIST  2
 
 /* Run parameters: the subset of simulation_control.txt that the per-step path
  * reads, after the reference's own host-side derivations
@@ -92,6 +102,7 @@ typedef struct mflbm_params {
     int32_t precision;        /* MFLBM_FP64 / MFLBM_FP32 / MFLBM_FP16                      */
     int32_t strict_fp;        /* 1: no FMA contraction (bit-identical to an IEEE restatement) */
     int32_t device;           /* CUDA device ordinal                                       */
+    int32_t layout;           /* PDF storage layout: MFLBM_LAYOUT_AUTO / _DENSE / _LIST        */
     double  la_nu1;           /* fluid1_viscosity (singlephase: fluid_viscosity)           */
     double  la_nu2;           /* fluid2_viscosity                                          */
     double  gamma;            /* surface_tension                                           */
@@ -124,6 +135,11 @@ typedef struct mflbm_ctx mflbm_ctx;
 
 /* Library ABI version (MFLBM_ABI_VERSION). */
 int32_t mflbm_version(void);
+
+/* Storage layout in use: MFLBM_LAYOUT_DENSE or MFLBM_LAYOUT_LIST, or
+ * MFLBM_LAYOUT_AUTO while a singlephase context has no geometry yet.
+ * No counterpart in the reference. */
+int32_t mflbm_layout(const mflbm_ctx *ctx);
 
 /* Allocate a context and its device arrays.  Replaces MemAllocate_multi /
  * MemAllocate (Init_multiphase.F90:583-828; singlephase Initialization.F90:380-516)
@@ -232,6 +248,55 @@ int32_t mflbm_get_profile(mflbm_ctx *ctx, double *region_ms, double *collide_ms,
  * MFLBM_ERANGE.  Errors are reported through mflbm_last_error(NULL). */
 int32_t mflbm_saturation_noalloc(const double *phi, const int8_t *walls, int32_t nx, int32_t ny, int32_t nz,
                                  double *vol, void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * Ensembles: many singlephase samples of uneven sizes updated together in one
+ * fluid-list arena (no counterpart in the reference, which runs one sample per job).
+ * The samples share `common` (precision, mrt, la_nu1, force_z, periodic and wall flags,
+ * device; nx/ny/nz are ignored) and each has its own dims[3*s..3*s+2] = nx, ny, nz and
+ * halo-2 wall array walls[s] (Fortran order, 1 = solid).  Every direction must be
+ * periodic or walled (no inlet/outlet).  Errors: mflbm_ensemble_last_error.
+ * --------------------------------------------------------------------------------- */
+typedef struct mflbm_ensemble mflbm_ensemble;
+
+int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, const int32_t *dims,
+                              const int8_t *const *walls, mflbm_ensemble **out);
+void mflbm_ensemble_destroy(mflbm_ensemble *ens);
+/* Last error of ens, or of the last failed mflbm_ensemble_create when ens is NULL. */
+const char *mflbm_ensemble_last_error(const mflbm_ensemble *ens);
+/* Rest state (equilibrium at rho = 1, u = 0) in every sample. */
+int32_t mflbm_ensemble_init(mflbm_ensemble *ens);
+/* active[s] = 0 drops sample s from the sweep (e.g. once converged); 1 keeps it. */
+int32_t mflbm_ensemble_set_active(mflbm_ensemble *ens, const int32_t *active);
+/* nsteps time steps of every active sample, starting with ntime0 (odd: stream+collide).
+ * Replayed from a CUDA graph captured on first use; asynchronous. */
+int32_t mflbm_ensemble_run(mflbm_ensemble *ens, int32_t ntime0, int32_t nsteps);
+/* Per-sample sum of w over the fluid nodes and max |u|^2 (valid after even steps);
+ * *status = MFLBM_FAILED on NaN or |u| > 0.5 in an active sample.  Returns
+ * MFLBM_ETIMEOUT when a grid barrier of the persistent kernel gave up (the ensemble
+ * must then be destroyed).  Synchronises. */
+int32_t mflbm_ensemble_flux(mflbm_ensemble *ens, double *w_sum, double *umax2, int32_t *status);
+/* Launch shape: threads per block (64..1024, multiple of 32) and persistent = 1 for one
+ * cooperative launch per run (grid barrier between steps) or 0 for one launch per step. */
+int32_t mflbm_ensemble_configure(mflbm_ensemble *ens, int32_t block, int32_t persistent);
+/* Times every launch shape over `steps` steps on the ensemble itself and applies the
+ * fastest; `report` (may be NULL) receives the timings as JSON.  Changes the PDF
+ * state: call mflbm_ensemble_init afterwards. */
+int32_t mflbm_ensemble_tune(mflbm_ensemble *ens, int32_t steps, char *report, int32_t report_len);
+/* Fluid nodes of the active samples and the launch shape in use. */
+int32_t mflbm_ensemble_info(const mflbm_ensemble *ens, int64_t *active_nodes, int32_t *block,
+                            int32_t *persistent, int32_t *grid);
+
+/* ---------------------------------------------------------------------------------
+ * Warm-start network building blocks (no counterpart in the reference).  Device
+ * pointers; `stream` is a cudaStream_t (NULL: the legacy default stream); `err` is a
+ * device int32 set to nonzero when a bounded device-side wait gave up.
+ * --------------------------------------------------------------------------------- */
+/* C[M][N] (fp32, row stride ldc) = (accumulate ? C : 0) + A[M][K] * B[N][K]^T with A, B
+ * bf16 (row strides lda, ldb), FP32 accumulation on the tcgen05 tensor cores.
+ * N % 16 == 0, K % 8 == 0, lda, ldb % 8 == 0, A and B 16-byte aligned. */
+int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
+                           int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t *err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -8,6 +8,9 @@ mf-lbm_gb300/mflbm/lib/libmflbm.so:
   csrc/kernels_strict.cu  the same kernels with --fmad=false (bit-identical to an IEEE
                           restatement that keeps the reference's operation order)
   csrc/noalloc.cu         mflbm_saturation_noalloc (fixed device scratch, no allocation)
+  csrc/listlayout.cpp     host construction of the fluid-list layout
+  csrc/ensemble.cu        batched samples in one fluid-list arena, launch-shape autotuner
+  csrc/nn_gemm.cu         BF16 tcgen05 GEMM (TMEM accumulators) of the warm-start network
 
 Only one -gencode (sm_103a) is built.  nvcc cross-compiles without a GPU, so this runs
 on the CPU build host and on the GPU host alike.
@@ -31,6 +34,9 @@ UNITS = {
     "kernels_fast.o": ("kernels_fast.cu", []),
     "kernels_strict.o": ("kernels_strict.cu", ["--fmad=false"]),
     "noalloc.o": ("noalloc.cu", []),
+    "listlayout.o": ("listlayout.cpp", []),
+    "ensemble.o": ("ensemble.cu", []),
+    "nn_gemm.o": ("nn_gemm.cu", []),
 }
 
 

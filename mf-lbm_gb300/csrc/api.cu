@@ -10,6 +10,7 @@
 // mflbm_run replays the same launches from CUDA graphs captured once per context.
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -17,6 +18,7 @@
 
 #include "../../include/mflbm.h"
 #include "kernels_api.h"
+#include "listlayout.h"
 
 using namespace mflbm;
 
@@ -31,6 +33,9 @@ struct mflbm_ctx {
     bool have_geometry = false;
     bool open_z = false;
     int64_t cells_cap = 0;
+    void *pdf = nullptr;          // PDF storage (dense planes or fluid-list arrays)
+    size_t pdf_bytes = 0;
+    std::vector<void *> list_bufs;  // neighbour table, cell map, link table, slice starts
     // graphs of whole even+odd step pairs
     cudaGraphExec_t g_pair = nullptr, g_block = nullptr;
     int block_pairs = 8;
@@ -94,7 +99,10 @@ int validate(const mflbm_params *p, std::string &err) {
             return MFLBM_EINVAL;
         }
         if (p->mrt < 1 || p->mrt > 4) { err = "mrt must be 1..4"; return MFLBM_EINVAL; }
-        if (p->precision != MFLBM_FP64) { err = "multiphase supports MFLBM_FP64 storage only"; return MFLBM_EINVAL; }
+        if (p->precision == MFLBM_FP16) {
+            err = "multiphase supports MFLBM_FP64 and MFLBM_FP32 storage (FP16 deviations cannot hold a vanishing species)";
+            return MFLBM_EINVAL;
+        }
         if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
     } else {
         if (p->iper == 1 && (p->wall_x_max == 1 || p->wall_x_min == 1)) {
@@ -123,7 +131,23 @@ int validate(const mflbm_params *p, std::string &err) {
         return MFLBM_EINVAL;
     }
     if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FP16) { err = "unknown precision"; return MFLBM_EINVAL; }
+    if (p->layout < MFLBM_LAYOUT_AUTO || p->layout > MFLBM_LAYOUT_LIST) { err = "unknown layout"; return MFLBM_EINVAL; }
+    if (p->layout == MFLBM_LAYOUT_LIST && (p->multiphase || p->inlet_bc != 0 || p->outlet_bc != 0)) {
+        err = "the fluid-list layout is singlephase without inlet/outlet boundary conditions";
+        return MFLBM_EINVAL;
+    }
     if (p->la_nu1 <= 0.0) { err = "la_nu1 must be positive"; return MFLBM_EINVAL; }
+    return MFLBM_OK;
+}
+
+int dalloc_bytes(mflbm_ctx *c, void **ptr, size_t bytes) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    c->allocs.push_back(p);
+    e = cudaMemsetAsync(p, 0, bytes, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync");
+    *ptr = p;
     return MFLBM_OK;
 }
 
@@ -135,6 +159,41 @@ template <class T> int dalloc(mflbm_ctx *c, T **ptr, int64_t count) {
     e = cudaMemsetAsync(p, 0, (size_t)count * sizeof(T), c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync");
     *ptr = reinterpret_cast<T *>(p);
+    return MFLBM_OK;
+}
+
+// cudaFree one tracked allocation
+void dfree(mflbm_ctx *c, void *ptr) {
+    if (!ptr) return;
+    for (size_t t = 0; t < c->allocs.size(); ++t)
+        if (c->allocs[t] == ptr) {
+            cudaFree(ptr);
+            c->allocs.erase(c->allocs.begin() + (long)t);
+            return;
+        }
+}
+
+// (re)allocate the PDF storage; zero-filled
+int alloc_pdf(mflbm_ctx *c, size_t bytes) {
+    if (c->pdf && c->pdf_bytes == bytes) return MFLBM_OK;
+    dfree(c, c->pdf);
+    c->pdf = nullptr;
+    c->pdf_bytes = 0;
+    int r = dalloc_bytes(c, &c->pdf, bytes);
+    if (r) return r;
+    c->pdf_bytes = bytes;
+    return MFLBM_OK;
+}
+
+// the dense planes of one or two species
+int alloc_dense(mflbm_ctx *c) {
+    const int nsp = c->p.multiphase ? 2 : 1;
+    const size_t plane = (size_t)19 * c->st.L.qs * c->elt;
+    int r = alloc_pdf(c, nsp * plane);
+    if (r) return r;
+    c->st.f = c->pdf;
+    c->st.g = c->p.multiphase ? (void *)((char *)c->pdf + plane) : nullptr;
+    c->st.list = 0;
     return MFLBM_OK;
 }
 
@@ -207,6 +266,11 @@ int ready(mflbm_ctx *c) {
 extern "C" {
 
 int32_t mflbm_version(void) { return MFLBM_ABI_VERSION; }
+
+int32_t mflbm_layout(const mflbm_ctx *c) {
+    if (!c || !c->pdf) return MFLBM_LAYOUT_AUTO;
+    return c->st.list ? MFLBM_LAYOUT_LIST : MFLBM_LAYOUT_DENSE;
+}
 
 const char *mflbm_last_error(const mflbm_ctx *ctx) {
     return ctx ? ctx->err.c_str() : g_last_create_error.c_str();
@@ -293,6 +357,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     c->st.fold32.fz = (float)P.force_z;
     c->st.multiphase = p.multiphase;
     c->st.prec = p.precision;
+    c->st.felt = (p.multiphase && p.precision == MFLBM_FP32) ? 4 : 8;
     c->st.ref = 1.0f;
     c->st.scale = 4096.0f;
     c->st.rk_weight2 = 1.0 / std::sqrt(2.0) / 36.0;
@@ -300,16 +365,11 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     // device arrays (MemAllocate_multi, Init_multiphase.F90:583-828)
     const int nsp = p.multiphase ? 2 : 1;
     int r = MFLBM_OK;
-    {
-        void *pdf = nullptr;
-        const size_t bytes = (size_t)nsp * 19 * (size_t)L.qs * c->elt;
-        e = cudaMalloc(&pdf, bytes);
-        if (e != cudaSuccess) { r = cuda_fail(c, e, "cudaMalloc(PDF)"); goto fail_create; }
-        c->allocs.push_back(pdf);
-        e = cudaMemsetAsync(pdf, 0, bytes, c->stream);
-        if (e != cudaSuccess) { r = cuda_fail(c, e, "cudaMemsetAsync(PDF)"); goto fail_create; }
-        c->st.f = pdf;
-        c->st.g = p.multiphase ? (void *)((char *)pdf + (size_t)19 * L.qs * c->elt) : nullptr;
+    (void)nsp;
+    // the singlephase storage layout is settled by mflbm_set_geometry; the other cases
+    // are dense from the start
+    if (p.multiphase || p.layout == MFLBM_LAYOUT_DENSE || p.inlet_bc != 0 || p.outlet_bc != 0) {
+        if ((r = alloc_dense(c))) goto fail_create;
     }
     if ((r = dalloc(c, &c->st.walls, n2(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.w_in, nplane(p)))) goto fail_create;
@@ -319,14 +379,18 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.w, n1(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.rho, n1(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.mon, (int64_t)kMonNQ * p.nz))) goto fail_create;
-    if (p.precision != MFLBM_FP64 && (r = dalloc(c, &c->st.stage, n1(p)))) goto fail_create;
+    // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
+    // phase field when that is larger
+    if ((p.precision != MFLBM_FP64 || !p.multiphase) &&
+        (r = dalloc(c, &c->st.stage, p.multiphase ? std::max(n1(p), n4(p)) : n1(p)))) goto fail_create;
     if (p.multiphase) {
-        if ((r = dalloc(c, &c->st.phi, n4(p)))) goto fail_create;
-        if ((r = dalloc(c, &c->st.cnx, n2(p)))) goto fail_create;
-        if ((r = dalloc(c, &c->st.cny, n2(p)))) goto fail_create;
-        if ((r = dalloc(c, &c->st.cnz, n2(p)))) goto fail_create;
-        if ((r = dalloc(c, &c->st.cnorm, n2(p)))) goto fail_create;
-        if ((r = dalloc(c, &c->st.curv, n1(p)))) goto fail_create;
+        const size_t fe = (size_t)c->st.felt;
+        if ((r = dalloc_bytes(c, &c->st.phi, fe * n4(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.cnx, fe * n2(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.cny, fe * n2(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.cnz, fe * n2(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.cnorm, fe * n2(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.curv, fe * n1(p)))) goto fail_create;
         if ((r = dalloc(c, &c->st.gconv, nplane(p) * 19))) goto fail_create;
         if ((r = dalloc(c, &c->st.phiconv, nplane(p)))) goto fail_create;
     }
@@ -403,6 +467,51 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
         if (r) return r;
         c->st.fb = fbd;
     }
+    // storage layout of a singlephase run: the fluid list when the geometry allows it
+    if (!p.multiphase && p.layout != MFLBM_LAYOUT_DENSE && p.inlet_bc == 0 && p.outlet_bc == 0) {
+        ListLayout ll;
+        std::string why;
+        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why);
+        for (void *b : c->list_bufs) dfree(c, b);
+        c->list_bufs.clear();
+        if (ok) {
+            int r = alloc_pdf(c, (size_t)19 * ll.stride * c->elt);
+            if (r) return r;
+            int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *seg = nullptr;
+            if ((r = dalloc(c, &nb, 18 * ll.nf))) return r;
+            c->list_bufs.push_back(nb);
+            if ((r = dalloc(c, &cell1, ll.nf))) return r;
+            c->list_bufs.push_back(cell1);
+            if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * ll.nlink)))) return r;
+            c->list_bufs.push_back(link);
+            if ((r = dalloc(c, &seg, p.nz + 1))) return r;
+            c->list_bufs.push_back(seg);
+            CK(c, cudaMemcpy(nb, ll.nb.data(), sizeof(int32_t) * ll.nb.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(cell1, ll.cell1.data(), sizeof(int32_t) * ll.cell1.size(), cudaMemcpyHostToDevice));
+            if (ll.nlink) CK(c, cudaMemcpy(link, ll.link.data(), sizeof(int32_t) * ll.link.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(seg, ll.slice.data(), sizeof(int32_t) * ll.slice.size(), cudaMemcpyHostToDevice));
+            DevState &st = c->st;
+            st.list = 1;
+            st.f = c->pdf;
+            st.g = nullptr;
+            st.lstride = ll.stride;
+            st.nb = nb;
+            st.cell1 = cell1;
+            st.link = link;
+            st.nlink = ll.nlink;
+            st.nfl = (int)ll.nf;
+            st.lseg = seg;
+            st.ncell = 0;
+            c->st.ns = 0;
+            c->st.nf = 0;
+            CK(c, cudaDeviceSynchronize());
+            c->have_geometry = true;
+            return MFLBM_OK;
+        }
+        if (p.layout == MFLBM_LAYOUT_LIST) return fail(c, MFLBM_EINVAL, "fluid-list layout: " + why);
+        int r = alloc_dense(c);
+        if (r) return r;
+    }
     // sorted list of interior fluid nodes (walls == 0): the collision sweep runs one
     // thread per entry, so no lane idles on a solid node
     {
@@ -433,9 +542,35 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     return MFLBM_OK;
 }
 
+// FP64 host array -> device field (phi or a gradient field) of the context's field type
+static int field_put(mflbm_ctx *c, void *dev, const double *host, int64_t n) {
+    if (c->st.felt == 8) {
+        CK(c, cudaMemcpyAsync(dev, host, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        CK(c, cudaMemcpyAsync(c->st.stage, host, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        c->kt->field_in(c->st, dev, n, c->stream);
+        CK(c, cudaPeekAtLastError());
+    }
+    return MFLBM_OK;
+}
+
+// device field -> FP64 host array; synchronises the context stream
+static int field_get(mflbm_ctx *c, double *host, const void *dev, int64_t n) {
+    if (c->st.felt == 8) {
+        CK(c, cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        c->kt->field_out(c->st, dev, n, c->stream);
+        CK(c, cudaPeekAtLastError());
+        CK(c, cudaMemcpyAsync(host, c->st.stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
 int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *const *g, const double *phi,
                            const double *f_convec, const double *g_convec, const double *phi_convec) {
     if (!c) return MFLBM_EINVAL;
+    if (!c->pdf) return fail(c, MFLBM_ESTATE, "the PDF storage is laid out by mflbm_set_geometry; call it first");
     const mflbm_params &p = c->p;
     if (!f) return fail(c, MFLBM_EINVAL, "f is NULL");
     for (int q = 0; q < 19; ++q) if (!f[q]) return fail(c, MFLBM_EINVAL, "f[q] is NULL");
@@ -452,7 +587,7 @@ int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *c
         const double *const *src = s == 0 ? f : g;
         char *base = (char *)(s == 0 ? c->st.f : c->st.g);
         for (int q = 0; q < 19; ++q) {
-            if (p.precision == MFLBM_FP64) {
+            if (p.precision == MFLBM_FP64 && !c->st.list) {
                 char *dst = base + ((size_t)q * L.qs + L.xo) * c->elt;
                 CK(c, cudaMemcpy2DAsync(dst, (size_t)L.pitch * 8, src[q], (size_t)(p.nx + 2) * 8, (size_t)(p.nx + 2) * 8,
                                         (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyHostToDevice, c->stream));
@@ -463,7 +598,10 @@ int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *c
             }
         }
     }
-    if (p.multiphase) CK(c, cudaMemcpyAsync(c->st.phi, phi, sizeof(double) * n4(p), cudaMemcpyHostToDevice, c->stream));
+    if (p.multiphase) {
+        int r = field_put(c, c->st.phi, phi, n4(p));
+        if (r) return r;
+    }
     if (f_convec) CK(c, cudaMemcpyAsync(c->st.fconv, f_convec, sizeof(double) * nplane(p) * 19, cudaMemcpyHostToDevice, c->stream));
     if (p.multiphase && g_convec)
         CK(c, cudaMemcpyAsync(c->st.gconv, g_convec, sizeof(double) * nplane(p) * 19, cudaMemcpyHostToDevice, c->stream));
@@ -476,6 +614,7 @@ int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *c
 int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, double *phi, double *f_convec,
                              double *g_convec, double *phi_convec) {
     if (!c) return MFLBM_EINVAL;
+    if (!c->pdf) return fail(c, MFLBM_ESTATE, "the PDF storage is laid out by mflbm_set_geometry; call it first");
     const mflbm_params &p = c->p;
     CK(c, cudaSetDevice(c->dev));
     const Layout &L = c->st.L;
@@ -486,7 +625,7 @@ int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, d
         const char *base = (const char *)(s == 0 ? c->st.f : c->st.g);
         for (int q = 0; q < 19; ++q) {
             if (!dstv[q]) continue;
-            if (p.precision == MFLBM_FP64) {
+            if (p.precision == MFLBM_FP64 && !c->st.list) {
                 const char *src = base + ((size_t)q * L.qs + L.xo) * c->elt;
                 CK(c, cudaMemcpy2DAsync(dstv[q], (size_t)(p.nx + 2) * 8, src, (size_t)L.pitch * 8, (size_t)(p.nx + 2) * 8,
                                         (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyDeviceToHost, c->stream));
@@ -497,7 +636,10 @@ int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, d
             }
         }
     }
-    if (p.multiphase && phi) CK(c, cudaMemcpyAsync(phi, c->st.phi, sizeof(double) * n4(p), cudaMemcpyDeviceToHost, c->stream));
+    if (p.multiphase && phi) {
+        int r = field_get(c, phi, c->st.phi, n4(p));
+        if (r) return r;
+    }
     if (f_convec) CK(c, cudaMemcpyAsync(f_convec, c->st.fconv, sizeof(double) * nplane(p) * 19, cudaMemcpyDeviceToHost, c->stream));
     if (p.multiphase && g_convec)
         CK(c, cudaMemcpyAsync(g_convec, c->st.gconv, sizeof(double) * nplane(p) * 19, cudaMemcpyDeviceToHost, c->stream));
@@ -509,10 +651,14 @@ int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, d
 
 int32_t mflbm_init_equilibrium(mflbm_ctx *c, const double *phi) {
     if (!c) return MFLBM_EINVAL;
+    if (!c->pdf) return fail(c, MFLBM_ESTATE, "the PDF storage is laid out by mflbm_set_geometry; call it first");
     const mflbm_params &p = c->p;
     if (p.multiphase && !phi) return fail(c, MFLBM_EINVAL, "phi is required for multiphase");
     CK(c, cudaSetDevice(c->dev));
-    if (p.multiphase) CK(c, cudaMemcpyAsync(c->st.phi, phi, sizeof(double) * n4(p), cudaMemcpyHostToDevice, c->stream));
+    if (p.multiphase) {
+        int r = field_put(c, c->st.phi, phi, n4(p));
+        if (r) return r;
+    }
     c->kt->init_equilibrium(c->st, p.outlet_bc == 1, c->stream);
     CK(c, cudaPeekAtLastError());
     CK(c, cudaStreamSynchronize(c->stream));
@@ -626,12 +772,13 @@ int32_t mflbm_get_gradient(mflbm_ctx *c, double *cn_x, double *cn_y, double *cn_
     const mflbm_params &p = c->p;
     CK(c, cudaSetDevice(c->dev));
     CK(c, cudaStreamSynchronize(c->stream));
-    const size_t b2 = sizeof(double) * n2(p);
-    if (cn_x) CK(c, cudaMemcpy(cn_x, c->st.cnx, b2, cudaMemcpyDeviceToHost));
-    if (cn_y) CK(c, cudaMemcpy(cn_y, c->st.cny, b2, cudaMemcpyDeviceToHost));
-    if (cn_z) CK(c, cudaMemcpy(cn_z, c->st.cnz, b2, cudaMemcpyDeviceToHost));
-    if (c_norm) CK(c, cudaMemcpy(c_norm, c->st.cnorm, b2, cudaMemcpyDeviceToHost));
-    if (curv) CK(c, cudaMemcpy(curv, c->st.curv, sizeof(double) * n1(p), cudaMemcpyDeviceToHost));
+    double *const dst[5] = {cn_x, cn_y, cn_z, c_norm, curv};
+    const void *src[5] = {c->st.cnx, c->st.cny, c->st.cnz, c->st.cnorm, c->st.curv};
+    for (int a = 0; a < 5; ++a) {
+        if (!dst[a]) continue;
+        int r = field_get(c, dst[a], src[a], a < 4 ? n2(p) : n1(p));
+        if (r) return r;
+    }
     return MFLBM_OK;
 }
 
@@ -648,7 +795,10 @@ int32_t mflbm_macro(mflbm_ctx *c, double *u, double *v, double *w, double *rho, 
     if (v) CK(c, cudaMemcpy(v, c->st.v, b1, cudaMemcpyDeviceToHost));
     if (w) CK(c, cudaMemcpy(w, c->st.w, b1, cudaMemcpyDeviceToHost));
     if (rho) CK(c, cudaMemcpy(rho, c->st.rho, b1, cudaMemcpyDeviceToHost));
-    if (phi && p.multiphase) CK(c, cudaMemcpy(phi, c->st.phi, sizeof(double) * n4(p), cudaMemcpyDeviceToHost));
+    if (phi && p.multiphase) {
+        int r2 = field_get(c, phi, c->st.phi, n4(p));
+        if (r2) return r2;
+    }
     return MFLBM_OK;
 }
 

@@ -133,6 +133,63 @@ __host__ __device__ __forceinline__ MrtFold<R> fold_rates(double s_e, double s_e
     return c;
 }
 
+// The same fold evaluated in the arithmetic type R, for the per-node rates of the
+// multiphase collision (omega depends on phi).  Divisions by the constant norms are
+// multiplications by their reciprocals (default build only; a division costs about ten
+// FP64 instructions), and a caller passing literal rates gets them constant-folded.
+template <class R>
+__device__ __forceinline__ MrtFold<R> fold_rates_dev(R s_e, R s_e2, R s_q, R s_nu, R s_pi, R s_t) {
+    MrtFold<R> c;
+    const R n_e = R(1.0 / 2394.0), n_e2 = R(1.0 / 252.0), n_q = R(1.0 / 40.0), n_x3 = R(1.0 / 36.0);
+    const R n_xi = R(1.0 / 72.0), n_w = R(1.0 / 12.0), n_wi = R(1.0 / 24.0), n_o = R(0.25), n_t = R(0.125);
+    c.e_m = (R(1.0) - s_e) * n_e;
+    c.e_den = R(-11.0) * s_e * n_e;
+    c.e_u2 = R(19.0) * s_e * n_e;
+    c.e_f = (R(38.0) - R(19.0) * s_e) * n_e;
+    c.e2_m = (R(1.0) - s_e2) * n_e2;
+    c.e2_u2 = s_e2 * R(-475.0 / 63.0) * n_e2;
+    c.e2_f = (R(-11.0) + R(5.5) * s_e2) * n_e2;
+    c.q_m = (R(1.0) - s_q) * n_q;
+    c.q_u = s_q * R(-2.0 / 3.0) * n_q;
+    c.q_f = (R(-2.0 / 3.0) + s_q * R(1.0 / 3.0)) * n_q;
+    c.x3_m = (R(1.0) - s_nu) * n_x3;
+    c.x3_eq = s_nu * n_x3;
+    c.x3_f = (R(2.0) - s_nu) * n_x3;
+    c.xi_m = (R(1.0) - s_pi) * n_xi;
+    c.xi_f = (R(1.0) - R(0.5) * s_pi) * n_xi;
+    c.w_m = (R(1.0) - s_nu) * n_w;
+    c.w_eq = s_nu * n_w;
+    c.w_f = (R(2.0) - s_nu) * n_w;
+    c.wi_m = (R(1.0) - s_pi) * n_wi;
+    c.wi_f = (R(1.0) - R(0.5) * s_pi) * n_wi;
+    c.o_m = (R(1.0) - s_nu) * n_o;
+    c.o_eq = s_nu * n_o;
+    c.o_f = (R(1.0) - R(0.5) * s_nu) * n_o;
+    c.t_m = (R(1.0) - s_t) * n_t;
+    c.fz = R(0.0);
+    return c;
+}
+
+// Ensemble launch arguments (kernels.cuh, k_ens_step / k_ens_persistent)
+struct EnsTile { int32_t start; int32_t count; };
+
+struct EnsArgs {
+    void *A;
+    int64_t stride;
+    const int32_t *nb;
+    int64_t nf;              // fluid nodes of the whole arena (neighbour-table row length)
+    const EnsTile *tiles;
+    const int32_t *ntiles;   // device scalar
+    StepParams P;
+    MrtFold<double> fold;
+    MrtFold<float> fold32;
+    float scale;
+    int32_t ntime0;          // ntime of the first step of the launch
+    int32_t nsteps;          // steps per persistent launch
+    unsigned int *bar;       // [2] arrival count, generation
+    int32_t *err;            // set when a barrier wait gives up
+};
+
 // FP16 deviation storage: value = w_q * ref + half_value * scale, ref = the rest
 // density of the species.
 template <class S> struct StoreTraits;

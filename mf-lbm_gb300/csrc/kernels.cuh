@@ -42,22 +42,61 @@ __device__ __forceinline__ int64_t qoff(const Layout &L, int q) {
 }
 
 // ---------------------------------------------------------------------------------
-// PDF storage types.  FP64 and FP32 store the value; FP16 stores
-// (f_q - w_q * ref) * scale, i.e. a scaled deviation from the lattice weight.
+// PDF storage types.
+//   double  FP64 value (the plain drop-in)
+//   float   FP32 value (multiphase mixed form: a vanishing species makes deviations
+//           from a rest state no smaller than the values)
+//   dfloat  FP32 deviation d = f_q - w_q * ref from the MRT rest state (singlephase
+//           mixed form)
+//   __half  FP16 scaled deviation (f_q - w_q * ref) * scale (singlephase)
+// ld/st work on values (boundary conditions); ldd/std on deviations, which is how the
+// singlephase sweep of the deviation forms runs its collision: the rest state W is a
+// fixed point of the reference's MRT collision C, which is affine in f apart from
+// terms in the momentum j (W carries none) and the force, so C(W + d) - W is the same
+// code applied to d with density sum(d).  Arithmetic on d keeps FP32's 24 bits for the
+// ~1e-6 signal of a creeping flow instead of spending them on the ~0.1 of f.
+// ld64/st64 convert to and from FP64 without passing through an FP32 value.
 // ---------------------------------------------------------------------------------
+struct dfloat { float x; };
+
 template <class S> struct Store;
 template <> struct Store<double> {
     using R = double;
+    static constexpr bool kDev = false;
     __device__ __forceinline__ static R ld(const double *p, int64_t o, R, R) { return p[o]; }
     __device__ __forceinline__ static void st(double *p, int64_t o, R v, R, R) { p[o] = v; }
+    __device__ __forceinline__ static R ldd(const double *p, int64_t o, R) { return p[o]; }
+    __device__ __forceinline__ static void std_(double *p, int64_t o, R v, R) { p[o] = v; }
+    __device__ __forceinline__ static double ld64(const double *p, int64_t o, double, float) { return p[o]; }
+    __device__ __forceinline__ static void st64(double *p, int64_t o, double v, double, float) { p[o] = v; }
 };
 template <> struct Store<float> {
     using R = float;
+    static constexpr bool kDev = false;
     __device__ __forceinline__ static R ld(const float *p, int64_t o, R, R) { return p[o]; }
     __device__ __forceinline__ static void st(float *p, int64_t o, R v, R, R) { p[o] = v; }
+    __device__ __forceinline__ static R ldd(const float *p, int64_t o, R) { return p[o]; }
+    __device__ __forceinline__ static void std_(float *p, int64_t o, R v, R) { p[o] = v; }
+    __device__ __forceinline__ static double ld64(const float *p, int64_t o, double, float) { return (double)p[o]; }
+    __device__ __forceinline__ static void st64(float *p, int64_t o, double v, double, float) { p[o] = (float)v; }
+};
+template <> struct Store<dfloat> {
+    using R = float;
+    static constexpr bool kDev = true;
+    __device__ __forceinline__ static R ld(const dfloat *p, int64_t o, R w_ref, R) { return w_ref + p[o].x; }
+    __device__ __forceinline__ static void st(dfloat *p, int64_t o, R v, R w_ref, R) { p[o].x = v - w_ref; }
+    __device__ __forceinline__ static R ldd(const dfloat *p, int64_t o, R) { return p[o].x; }
+    __device__ __forceinline__ static void std_(dfloat *p, int64_t o, R d, R) { p[o].x = d; }
+    __device__ __forceinline__ static double ld64(const dfloat *p, int64_t o, double w_ref, float) {
+        return w_ref + (double)p[o].x;
+    }
+    __device__ __forceinline__ static void st64(dfloat *p, int64_t o, double v, double w_ref, float) {
+        p[o].x = (float)(v - w_ref);
+    }
 };
 template <> struct Store<__half> {
     using R = float;
+    static constexpr bool kDev = true;
     // w_ref = w_q * ref density; sc = scale (store) / 1/scale (load)
     __device__ __forceinline__ static R ld(const __half *p, int64_t o, R w_ref, R inv_scale) {
         return w_ref + __half2float(p[o]) * inv_scale;
@@ -65,7 +104,29 @@ template <> struct Store<__half> {
     __device__ __forceinline__ static void st(__half *p, int64_t o, R v, R w_ref, R scale) {
         p[o] = __float2half_rn((v - w_ref) * scale);
     }
+    __device__ __forceinline__ static R ldd(const __half *p, int64_t o, R inv_scale) { return __half2float(p[o]) * inv_scale; }
+    __device__ __forceinline__ static void std_(__half *p, int64_t o, R d, R scale) { p[o] = __float2half_rn(d * scale); }
+    __device__ __forceinline__ static double ld64(const __half *p, int64_t o, double w_ref, float inv_scale) {
+        return w_ref + (double)__half2float(p[o]) * (double)inv_scale;
+    }
+    __device__ __forceinline__ static void st64(__half *p, int64_t o, double v, double w_ref, float scale) {
+        p[o] = __float2half_rn((float)((v - w_ref) * (double)scale));
+    }
 };
+
+// load/store of the collision sweep: deviations for the deviation forms, values else
+template <class S>
+__device__ __forceinline__ typename Store<S>::R ld_sweep(const S *p, int64_t o, int q, typename Store<S>::R inv) {
+    using R = typename Store<S>::R;
+    if constexpr (Store<S>::kDev) return Store<S>::ldd(p, o, inv);
+    else return Store<S>::ld(p, o, R(WREST(q)), inv);
+}
+template <class S>
+__device__ __forceinline__ void st_sweep(S *p, int64_t o, int q, typename Store<S>::R v, typename Store<S>::R sc) {
+    using R = typename Store<S>::R;
+    if constexpr (Store<S>::kDev) Store<S>::std_(p, o, v, sc);
+    else Store<S>::st(p, o, v, R(WREST(q)), sc);
+}
 
 // ---------------------------------------------------------------------------------
 // MRT collision, the "MRT kernel, repeated part" of the reference
@@ -332,9 +393,9 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
         if (ODD)
-            ft[q] = St::ld(f, (int64_t)q * L.qs + c - qoff(L, q), R(WREST(q)), inv_scale);
+            ft[q] = ld_sweep<S>(f, (int64_t)q * L.qs + c - qoff(L, q), q, inv_scale);
         else
-            ft[q] = St::ld(f, (int64_t)OPP(q) * L.qs + c, R(WREST(q)), inv_scale);
+            ft[q] = ld_sweep<S>(f, (int64_t)OPP(q) * L.qs + c, q, inv_scale);
     }
 #ifdef MFLBM_STRICT
     const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
@@ -346,12 +407,12 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
 #endif
     const R sc = R(scale);
     if (ODD) {
-        St::st(f, c, ft[0], R(WREST(0)), sc);
+        st_sweep<S>(f, c, 0, ft[0], sc);
 #pragma unroll
-        for (int q = 1; q < 19; ++q) St::st(f, (int64_t)OPP(q) * L.qs + c + qoff(L, q), ft[q], R(WREST(q)), sc);
+        for (int q = 1; q < 19; ++q) st_sweep<S>(f, (int64_t)OPP(q) * L.qs + c + qoff(L, q), q, ft[q], sc);
     } else {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) St::st(f, (int64_t)q * L.qs + c, ft[q], R(WREST(q)), sc);
+        for (int q = 0; q < 19; ++q) st_sweep<S>(f, (int64_t)q * L.qs + c, q, ft[q], sc);
     }
 }
 
@@ -361,11 +422,13 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
 // CSF force, viscosity interpolation in 1/nu, R-K recolouring into f (fluid 1) and
 // g (fluid 2), phi written for the gradient pass.
 // ---------------------------------------------------------------------------------
-template <bool ODD>
-__global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double *__restrict__ g, double *__restrict__ phi,
-                                                 const double *__restrict__ cnx, const double *__restrict__ cny,
-                                                 const double *__restrict__ cnz, const double *__restrict__ cnorm,
-                                                 const double *__restrict__ curv, const int32_t *__restrict__ cells,
+// T = double: the FP64 drop-in; T = float: the mixed form (FP32 storage of f, g, phi
+// and the gradient fields, FP32 arithmetic).
+template <class T, bool ODD>
+__global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
+                                                 const T *__restrict__ cnx, const T *__restrict__ cny,
+                                                 const T *__restrict__ cnz, const T *__restrict__ cnorm,
+                                                 const T *__restrict__ curv, const int32_t *__restrict__ cells,
                                                  const int ncell, const Layout L, const StepParams P, const double rk_weight2) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) return;
@@ -376,75 +439,89 @@ __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double 
     const int j = (int)(r / L.pitch);
     const int i = (int)(r - (int64_t)j * L.pitch) - L.xo;
     const int64_t w2 = L.i2(i, j, k);
-    double ft[19];
-    double rho1 = 0.0, rho2 = 0.0;
+    T ft[19];
+    T rho1 = T(0.0), rho2 = T(0.0);
     // pull (odd) or local swapped read (even); rho1/rho2 accumulate in the written order
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const double a = ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c];
+        const T a = ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c];
         ft[q] = a;
         rho1 = q == 0 ? a : rho1 + a;
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const double b = ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c];
+        const T b = ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c];
         ft[q] = ft[q] + b;
         rho2 = q == 0 ? b : rho2 + b;
     }
 #ifdef MFLBM_STRICT
-    const double ph = (rho1 - rho2) / (rho1 + rho2);
+    const T ph = (rho1 - rho2) / (rho1 + rho2);
 #else
-    const double inv_den = 1.0 / (rho1 + rho2);   // one division serves phi and the recolouring
-    const double ph = (rho1 - rho2) * inv_den;
+    const T inv_den = T(1.0) / (rho1 + rho2);   // one division serves phi and the recolouring
+    const T ph = (rho1 - rho2) * inv_den;
 #endif
     phi[L.i4(i, j, k)] = ph;
-    const double cx = cnx[w2], cy = cny[w2], cz = cnz[w2];
-    double tmp = 0.5 * P.gamma * curv[L.i1(i, j, k)] * cnorm[w2];
-    const double fx = tmp * cx;
-    const double fy = tmp * cy;
-    const double fz = tmp * cz + P.force_z;
+    const T cx = cnx[w2], cy = cny[w2], cz = cnz[w2];
+    T tmp = T(0.5) * T(P.gamma) * curv[L.i1(i, j, k)] * cnorm[w2];
+    const T fx = tmp * cx;
+    const T fy = tmp * cy;
+    const T fz = tmp * cz + T(P.force_z);
+    const T nui1 = T(P.la_nui1), nui2 = T(P.la_nui2);
 #ifdef MFLBM_STRICT
-    const double omega = 1.0 / (6.0 / ((1.0 + ph) * P.la_nui1 + (1.0 - ph) * P.la_nui2) + 0.5);
+    const T omega = T(1.0) / (T(6.0) / ((T(1.0) + ph) * nui1 + (T(1.0) - ph) * nui2) + T(0.5));
 #else
     // 1/(6/X + 1/2) = X / (6 + X/2): one division
-    const double visc = (1.0 + ph) * P.la_nui1 + (1.0 - ph) * P.la_nui2;
-    const double omega = visc / (6.0 + 0.5 * visc);
+    const T visc = (T(1.0) + ph) * nui1 + (T(1.0) - ph) * nui2;
+    const T omega = visc / (T(6.0) + T(0.5) * visc);
 #endif
-    double s_e, s_e2, s_pi, s_q, s_t;
+    const T den = rho1 + rho2;
+#ifdef MFLBM_STRICT
+    T s_e, s_e2, s_pi, s_q, s_t;
     if (P.mrt == 1) {
         s_e = omega; s_e2 = omega; s_pi = omega;
-        s_q = 8.0 * (2.0 - omega) / (8.0 - omega);
+        s_q = T(8.0) * (T(2.0) - omega) / (T(8.0) - omega);
         s_t = s_q;
     } else if (P.mrt == 3) {
         s_e = omega; s_e2 = omega; s_pi = omega; s_q = omega; s_t = omega;
     } else if (P.mrt == 4) {
         s_e = omega; s_e2 = omega; s_pi = omega;
-        s_q = (6.0 - 3.0 * omega) / (3.0 - omega);
+        s_q = (T(6.0) - T(3.0) * omega) / (T(3.0) - omega);
         s_t = omega;
     } else {
-        s_e = 1.19; s_e2 = 1.4; s_pi = 1.4; s_q = 1.2; s_t = 1.98;
+        s_e = T(1.19); s_e2 = T(1.4); s_pi = T(1.4); s_q = T(1.2); s_t = T(1.98);
     }
-    const double den = rho1 + rho2;
-#ifdef MFLBM_STRICT
-    mrt_collide<double>(ft, den, fx, fy, fz, s_e, s_e2, s_q, omega, s_pi, s_t);
+    mrt_collide<T>(ft, den, fx, fy, fz, s_e, s_e2, s_q, omega, s_pi, s_t);
 #else
-    const MrtFold<double> cf = fold_rates<double>(s_e, s_e2, s_q, omega, s_pi, s_t);
-    mrt_collide_pairs<double, true, false>(ft, den, fx, fy, fz, cf);
+    // rates of Kernel_multiphase.F90:124-155; each branch folds its literal rates
+    MrtFold<T> cf;
+    if (P.mrt == 1) {
+        const T sq = T(8.0) * (T(2.0) - omega) / (T(8.0) - omega);
+        cf = fold_rates_dev<T>(omega, omega, sq, omega, omega, sq);
+    } else if (P.mrt == 3) {
+        cf = fold_rates_dev<T>(omega, omega, omega, omega, omega, omega);
+    } else if (P.mrt == 4) {
+        const T sq = (T(6.0) - T(3.0) * omega) / (T(3.0) - omega);
+        cf = fold_rates_dev<T>(omega, omega, sq, omega, omega, omega);
+    } else {
+        cf = fold_rates_dev<T>(T(1.19), T(1.4), T(1.2), omega, T(1.4), T(1.98));
+    }
+    mrt_collide_pairs<T, true, false>(ft, den, fx, fy, fz, cf);
 #endif
     // recolouring (Kernel_multiphase.F90:272-315)
 #ifdef MFLBM_STRICT
-    const double tmp1 = rho1 / den;
-    tmp = rho1 * rho2 * P.beta / den;
+    const T tmp1 = rho1 / den;
+    tmp = rho1 * rho2 * T(P.beta) / den;
 #else
-    const double tmp1 = rho1 * inv_den;
-    tmp = rho1 * rho2 * P.beta * inv_den;
+    const T tmp1 = rho1 * inv_den;
+    tmp = rho1 * rho2 * T(P.beta) * inv_den;
 #endif
     f[c] = tmp1 * ft[0];
-    g[c] = ft[0] * (1.0 - tmp1);
+    g[c] = ft[0] * (T(1.0) - tmp1);
+    const T rkw2 = T(rk_weight2);
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
-        const double ex = (double)EX(q), ey = (double)EY(q), ez = (double)EZ(q);
-        double proj;
+        const T ex = (T)EX(q), ey = (T)EY(q), ez = (T)EZ(q);
+        T proj;
         // the reference writes each projection as a signed sum of the two non-zero
         // components in x, y, z order, e.g. (-cnx + cny)
         if (q <= 6)
@@ -455,9 +532,9 @@ __global__ void __launch_bounds__(128) k_mp_step(double *__restrict__ f, double 
             proj = ex * cx + ez * cz;
         else
             proj = ey * cy + ez * cz;
-        const double wq = q <= 6 ? w_equ_1 : rk_weight2;
-        const double a = tmp1 * ft[q] + wq * tmp * (proj);
-        const double b = ft[q] - a;
+        const T wq = q <= 6 ? T(w_equ_1) : rkw2;
+        const T a = tmp1 * ft[q] + wq * tmp * (proj);
+        const T b = ft[q] - a;
         const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
         f[o] = a;
         g[o] = b;
@@ -567,7 +644,8 @@ __global__ void k_wrap_edges(S *__restrict__ f, int nspecies, const Layout L, in
 
 // phi halo, 4 layers (MPI_phi_async_pack / MPI_phi_sync_update, Mpi.F90:608-867):
 // z faces (i,j interior), y faces (i,k interior), x-edges; sources are all interior.
-__global__ void k_wrap_phi(double *__restrict__ phi, const Layout L, int py, int pz) {
+template <class T>
+__global__ void k_wrap_phi(T *__restrict__ phi, const Layout L, int py, int pz) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = L.nx, ny = L.ny, nz = L.nz;
     const int64_t nzf = pz ? (int64_t)4 * nx * ny : 0;
@@ -610,7 +688,7 @@ template <class R> __device__ __forceinline__ R sel(R x, R y, int w) { return x 
 
 // velocity inlet (Boundary_multiphase_inlet.F90:6-102; singlephase Boundary.F90:5-73)
 template <class S>
-__global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+__global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
                                  const int8_t *__restrict__ walls, const double *__restrict__ w_in, const Layout L,
                                  const StepParams P, int before_odd, int multiphase, float ref, float scale) {
     using St = Store<S>;
@@ -660,7 +738,7 @@ __global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, double *_
 
 // Zou-He pressure inlet (Boundary_multiphase_inlet.F90:115-294; Boundary.F90:80-187)
 template <class S>
-__global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+__global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
                               const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
                               int multiphase, float ref, float scale) {
     using St = Store<S>;
@@ -727,7 +805,7 @@ __global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__re
 
 // convective outlet (Boundary_multiphase_outlet.F90:7-127; Boundary.F90:196-276)
 template <class S>
-__global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+__global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
                                     double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
                                     const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
                                     int multiphase, float ref, float scale) {
@@ -786,7 +864,7 @@ __global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, double
 
 // Zou-He pressure outlet (Boundary_multiphase_outlet.F90:139-311; Boundary.F90:284-389)
 template <class S>
-__global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__restrict__ phi,
+__global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
                                const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
                                int multiphase, float ref, float scale) {
     using St = Store<S>;
@@ -865,13 +943,14 @@ __global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, double *__r
 
 // porous plate (Boundary_multiphase_other.F90:8-184); blocked = the species that is
 // reflected, passing = the species copied across.
-__global__ void k_porous_plate(double *__restrict__ blocked, double *__restrict__ passing, const Layout L, int z,
+template <class T>
+__global__ void k_porous_plate(T *__restrict__ blocked, T *__restrict__ passing, const Layout L, int z,
                                int before_odd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1;
     if (i > L.nx) return;
-    auto b = [&](int q, int ii, int jj, int kk) -> double & { return blocked[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
-    auto c = [&](int q, int ii, int jj, int kk) -> double & { return passing[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
+    auto b = [&](int q, int ii, int jj, int kk) -> T & { return blocked[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
+    auto c = [&](int q, int ii, int jj, int kk) -> T & { return passing[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
     if (before_odd) {
         b(6, i, j, z) = b(5, i, j, z - 1);
         b(13, i - 1, j, z) = b(12, i, j, z - 1);
@@ -921,51 +1000,54 @@ __global__ void k_porous_plate(double *__restrict__ blocked, double *__restrict_
 // color_gradient (Phase_gradient.F90:5-265)
 // ---------------------------------------------------------------------------------
 // phi extrapolation to the solid-boundary list (:13-30)
-__global__ void k_extrap_phi(double *__restrict__ phi, const SolidBnd *__restrict__ sb, int ns, const Layout L) {
+template <class T>
+__global__ void k_extrap_phi(T *__restrict__ phi, const SolidBnd *__restrict__ sb, int ns, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
     const SolidBnd s = sb[t];
-    double acc = 0.0;
+    T acc = T(0.0);
     for (int n = 0; n < s.i_fluid_num; ++n) {
         const int ie = s.nbr[n];
         int dx = 0, dy = 0, dz = 0;
-        double w = 0.0;
+        T w = T(0.0);
 #pragma unroll
         for (int q = 1; q < 19; ++q)
-            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = WEQ(q); }
+            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = T(WEQ(q)); }
         acc = acc + phi[L.i4(s.ix + dx, s.iy + dy, s.iz + dz)] * w;
     }
-    phi[L.i4(s.ix, s.iy, s.iz)] = acc / s.la_weight;
+    phi[L.i4(s.ix, s.iy, s.iz)] = acc / T(s.la_weight);
 }
 
 // ISO4 gradient and unit normal over [1-2, n+2]^3 (:33-79)
-__global__ void __launch_bounds__(256) k_normals(const double *__restrict__ phi, const int8_t *__restrict__ walls,
-                                                 double *__restrict__ cnx, double *__restrict__ cny,
-                                                 double *__restrict__ cnz, double *__restrict__ cnorm, const Layout L) {
+template <class T>
+__global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                 T *__restrict__ cnx, T *__restrict__ cny,
+                                                 T *__restrict__ cnz, T *__restrict__ cnorm, const Layout L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
     if (i > L.nx + 2 || j > L.ny + 2) return;
     const int64_t id = L.i2(i, j, k);
     if (walls[id] == 1) {  // the reference zeroes normals at wall nodes (Phase_gradient.F90:65-69)
-        cnx[id] = 0.0; cny[id] = 0.0; cnz[id] = 0.0; cnorm[id] = 0.0;
+        cnx[id] = T(0.0); cny[id] = T(0.0); cnz[id] = T(0.0); cnorm[id] = T(0.0);
         return;
     }
     auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
-    double gx = ISO4_1 * (P(1, 0, 0) - P(-1, 0, 0)) +
-                ISO4_2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
-    double gy = ISO4_1 * (P(0, 1, 0) - P(0, -1, 0)) +
-                ISO4_2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
-    double gz = ISO4_1 * (P(0, 0, 1) - P(0, 0, -1)) +
-                ISO4_2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
-    double cn = sqrt(gx * gx + gy * gy + gz * gz);
-    if (cn < 1e-6) {
-        gx = 0.0; gy = 0.0; gz = 0.0; cn = 0.0;
+    const T c1 = T(ISO4_1), c2 = T(ISO4_2);
+    T gx = c1 * (P(1, 0, 0) - P(-1, 0, 0)) +
+           c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
+    T gy = c1 * (P(0, 1, 0) - P(0, -1, 0)) +
+           c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
+    T gz = c1 * (P(0, 0, 1) - P(0, 0, -1)) +
+           c2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
+    T cn = sqrt(gx * gx + gy * gy + gz * gz);
+    if (cn < T(1e-6)) {
+        gx = T(0.0); gy = T(0.0); gz = T(0.0); cn = T(0.0);
     } else {
 #ifdef MFLBM_STRICT
         gx = gx / cn; gy = gy / cn; gz = gz / cn;
 #else
-        const double inv = 1.0 / cn;
+        const T inv = T(1.0) / cn;
         gx = gx * inv; gy = gy * inv; gz = gz * inv;
 #endif
     }
@@ -973,27 +1055,29 @@ __global__ void __launch_bounds__(256) k_normals(const double *__restrict__ phi,
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
-__global__ void k_wetting(double *__restrict__ cnx, double *__restrict__ cny, double *__restrict__ cnz,
-                          const double *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L) {
+template <class T>
+__global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+                          const T *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
     const FluidBnd b = fb[t];
     const int64_t id = L.i2(b.ix, b.iy, b.iz);
-    if (cnorm[id] > 1e-6) {
-        const double cnx0 = cnx[id], cny0 = cny[id], cnz0 = cnz[id];
-        const double tmpCos = b.cos_t;
-        const double tmp1 = b.nwx * cnx0 + b.nwy * cny0 + b.nwz * cnz0;
-        const double tmp2 = 1.0 / sqrt(1.0 - tmp1 * tmp1);
-        const double coe1 = b.sin_t * tmp1 * tmp2;
-        const double coe2 = b.sin_t * tmp2;
-        const double cnxp = (tmpCos - coe1) * b.nwx + coe2 * cnx0;
-        const double cnyp = (tmpCos - coe1) * b.nwy + coe2 * cny0;
-        const double cnzp = (tmpCos - coe1) * b.nwz + coe2 * cnz0;
-        const double cnxm = (tmpCos + coe1) * b.nwx - coe2 * cnx0;
-        const double cnym = (tmpCos + coe1) * b.nwy - coe2 * cny0;
-        const double cnzm = (tmpCos + coe1) * b.nwz - coe2 * cnz0;
-        const double distP = (cnxp - cnx0) * (cnxp - cnx0) + (cnyp - cny0) * (cnyp - cny0) + (cnzp - cnz0) * (cnzp - cnz0);
-        const double distM = (cnxm - cnx0) * (cnxm - cnx0) + (cnym - cny0) * (cnym - cny0) + (cnzm - cnz0) * (cnzm - cnz0);
+    if (cnorm[id] > T(1e-6)) {
+        const T cnx0 = cnx[id], cny0 = cny[id], cnz0 = cnz[id];
+        const T nwx = T(b.nwx), nwy = T(b.nwy), nwz = T(b.nwz), sin_t = T(b.sin_t);
+        const T tmpCos = T(b.cos_t);
+        const T tmp1 = nwx * cnx0 + nwy * cny0 + nwz * cnz0;
+        const T tmp2 = T(1.0) / sqrt(T(1.0) - tmp1 * tmp1);
+        const T coe1 = sin_t * tmp1 * tmp2;
+        const T coe2 = sin_t * tmp2;
+        const T cnxp = (tmpCos - coe1) * nwx + coe2 * cnx0;
+        const T cnyp = (tmpCos - coe1) * nwy + coe2 * cny0;
+        const T cnzp = (tmpCos - coe1) * nwz + coe2 * cnz0;
+        const T cnxm = (tmpCos + coe1) * nwx - coe2 * cnx0;
+        const T cnym = (tmpCos + coe1) * nwy - coe2 * cny0;
+        const T cnzm = (tmpCos + coe1) * nwz - coe2 * cnz0;
+        const T distP = (cnxp - cnx0) * (cnxp - cnx0) + (cnyp - cny0) * (cnyp - cny0) + (cnzp - cnz0) * (cnzp - cnz0);
+        const T distM = (cnxm - cnx0) * (cnxm - cnx0) + (cnym - cny0) * (cnym - cny0) + (cnzm - cnz0) * (cnzm - cnz0);
         if (distP <= distM) {
             cnx[id] = cnxp; cny[id] = cnyp; cnz[id] = cnzp;
         } else {
@@ -1003,34 +1087,37 @@ __global__ void k_wetting(double *__restrict__ cnx, double *__restrict__ cny, do
 }
 
 // normal extrapolation to solid-boundary nodes inside [0, n+1]^3 (:85-110)
-__global__ void k_extrap_normals(double *__restrict__ cnx, double *__restrict__ cny, double *__restrict__ cnz,
+template <class T>
+__global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
                                  const SolidBnd *__restrict__ sb, int ns, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
     const SolidBnd s = sb[t];
     if (!(s.ix >= 0 && s.ix <= L.nx + 1 && s.iy >= 0 && s.iy <= L.ny + 1 && s.iz >= 0 && s.iz <= L.nz + 1)) return;
-    double ax = 0.0, ay = 0.0, az = 0.0;
+    T ax = T(0.0), ay = T(0.0), az = T(0.0);
     for (int n = 0; n < s.i_fluid_num; ++n) {
         const int ie = s.nbr[n];
         int dx = 0, dy = 0, dz = 0;
-        double w = 0.0;
+        T w = T(0.0);
 #pragma unroll
         for (int q = 1; q < 19; ++q)
-            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = WEQ(q); }
+            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = T(WEQ(q)); }
         const int64_t nb = L.i2(s.ix + dx, s.iy + dy, s.iz + dz);
         ax = ax + cnx[nb] * w;
         ay = ay + cny[nb] * w;
         az = az + cnz[nb] * w;
     }
     const int64_t id = L.i2(s.ix, s.iy, s.iz);
-    cnx[id] = ax / s.la_weight;
-    cny[id] = ay / s.la_weight;
-    cnz[id] = az / s.la_weight;
+    const T lw = T(s.la_weight);
+    cnx[id] = ax / lw;
+    cny[id] = ay / lw;
+    cnz[id] = az / lw;
 }
 
 // curvature over [1, n]^3 (:113-201)
-__global__ void __launch_bounds__(256) k_curvature(const double *__restrict__ cnx, const double *__restrict__ cny,
-                                                   const double *__restrict__ cnz, double *__restrict__ curv,
+template <class T>
+__global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                                   const T *__restrict__ cnz, T *__restrict__ curv,
                                                    const int8_t *__restrict__ walls, const Layout L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -1040,33 +1127,34 @@ __global__ void __launch_bounds__(256) k_curvature(const double *__restrict__ cn
     // curv is read only at fluid nodes (collision, compute_macro_vars masks walls); the
     // default build leaves 0 at wall nodes instead of the reference's unused value
     if (walls[L.i2(i, j, k)] != 0) {
-        curv[L.i1(i, j, k)] = 0.0;
+        curv[L.i1(i, j, k)] = T(0.0);
         return;
     }
 #endif
+    const T c1 = T(ISO4_1), c2 = T(ISO4_2);
     auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
     auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
     auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };
-    const double kxx = ISO4_1 * (X(1, 0, 0) - X(-1, 0, 0)) +
-                       ISO4_2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
-    const double kyy = ISO4_1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
-                       ISO4_2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(-1, 1, 0) - Y(1, -1, 0) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, 1, -1) - Y(0, -1, 1));
-    const double kzz = ISO4_1 * (Z(0, 0, 1) - Z(0, 0, -1)) +
-                       ISO4_2 * (Z(1, 0, 1) - Z(-1, 0, -1) + Z(-1, 0, 1) - Z(1, 0, -1) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, -1, 1) - Z(0, 1, -1));
-    const double kxy = ISO4_1 * (X(0, 1, 0) - X(0, -1, 0)) +
-                       ISO4_2 * (X(1, 1, 0) - X(-1, -1, 0) + X(-1, 1, 0) - X(1, -1, 0) + X(0, 1, 1) - X(0, -1, -1) + X(0, 1, -1) - X(0, -1, 1));
-    const double kxz = ISO4_1 * (X(0, 0, 1) - X(0, 0, -1)) +
-                       ISO4_2 * (X(1, 0, 1) - X(-1, 0, -1) + X(-1, 0, 1) - X(1, 0, -1) + X(0, 1, 1) - X(0, -1, -1) + X(0, -1, 1) - X(0, 1, -1));
-    const double kyx = ISO4_1 * (Y(1, 0, 0) - Y(-1, 0, 0)) +
-                       ISO4_2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(1, -1, 0) - Y(-1, 1, 0) + Y(1, 0, 1) - Y(-1, 0, -1) + Y(1, 0, -1) - Y(-1, 0, 1));
-    const double kyz = ISO4_1 * (Y(0, 0, 1) - Y(0, 0, -1)) +
-                       ISO4_2 * (Y(1, 0, 1) - Y(-1, 0, -1) + Y(-1, 0, 1) - Y(1, 0, -1) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, -1, 1) - Y(0, 1, -1));
-    const double kzx = ISO4_1 * (Z(1, 0, 0) - Z(-1, 0, 0)) +
-                       ISO4_2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(1, -1, 0) - Z(-1, 1, 0) + Z(1, 0, 1) - Z(-1, 0, -1) + Z(1, 0, -1) - Z(-1, 0, 1));
-    const double kzy = ISO4_1 * (Z(0, 1, 0) - Z(0, -1, 0)) +
-                       ISO4_2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(-1, 1, 0) - Z(1, -1, 0) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, 1, -1) - Z(0, -1, 1));
-    const double cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
-    curv[L.i1(i, j, k)] = (cx * cx - 1.0) * kxx + (cy * cy - 1.0) * kyy + (cz * cz - 1.0) * kzz + cx * cy * (kxy + kyx) +
+    const T kxx = c1 * (X(1, 0, 0) - X(-1, 0, 0)) +
+                       c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
+    const T kyy = c1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
+                       c2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(-1, 1, 0) - Y(1, -1, 0) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, 1, -1) - Y(0, -1, 1));
+    const T kzz = c1 * (Z(0, 0, 1) - Z(0, 0, -1)) +
+                       c2 * (Z(1, 0, 1) - Z(-1, 0, -1) + Z(-1, 0, 1) - Z(1, 0, -1) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, -1, 1) - Z(0, 1, -1));
+    const T kxy = c1 * (X(0, 1, 0) - X(0, -1, 0)) +
+                       c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(-1, 1, 0) - X(1, -1, 0) + X(0, 1, 1) - X(0, -1, -1) + X(0, 1, -1) - X(0, -1, 1));
+    const T kxz = c1 * (X(0, 0, 1) - X(0, 0, -1)) +
+                       c2 * (X(1, 0, 1) - X(-1, 0, -1) + X(-1, 0, 1) - X(1, 0, -1) + X(0, 1, 1) - X(0, -1, -1) + X(0, -1, 1) - X(0, 1, -1));
+    const T kyx = c1 * (Y(1, 0, 0) - Y(-1, 0, 0)) +
+                       c2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(1, -1, 0) - Y(-1, 1, 0) + Y(1, 0, 1) - Y(-1, 0, -1) + Y(1, 0, -1) - Y(-1, 0, 1));
+    const T kyz = c1 * (Y(0, 0, 1) - Y(0, 0, -1)) +
+                       c2 * (Y(1, 0, 1) - Y(-1, 0, -1) + Y(-1, 0, 1) - Y(1, 0, -1) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, -1, 1) - Y(0, 1, -1));
+    const T kzx = c1 * (Z(1, 0, 0) - Z(-1, 0, 0)) +
+                       c2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(1, -1, 0) - Z(-1, 1, 0) + Z(1, 0, 1) - Z(-1, 0, -1) + Z(1, 0, -1) - Z(-1, 0, 1));
+    const T kzy = c1 * (Z(0, 1, 0) - Z(0, -1, 0)) +
+                       c2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(-1, 1, 0) - Z(1, -1, 0) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, 1, -1) - Z(0, -1, 1));
+    const T cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
+    curv[L.i1(i, j, k)] = (cx * cx - T(1.0)) * kxx + (cy * cy - T(1.0)) * kyy + (cz * cz - T(1.0)) * kzz + cx * cy * (kxy + kyx) +
                           cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz);
 }
 
@@ -1082,10 +1170,10 @@ constexpr int MON_NQ = 10;  // fl1 fl2 vol1 vol2 mass1 mass2 pre | umax usq1 usq
 
 template <class S>
 __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f, const S *__restrict__ g,
-                                                         double *__restrict__ phi, const int8_t *__restrict__ walls,
-                                                         const double *__restrict__ cnx, const double *__restrict__ cny,
-                                                         const double *__restrict__ cnz, const double *__restrict__ cnorm,
-                                                         const double *__restrict__ curv, double *__restrict__ u,
+                                                         typename Store<S>::R *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                         const typename Store<S>::R *__restrict__ cnx, const typename Store<S>::R *__restrict__ cny,
+                                                         const typename Store<S>::R *__restrict__ cnz, const typename Store<S>::R *__restrict__ cnorm,
+                                                         const typename Store<S>::R *__restrict__ curv, double *__restrict__ u,
                                                          double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho,
                                                          double *__restrict__ out, const Layout L, const StepParams P,
                                                          int multiphase, int write_fields, float ref, float scale) {
@@ -1104,8 +1192,8 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
         double ft[19];
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            double a = (double)St::ld(f, (int64_t)q * L.qs + c, R(WREST(q) * ref), inv);
-            if (multiphase) a = a + (double)St::ld(g, (int64_t)q * L.qs + c, R(WREST(q) * ref), inv);
+            double a = St::ld64(f, (int64_t)q * L.qs + c, WREST(q) * ref, inv);
+            if (multiphase) a = a + St::ld64(g, (int64_t)q * L.qs + c, WREST(q) * ref, inv);
             ft[q] = a;
         }
         const double m = (double)(1 - wi);
@@ -1115,10 +1203,10 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
         const int64_t i1 = L.i1(i, j, k);
         if (multiphase) {
             const int64_t i2 = L.i2(i, j, k);
-            const double tmp = 0.5 * P.gamma * curv[i1] * cnorm[i2];
-            fx = tmp * cnx[i2];
-            fy = tmp * cny[i2];
-            fz = tmp * cnz[i2] + P.force_z;
+            const double tmp = 0.5 * P.gamma * (double)curv[i1] * (double)cnorm[i2];
+            fx = tmp * (double)cnx[i2];
+            fy = tmp * (double)cny[i2];
+            fz = tmp * (double)cnz[i2] + P.force_z;
         }
         const double uu = (ft[1] - ft[2] + ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14] - 0.5 * fx) * m;
         const double vv = (ft[3] - ft[4] + ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18] - 0.5 * fy) * m;
@@ -1128,8 +1216,8 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
         acc[7] = (acc[7] < temp) ? temp : acc[7];
         if (multiphase) {
             const int64_t i4 = L.i4(i, j, k);
-            const double ph = 0.0 * (double)wi + phi[i4] * m;
-            phi[i4] = ph;
+            const double ph = 0.0 * (double)wi + (double)phi[i4] * m;
+            phi[i4] = (R)ph;
             if (ph > 0.999) acc[8] += temp;
             else if (ph < -0.999) acc[9] += temp;
             acc[2] += 0.5 * (1.0 + ph) * m;
@@ -1166,7 +1254,8 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
 }
 
 // cal_saturation partial sums per slice (Monitor.F90:512-550)
-__global__ void __launch_bounds__(MON_THREADS) k_saturation(const double *__restrict__ phi, const int8_t *__restrict__ walls,
+template <class T>
+__global__ void __launch_bounds__(MON_THREADS) k_saturation(const T *__restrict__ phi, const int8_t *__restrict__ walls,
                                                             double *__restrict__ out, const Layout L) {
     const int k = blockIdx.x + 1;
     const int64_t n = (int64_t)L.nx * L.ny;
@@ -1174,7 +1263,7 @@ __global__ void __launch_bounds__(MON_THREADS) k_saturation(const double *__rest
     for (int64_t t = threadIdx.x; t < n; t += MON_THREADS) {
         const int i = (int)(t % L.nx) + 1, j = (int)(t / L.nx) + 1;
         const double m = (double)(1 - walls[L.i2(i, j, k)]);
-        const double ph = phi[L.i4(i, j, k)];
+        const double ph = (double)phi[L.i4(i, j, k)];
         v1 += 0.5 * (1.0 + ph) * m;
         v2 += 0.5 * (1.0 - ph) * m;
     }
@@ -1198,7 +1287,7 @@ __global__ void __launch_bounds__(MON_THREADS) k_saturation(const double *__rest
 // singlephase Initialization.F90:248-276), and the convective-outlet memory (:418-467)
 // ---------------------------------------------------------------------------------
 template <class S>
-__global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const double *__restrict__ phi, double *__restrict__ u,
+__global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const typename Store<S>::R *__restrict__ phi, double *__restrict__ u,
                           double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho, const Layout L,
                           int multiphase, float ref, float scale) {
     using St = Store<S>;
@@ -1218,7 +1307,7 @@ __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const double *__
     const double usqrt = 0.0;
     double r0, r1 = 0.0;
     if (multiphase) {
-        const double ph = phi[L.i4(i, j, k)];
+        const double ph = (double)phi[L.i4(i, j, k)];
         r0 = 1.0 * (1.0 + ph) * 0.5;
         r1 = 1.0 * (1.0 - ph) * 0.5;
     } else {
@@ -1230,16 +1319,16 @@ __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const double *__
         const double wq = WEQ(q);
         const double cu = 0.0;
         const double a = q == 0 ? r0 * wq + r0 * wq * (-1.5 * usqrt) : r0 * wq + r0 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
-        St::st(f, (int64_t)q * L.qs + c, R(a), R(WREST(q) * ref), sc);
+        St::st64(f, (int64_t)q * L.qs + c, a, WREST(q) * ref, scale);
         if (multiphase) {
             const double b = q == 0 ? r1 * wq + r1 * wq * (-1.5 * usqrt) : r1 * wq + r1 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
-            St::st(g, (int64_t)q * L.qs + c, R(b), R(WREST(q) * ref), sc);
+            St::st64(g, (int64_t)q * L.qs + c, b, WREST(q) * ref, scale);
         }
     }
 }
 
 template <class S>
-__global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, const double *__restrict__ phi,
+__global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, const typename Store<S>::R *__restrict__ phi,
                               double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
                               const Layout L, int multiphase, float ref, float scale) {
     using St = Store<S>;
@@ -1250,11 +1339,11 @@ __global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, 
     const int i = (int)(t % (L.nx + 2)), j = (int)(t / (L.nx + 2));
     const R inv = R(1.0f / scale);
     for (int q = 0; q < 19; ++q) {
-        fconv[L.ic(i, j, q)] = (double)St::ld(f, (int64_t)q * L.qs + L.cell(i, j, L.nz), R(WREST(q) * ref), inv);
+        fconv[L.ic(i, j, q)] = St::ld64(f, (int64_t)q * L.qs + L.cell(i, j, L.nz), WREST(q) * ref, inv);
         if (multiphase)
-            gconv[L.ic(i, j, q)] = (double)St::ld(g, (int64_t)q * L.qs + L.cell(i, j, L.nz), R(WREST(q) * ref), inv);
+            gconv[L.ic(i, j, q)] = St::ld64(g, (int64_t)q * L.qs + L.cell(i, j, L.nz), WREST(q) * ref, inv);
     }
-    if (multiphase) phiconv[L.ip(i, j)] = phi[L.i4(i, j, L.nz)];
+    if (multiphase) phiconv[L.ip(i, j)] = (double)phi[L.i4(i, j, L.nz)];
 }
 
 // FP64 <-> storage conversion of one direction plane (upload/download of FP32/FP16 state)
@@ -1269,7 +1358,7 @@ __global__ void k_convert_in(S *__restrict__ dst, const double *__restrict__ src
     const int i = (int)(t % (L.nx + 2));
     const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
     const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
-    St::st(dst, L.cell(i, j, k), R(src[t]), R(WREST(q) * ref), R(scale));
+    St::st64(dst, L.cell(i, j, k), src[t], WREST(q) * ref, scale);
 }
 
 template <class S>
@@ -1283,7 +1372,273 @@ __global__ void k_convert_out(double *__restrict__ dst, const S *__restrict__ sr
     const int i = (int)(t % (L.nx + 2));
     const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
     const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
-    dst[t] = (double)St::ld(src, L.cell(i, j, k), R(WREST(q) * ref), R(1.0f / scale));
+    dst[t] = St::ld64(src, L.cell(i, j, k), WREST(q) * ref, 1.0f / scale);
+}
+
+// ---------------------------------------------------------------------------------
+// Fluid-list layout (singlephase samples whose every direction is periodic or walled).
+// A_q = A + q*stride holds the fluid nodes [0, nf) and the bounce-back link slots;
+// nb[(d-1)*nf + x] is the slot of x + e_d (see listlayout.h).  The arithmetic is the
+// dense kernel's (k_sp_step), so the strict flavour stays bit-identical to the oracle.
+// ---------------------------------------------------------------------------------
+// one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
+template <class S, bool ODD>
+__device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
+                                             const int64_t nf, const int64_t t, const StepParams &P,
+                                             const MrtFold<typename Store<S>::R> &cf, const float scale) {
+    using R = typename Store<S>::R;
+    const R inv_scale = R(1.0f / scale);
+    R ft[19];
+    int32_t nbr[18];
+    if (ODD) {
+#pragma unroll
+        for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * nf + t];
+        ft[0] = ld_sweep<S>(A, t, 0, inv_scale);
+#pragma unroll
+        for (int q = 1; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)q * stride + nbr[OPP(q) - 1], q, inv_scale);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
+    }
+#ifdef MFLBM_STRICT
+    const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
+                  ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+    mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
+#else
+    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+#endif
+    const R sc = R(scale);
+    if (ODD) {
+        st_sweep<S>(A, t, 0, ft[0], sc);
+#pragma unroll
+        for (int q = 1; q < 19; ++q) st_sweep<S>(A, (int64_t)OPP(q) * stride + nbr[q - 1], q, ft[q], sc);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) st_sweep<S>(A, (int64_t)q * stride + t, q, ft[q], sc);
+    }
+}
+
+template <class S, bool ODD>
+__global__ void __launch_bounds__(128) k_sp_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
+                                                 const int nf, const StepParams P,
+                                                 const MrtFold<typename Store<S>::R> cf, const float scale) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf) return;
+    sp_list_node<S, ODD>(A, stride, nb, nf, t, P, cf, scale);
+}
+
+// ---------------------------------------------------------------------------------
+// Ensembles: many samples share one fluid-list arena (fluid nodes of all samples first,
+// then all link slots); a tile is a run of at most blockDim fluid nodes of one sample.
+// The tile table and its length live in device memory, so a captured graph keeps
+// working when the host drops converged samples from the table.
+// ---------------------------------------------------------------------------------
+template <class R> __device__ __forceinline__ const MrtFold<R> &ens_fold(const EnsArgs &a);
+template <> __device__ __forceinline__ const MrtFold<double> &ens_fold<double>(const EnsArgs &a) { return a.fold; }
+template <> __device__ __forceinline__ const MrtFold<float> &ens_fold<float>(const EnsArgs &a) { return a.fold32; }
+
+template <class S, bool ODD>
+__device__ __forceinline__ void ens_sweep(const EnsArgs &a) {
+    const int nt = *a.ntiles;
+    for (int tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        const EnsTile T = a.tiles[tile];
+        if ((int)threadIdx.x < T.count)
+            sp_list_node<S, ODD>(reinterpret_cast<S *>(a.A), a.stride, a.nb, a.nf, (int64_t)T.start + threadIdx.x, a.P,
+                                 ens_fold<typename Store<S>::R>(a), a.scale);
+    }
+}
+
+// one step over the active tiles (grid-stride over the tile table)
+template <class S, bool ODD>
+__global__ void k_ens_step(const EnsArgs a) {
+    ens_sweep<S, ODD>(a);
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident).  Sense by
+// generation counter; the wait is bounded: after kBarrierSpins polls the block sets
+// *err and every block leaves at its next barrier.
+constexpr long long kBarrierSpins = 1ll << 26;
+
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, int32_t *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int *vgen = bar + 1;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == gen) {
+                if (++it > kBarrierSpins || *(volatile int32_t *)err) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// nsteps AA steps in one cooperative launch, a grid barrier between consecutive steps
+template <class S>
+__global__ void k_ens_persistent(const EnsArgs a) {
+    for (int s = 0; s < a.nsteps; ++s) {
+        if (((a.ntime0 + s) & 1) != 0) ens_sweep<S, true>(a);
+        else ens_sweep<S, false>(a);
+        if (s + 1 < a.nsteps && !grid_barrier(a.bar, a.err)) return;
+    }
+}
+
+// equilibrium at rest (r0 = 1, u = 0: f_q = w_q) in every slot of the list arrays
+template <class S>
+__global__ void k_list_init(S *__restrict__ A, const int64_t stride, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 19 * stride) return;
+    const int q = (int)(t / stride);
+    St::st64(A, t, WEQ(q), WREST(q), scale);
+}
+
+// dense FP64 plane q (halo-1 Fortran order, in stage) -> list slots of direction q
+template <class S>
+__global__ void k_list_in(S *__restrict__ A, const int64_t stride, const int q, const int32_t *__restrict__ cell1,
+                          const int nf, const int32_t *__restrict__ link, const int64_t nlink,
+                          const double *__restrict__ stage, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    S *Aq = A + (int64_t)q * stride;
+    if (t < nf) {
+        St::st64(Aq, t, stage[cell1[t]], WREST(q), scale);
+    } else if (t - nf < nlink) {
+        const int64_t l = t - nf;
+        if (link[3 * l] == q) St::st64(Aq, link[3 * l + 1], stage[link[3 * l + 2]], WREST(q), scale);
+    }
+}
+
+// list slots of direction q -> dense FP64 plane (stage): every cell first gets the rest
+// equilibrium w_q (the value the reference's untouched slots keep after
+// initialisation), then the fluid nodes and link slots are scattered, then the ghost
+// layers of periodic directions receive their periodic images.
+__global__ void k_list_plane_fill(double *__restrict__ stage, int64_t n, double v) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) stage[t] = v;
+}
+
+template <class S>
+__global__ void k_list_out(const S *__restrict__ A, const int64_t stride, const int q, const int32_t *__restrict__ cell1,
+                           const int nf, const int32_t *__restrict__ link, const int64_t nlink,
+                           double *__restrict__ stage, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const S *Aq = A + (int64_t)q * stride;
+    const R inv = R(1.0f / scale);
+    if (t < nf) {
+        stage[cell1[t]] = St::ld64(Aq, t, WREST(q), 1.0f / scale);
+    } else if (t - nf < nlink) {
+        const int64_t l = t - nf;
+        if (link[3 * l] == q) stage[link[3 * l + 2]] = St::ld64(Aq, link[3 * l + 1], WREST(q), 1.0f / scale);
+    }
+}
+
+__global__ void k_list_ghosts(double *__restrict__ stage, const Layout L, int px, int py, int pz) {
+    const int64_t n = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = (int)(t % (L.nx + 2)), j = (int)((t / (L.nx + 2)) % (L.ny + 2)), k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    const bool gx = i == 0 || i == L.nx + 1, gy = j == 0 || j == L.ny + 1, gz = k == 0 || k == L.nz + 1;
+    if (!(gx || gy || gz)) return;
+    if ((gx && !px) || (gy && !py) || (gz && !pz)) return;
+    if (gx) i = i == 0 ? L.nx : 1;
+    if (gy) j = j == 0 ? L.ny : 1;
+    if (gz) k = k == 0 ? L.nz : 1;
+    stage[t] = stage[L.i1(i, j, k)];
+}
+
+// compute_macro_vars + monitor reductions over the fluid list (singlephase): one block
+// per segment [seg0[b], seg1[b]) of fluid indices (a z slice of one sample, or a whole
+// sample of an ensemble).  out[m * nseg + b]: m = 0 sum w, 6 sum rho, 7 max |u|^2
+// (the rows of the dense k_monitor).  Fields u, v, w, rho are scattered to the halo-1
+// arrays when write_fields (solid cells keep the zeros written before).
+template <class S>
+__global__ void __launch_bounds__(MON_THREADS) k_list_monitor(const S *__restrict__ A, const int64_t stride,
+                                                              const int32_t *__restrict__ seg0,
+                                                              const int32_t *__restrict__ seg1, const int nseg,
+                                                              const int32_t *__restrict__ cell1, double *__restrict__ u,
+                                                              double *__restrict__ v, double *__restrict__ w,
+                                                              double *__restrict__ rho, double *__restrict__ out,
+                                                              const StepParams P, int write_fields, float scale) {
+    using St = Store<S>;
+    using R = typename St::R;
+    const int b = blockIdx.x;
+    const int x0 = seg0[b], x1 = seg1[b];
+    const R inv = R(1.0f / scale);
+    double sw = 0.0, sr = 0.0, um = 0.0;
+    for (int x = x0 + (int)threadIdx.x; x < x1; x += MON_THREADS) {
+        double ft[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = St::ld64(A, (int64_t)q * stride + x, WREST(q), 1.0f / scale);
+        const double rr = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
+                          ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+        const double uu = ft[1] - ft[2] + ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14] - 0.5 * 0.0;
+        const double vv = ft[3] - ft[4] + ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18] - 0.5 * 0.0;
+        const double ww = ft[5] - ft[6] + ft[11] + ft[12] - ft[13] - ft[14] + ft[15] + ft[16] - ft[17] - ft[18] - 0.5 * P.force_z;
+        if (write_fields) {
+            const int32_t c = cell1[x];
+            u[c] = uu; v[c] = vv; w[c] = ww; rho[c] = rr;
+        }
+        const double temp = uu * uu + vv * vv + ww * ww;
+        um = (um < temp) ? temp : um;
+        sw += ww;
+        sr += rr;
+    }
+    __shared__ double red[3][MON_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sw += __shfl_down_sync(0xffffffffu, sw, o);
+        sr += __shfl_down_sync(0xffffffffu, sr, o);
+        const double y = __shfl_down_sync(0xffffffffu, um, o);
+        um = (um < y) ? y : um;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = sw; red[1][threadIdx.x >> 5] = sr; red[2][threadIdx.x >> 5] = um;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, r = 0.0, m = 0.0;
+        for (int q = 0; q < MON_THREADS / 32; ++q) {
+            a += red[0][q];
+            r += red[1][q];
+            m = (m < red[2][q]) ? red[2][q] : m;
+        }
+        out[b] = a;
+        out[(int64_t)6 * nseg + b] = r;
+        out[(int64_t)7 * nseg + b] = m;
+    }
+}
+
+// FP64 host image <-> field array of type T (phi, gradient fields of the mixed form)
+template <class T>
+__global__ void k_field_in(T *__restrict__ dst, const double *__restrict__ src, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (T)src[t];
+}
+
+template <class T>
+__global__ void k_field_out(double *__restrict__ dst, const T *__restrict__ src, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (double)src[t];
 }
 
 }  // namespace MFLBM_NS

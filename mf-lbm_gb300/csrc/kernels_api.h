@@ -18,9 +18,13 @@ struct DevState {
     double rk_weight2;     // 1/sqrt(2)/36 evaluated on the host
     void *f;               // species 1 PDFs (19 planes)
     void *g;               // species 2 PDFs (19 planes), multiphase only
-    double *phi;           // halo 4
-    double *cnx, *cny, *cnz, *cnorm;  // halo 2
-    double *curv, *u, *v, *w, *rho;   // halo 1
+    // phase field and colour-gradient fields: double, or float in the multiphase
+    // FP32 form (element size felt)
+    void *phi;             // halo 4
+    void *cnx, *cny, *cnz, *cnorm;    // halo 2
+    void *curv;            // halo 1
+    int felt;
+    double *u, *v, *w, *rho;          // halo 1, FP64 in every form
     int8_t *walls;         // halo 2
     double *w_in;          // (nx+2)(ny+2)
     double *fconv, *gconv, *phiconv;
@@ -32,6 +36,16 @@ struct DevState {
     double *stage;         // one FP64 plane of the halo-1 box (conversion staging)
     const int32_t *cells;  // padded-layout index of every interior fluid node, ascending
     int ncell;
+    // fluid-list layout (singlephase samples that are periodic or walled in every
+    // direction): f holds 19 arrays of lstride elements, see listlayout.h
+    int list;
+    int64_t lstride;
+    const int32_t *nb;     // [18][nfl]
+    const int32_t *cell1;  // halo-1 index of every fluid node
+    const int32_t *link;   // [nlink][3]
+    int64_t nlink;
+    int nfl;
+    const int32_t *lseg;   // [nz+1] first fluid index of every z slice
     MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
     MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
 };
@@ -55,6 +69,21 @@ struct KernelTable {
     // FP64 plane <-> storage plane (q of species s) through st.stage
     int (*convert_in)(const DevState &, int species, int q, cudaStream_t);
     int (*convert_out)(const DevState &, int species, int q, cudaStream_t);
+    // FP64 image in st.stage <-> field array (phi, gradient fields) of n elements
+    int (*field_in)(const DevState &, void *dst, int64_t n, cudaStream_t);
+    int (*field_out)(const DevState &, const void *src, int64_t n, cudaStream_t);
+    // ensembles (fluid-list arena of many singlephase samples), storage by prec:
+    // persistent != 0: one cooperative launch of a.nsteps steps on `grid` blocks;
+    // else a.nsteps launches of one step each.  Returns kernels launched, -1 on a
+    // launch error.
+    int (*ens_run)(const EnsArgs &a, int prec, int persistent, int grid, int block, cudaStream_t);
+    // per-sample sums into out[m * nseg + b] (m = 0 sum w, 6 sum rho, 7 max |u|^2)
+    int (*ens_monitor)(const EnsArgs &a, int prec, const int32_t *seg0, const int32_t *seg1, int nseg, double *out,
+                       cudaStream_t);
+    // rest equilibrium in every slot
+    int (*ens_init)(const EnsArgs &a, int prec, cudaStream_t);
+    // largest co-resident grid of the persistent kernel for this block size
+    int (*ens_max_grid)(int prec, int block);
 };
 
 const KernelTable *kernels_fast();

@@ -13,13 +13,30 @@ inline dim3 row_block(int nx) {
 
 template <class S> S *fs(const DevState &st) { return reinterpret_cast<S *>(st.f); }
 template <class S> S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g); }
+// field arrays (phi, gradient) of the compute type T
+template <class T> T *fld(void *p) { return reinterpret_cast<T *>(p); }
+
+// storage type of the multiphase forms: FP64, or FP32 for the mixed form
+inline bool mp_fp32(const DevState &st) { return st.multiphase && st.prec == MFLBM_FP32; }
 
 template <class R> const MrtFold<R> &fold_of(const DevState &st);
 template <> const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
 template <> const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
 
 template <class S>
+int collide_list(const DevState &st, bool odd, cudaStream_t s) {
+    const unsigned nb = (unsigned)((st.nfl + 127) / 128);
+    const auto &cf = fold_of<typename Store<S>::R>(st);
+    if (odd)
+        k_sp_list<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+    else
+        k_sp_list<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+    return 1;
+}
+
+template <class S>
 int collide_t(const DevState &st, bool odd, cudaStream_t s) {
+    if (st.list) return collide_list<S>(st, odd, s);
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::R>(st);
@@ -30,21 +47,26 @@ int collide_t(const DevState &st, bool odd, cudaStream_t s) {
     return 1;
 }
 
+template <class T>
+int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
+    if (st.ncell == 0) return 0;
+    const unsigned nb = (unsigned)((st.ncell + 127) / 128);
+    T *f = fs<T>(st), *gg = gs<T>(st);
+    if (odd)
+        k_mp_step<T, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny), fld<T>(st.cnz),
+                                              fld<T>(st.cnorm), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
+                                              st.rk_weight2);
+    else
+        k_mp_step<T, false><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny), fld<T>(st.cnz),
+                                               fld<T>(st.cnorm), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
+                                               st.rk_weight2);
+    return 1;
+}
+
 int collide(const DevState &st, bool odd, cudaStream_t s) {
-    if (st.multiphase) {
-        if (st.ncell == 0) return 0;
-        const unsigned nb = (unsigned)((st.ncell + 127) / 128);
-        double *f = fs<double>(st), *gg = gs<double>(st);
-        if (odd)
-            k_mp_step<true><<<nb, 128, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.cells, st.ncell,
-                                               st.L, st.P, st.rk_weight2);
-        else
-            k_mp_step<false><<<nb, 128, 0, s>>>(f, gg, st.phi, st.cnx, st.cny, st.cnz, st.cnorm, st.curv, st.cells,
-                                                st.ncell, st.L, st.P, st.rk_weight2);
-        return 1;
-    }
+    if (st.multiphase) return mp_fp32(st) ? collide_mp<float>(st, odd, s) : collide_mp<double>(st, odd, s);
     switch (st.prec) {
-        case MFLBM_FP32: return collide_t<float>(st, odd, s);
+        case MFLBM_FP32: return collide_t<dfloat>(st, odd, s);
         case MFLBM_FP16: return collide_t<__half>(st, odd, s);
         default: return collide_t<double>(st, odd, s);
     }
@@ -80,10 +102,11 @@ int wrap_t(const DevState &st, bool pull, cudaStream_t s) {
 }
 
 int wrap(const DevState &st, bool pull, cudaStream_t s) {
-    if (!(st.P.iper || st.P.jper || st.P.kper)) return 0;
+    // the fluid-list neighbour table already wraps periodic directions
+    if (st.list || !(st.P.iper || st.P.jper || st.P.kper)) return 0;
     int n_launch;
-    switch (st.multiphase ? MFLBM_FP64 : st.prec) {
-        case MFLBM_FP32: n_launch = wrap_t<float>(st, pull, s); break;
+    switch (st.prec) {
+        case MFLBM_FP32: n_launch = st.multiphase ? wrap_t<float>(st, pull, s) : wrap_t<dfloat>(st, pull, s); break;
         case MFLBM_FP16: n_launch = wrap_t<__half>(st, pull, s); break;
         default: n_launch = wrap_t<double>(st, pull, s); break;
     }
@@ -91,7 +114,10 @@ int wrap(const DevState &st, bool pull, cudaStream_t s) {
         const Layout &L = st.L;
         const int64_t n = (st.P.kper ? (int64_t)4 * L.nx * L.ny : 0) + (st.P.jper ? (int64_t)4 * L.nx * L.nz : 0) +
                           ((st.P.jper && st.P.kper) ? (int64_t)16 * L.nx : 0);
-        k_wrap_phi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st.phi, L, st.P.jper, st.P.kper);
+        if (mp_fp32(st))
+            k_wrap_phi<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fld<float>(st.phi), L, st.P.jper, st.P.kper);
+        else
+            k_wrap_phi<double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fld<double>(st.phi), L, st.P.jper, st.P.kper);
         ++n_launch;
     }
     return n_launch;
@@ -104,17 +130,19 @@ int boundary_t(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc,
     const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
     const dim3 b(bx), g((L.nx + bx - 1) / bx, L.ny);
     S *f = fs<S>(st), *gg = st.multiphase ? gs<S>(st) : nullptr;
+    using FT = typename Store<S>::R;
+    FT *phi = st.multiphase ? fld<FT>(st.phi) : nullptr;
     const int bo = before_odd ? 1 : 0;
     if (open_z) {
         if (inlet_bc == 1)
-            k_inlet_velocity<S><<<g, b, 0, s>>>(f, gg, st.phi, st.walls, st.w_in, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_inlet_velocity<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, st.w_in, L, st.P, bo, st.multiphase, st.ref, st.scale);
         else if (inlet_bc == 2)
-            k_inlet_zouhe<S><<<g, b, 0, s>>>(f, gg, st.phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_inlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
         if (outlet_bc == 1)
-            k_outlet_convective<S><<<g, b, 0, s>>>(f, gg, st.phi, st.fconv, st.gconv, st.phiconv, st.walls, L, st.P, bo,
+            k_outlet_convective<S><<<g, b, 0, s>>>(f, gg, phi, st.fconv, st.gconv, st.phiconv, st.walls, L, st.P, bo,
                                                    st.multiphase, st.ref, st.scale);
         else if (outlet_bc == 2)
-            k_outlet_zouhe<S><<<g, b, 0, s>>>(f, gg, st.phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_outlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
         n_launch += (inlet_bc == 1 || inlet_bc == 2) + (outlet_bc == 1 || outlet_bc == 2);
     }
     return n_launch;
@@ -122,58 +150,85 @@ int boundary_t(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc,
 
 int boundary(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc, bool open_z, cudaStream_t s) {
     int n_launch;
-    switch (st.multiphase ? MFLBM_FP64 : st.prec) {
-        case MFLBM_FP32: n_launch = boundary_t<float>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
+    switch (st.prec) {
+        case MFLBM_FP32:
+            n_launch = st.multiphase ? boundary_t<float>(st, before_odd, inlet_bc, outlet_bc, open_z, s)
+                                     : boundary_t<dfloat>(st, before_odd, inlet_bc, outlet_bc, open_z, s);
+            break;
         case MFLBM_FP16: n_launch = boundary_t<__half>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
         default: n_launch = boundary_t<double>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
     }
     if (st.multiphase && st.P.porous_plate_cmd != 0 && st.P.z_porous_plate >= 1 && st.P.z_porous_plate <= st.L.nz) {
         const Layout &L = st.L;
         const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
-        double *f = fs<double>(st), *gg = gs<double>(st);
-        double *blocked = st.P.porous_plate_cmd == 1 ? f : gg;
-        double *passing = st.P.porous_plate_cmd == 1 ? gg : f;
-        k_porous_plate<<<dim3((L.nx + bx - 1) / bx, L.ny), bx, 0, s>>>(blocked, passing, L, st.P.z_porous_plate,
-                                                                        before_odd ? 1 : 0);
+        void *blocked = st.P.porous_plate_cmd == 1 ? st.f : st.g;
+        void *passing = st.P.porous_plate_cmd == 1 ? st.g : st.f;
+        const dim3 gp((L.nx + bx - 1) / bx, L.ny);
+        if (mp_fp32(st))
+            k_porous_plate<float><<<gp, bx, 0, s>>>(fld<float>(blocked), fld<float>(passing), L, st.P.z_porous_plate,
+                                                    before_odd ? 1 : 0);
+        else
+            k_porous_plate<double><<<gp, bx, 0, s>>>(fld<double>(blocked), fld<double>(passing), L,
+                                                     st.P.z_porous_plate, before_odd ? 1 : 0);
         ++n_launch;
+    }
+    return n_launch;
+}
+
+template <class T>
+int color_gradient_t(const DevState &st, cudaStream_t s) {
+    const Layout &L = st.L;
+    T *phi = fld<T>(st.phi), *cnx = fld<T>(st.cnx), *cny = fld<T>(st.cny), *cnz = fld<T>(st.cnz);
+    T *cnorm = fld<T>(st.cnorm), *curv = fld<T>(st.curv);
+    int n_launch = 2 + (st.ns > 0 ? 2 : 0) + (st.nf > 0 ? 1 : 0);
+    if (st.ns > 0) k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
+    {
+        const int nxh = L.nx + 4;
+        const int bx = nxh >= 128 ? 128 : ((nxh + 31) / 32) * 32;
+        const dim3 b(bx, 256 / bx > 0 ? (unsigned)(256 / bx) : 1u);
+        const dim3 g((nxh + b.x - 1) / b.x, (L.ny + 4 + b.y - 1) / b.y, L.nz + 4);
+        k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
+    }
+    if (st.nf > 0) k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L);
+    if (st.ns > 0) k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
+    {
+        const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
+        const dim3 b(bx, 256 / bx);
+        const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
+        k_curvature<T><<<g, b, 0, s>>>(cnx, cny, cnz, curv, st.walls, L);
     }
     return n_launch;
 }
 
 int color_gradient(const DevState &st, cudaStream_t s) {
     if (!st.multiphase) return 0;
-    const Layout &L = st.L;
-    int n_launch = 2 + (st.ns > 0 ? 2 : 0) + (st.nf > 0 ? 1 : 0);
-    if (st.ns > 0) k_extrap_phi<<<(st.ns + 127) / 128, 128, 0, s>>>(st.phi, st.sb, st.ns, L);
-    {
-        const int nxh = L.nx + 4;
-        const int bx = nxh >= 128 ? 128 : ((nxh + 31) / 32) * 32;
-        const dim3 b(bx, 256 / bx > 0 ? (unsigned)(256 / bx) : 1u);
-        const dim3 g((nxh + b.x - 1) / b.x, (L.ny + 4 + b.y - 1) / b.y, L.nz + 4);
-        k_normals<<<g, b, 0, s>>>(st.phi, st.walls, st.cnx, st.cny, st.cnz, st.cnorm, L);
-    }
-    if (st.nf > 0) k_wetting<<<(st.nf + 127) / 128, 128, 0, s>>>(st.cnx, st.cny, st.cnz, st.cnorm, st.fb, st.nf, L);
-    if (st.ns > 0) k_extrap_normals<<<(st.ns + 127) / 128, 128, 0, s>>>(st.cnx, st.cny, st.cnz, st.sb, st.ns, L);
-    {
-        const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
-        const dim3 b(bx, 256 / bx);
-        const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
-        k_curvature<<<g, b, 0, s>>>(st.cnx, st.cny, st.cnz, st.curv, st.walls, L);
-    }
-    return n_launch;
+    return mp_fp32(st) ? color_gradient_t<float>(st, s) : color_gradient_t<double>(st, s);
 }
 
 template <class S>
 int monitor_t(const DevState &st, cudaStream_t s) {
-    k_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.multiphase ? gs<S>(st) : nullptr, st.phi, st.walls, st.cnx,
-                                                 st.cny, st.cnz, st.cnorm, st.curv, st.u, st.v, st.w, st.rho, st.mon, st.L,
+    using FT = typename Store<S>::R;
+    if (st.list) {
+        const size_t b1 = sizeof(double) * (size_t)(st.L.nx + 2) * (st.L.ny + 2) * (st.L.nz + 2);
+        cudaMemsetAsync(st.u, 0, b1, s);
+        cudaMemsetAsync(st.v, 0, b1, s);
+        cudaMemsetAsync(st.w, 0, b1, s);
+        cudaMemsetAsync(st.rho, 0, b1, s);
+        cudaMemsetAsync(st.mon, 0, sizeof(double) * kMonNQ * st.L.nz, s);
+        k_list_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.lstride, st.lseg, st.lseg + 1, st.L.nz, st.cell1, st.u, st.v,
+                                                          st.w, st.rho, st.mon, st.P, 1, st.scale);
+        return 1;
+    }
+    k_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.multiphase ? gs<S>(st) : nullptr, fld<FT>(st.phi), st.walls,
+                                                 fld<FT>(st.cnx), fld<FT>(st.cny), fld<FT>(st.cnz), fld<FT>(st.cnorm),
+                                                 fld<FT>(st.curv), st.u, st.v, st.w, st.rho, st.mon, st.L,
                                                  st.P, st.multiphase, 1, st.ref, st.scale);
     return 1;
 }
 
 int monitor(const DevState &st, cudaStream_t s) {
-    switch (st.multiphase ? MFLBM_FP64 : st.prec) {
-        case MFLBM_FP32: return monitor_t<float>(st, s);
+    switch (st.prec) {
+        case MFLBM_FP32: return st.multiphase ? monitor_t<float>(st, s) : monitor_t<dfloat>(st, s);
         case MFLBM_FP16: return monitor_t<__half>(st, s);
         default: return monitor_t<double>(st, s);
     }
@@ -181,20 +236,35 @@ int monitor(const DevState &st, cudaStream_t s) {
 
 int saturation(const DevState &st, cudaStream_t s) {
     if (!st.multiphase) return 0;
-    k_saturation<<<st.L.nz, MON_THREADS, 0, s>>>(st.phi, st.walls, st.mon, st.L);
+    if (mp_fp32(st))
+        k_saturation<float><<<st.L.nz, MON_THREADS, 0, s>>>(fld<float>(st.phi), st.walls, st.mon, st.L);
+    else
+        k_saturation<double><<<st.L.nz, MON_THREADS, 0, s>>>(fld<double>(st.phi), st.walls, st.mon, st.L);
     return 1;
 }
 
 template <class S>
 int init_t(const DevState &st, bool convec, cudaStream_t s) {
     const Layout &L = st.L;
+    if (st.list) {
+        const int64_t n = 19 * st.lstride;
+        k_list_init<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.scale);
+        const size_t b1 = sizeof(double) * (size_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        cudaMemsetAsync(st.u, 0, b1, s);
+        cudaMemsetAsync(st.v, 0, b1, s);
+        cudaMemsetAsync(st.w, 0, b1, s);
+        const int64_t nb1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        k_list_plane_fill<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.rho, nb1, 1.0);
+        return 2;
+    }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     S *g = st.multiphase ? gs<S>(st) : nullptr;
-    k_init_eq<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), g, st.phi, st.u, st.v, st.w, st.rho, L,
+    using FT = typename Store<S>::R;
+    k_init_eq<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), g, fld<FT>(st.phi), st.u, st.v, st.w, st.rho, L,
                                                               st.multiphase, st.ref, st.scale);
     if (convec) {
         const int64_t np = (int64_t)(L.nx + 2) * (L.ny + 2);
-        k_init_convec<S><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(fs<S>(st), g, st.phi, st.fconv, st.gconv, st.phiconv,
+        k_init_convec<S><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(fs<S>(st), g, fld<FT>(st.phi), st.fconv, st.gconv, st.phiconv,
                                                                       L, st.multiphase, st.ref, st.scale);
         return 2;
     }
@@ -202,8 +272,8 @@ int init_t(const DevState &st, bool convec, cudaStream_t s) {
 }
 
 int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
-    switch (st.multiphase ? MFLBM_FP64 : st.prec) {
-        case MFLBM_FP32: return init_t<float>(st, convec, s);
+    switch (st.prec) {
+        case MFLBM_FP32: return st.multiphase ? init_t<float>(st, convec, s) : init_t<dfloat>(st, convec, s);
         case MFLBM_FP16: return init_t<__half>(st, convec, s);
         default: return init_t<double>(st, convec, s);
     }
@@ -212,6 +282,12 @@ int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
 template <class S>
 int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
+    if (st.list) {
+        const int64_t n = st.nfl + st.nlink;
+        k_list_in<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, q, st.cell1, st.nfl, st.link,
+                                                                 st.nlink, st.stage, st.scale);
+        return 1;
+    }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     S *base = (sp == 0 ? fs<S>(st) : gs<S>(st)) + (int64_t)q * L.qs;
     k_convert_in<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(base, st.stage, L, q, st.ref, st.scale);
@@ -221,6 +297,15 @@ int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
 template <class S>
 int convert_out_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
+    if (st.list) {
+        const int64_t nb1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        const int64_t n = st.nfl + st.nlink;
+        k_list_plane_fill<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.stage, nb1, WEQ(q));
+        k_list_out<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, q, st.cell1, st.nfl, st.link,
+                                                                  st.nlink, st.stage, st.scale);
+        k_list_ghosts<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.stage, L, st.P.iper, st.P.jper, st.P.kper);
+        return 3;
+    }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const S *base = (sp == 0 ? fs<S>(st) : gs<S>(st)) + (int64_t)q * L.qs;
     k_convert_out<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(st.stage, base, L, q, st.ref, st.scale);
@@ -229,7 +314,7 @@ int convert_out_t(const DevState &st, int sp, int q, cudaStream_t s) {
 
 int convert_in(const DevState &st, int sp, int q, cudaStream_t s) {
     switch (st.prec) {
-        case MFLBM_FP32: return convert_in_t<float>(st, sp, q, s);
+        case MFLBM_FP32: return st.multiphase ? convert_in_t<float>(st, sp, q, s) : convert_in_t<dfloat>(st, sp, q, s);
         case MFLBM_FP16: return convert_in_t<__half>(st, sp, q, s);
         default: return convert_in_t<double>(st, sp, q, s);
     }
@@ -237,13 +322,92 @@ int convert_in(const DevState &st, int sp, int q, cudaStream_t s) {
 
 int convert_out(const DevState &st, int sp, int q, cudaStream_t s) {
     switch (st.prec) {
-        case MFLBM_FP32: return convert_out_t<float>(st, sp, q, s);
+        case MFLBM_FP32: return st.multiphase ? convert_out_t<float>(st, sp, q, s) : convert_out_t<dfloat>(st, sp, q, s);
         case MFLBM_FP16: return convert_out_t<__half>(st, sp, q, s);
         default: return convert_out_t<double>(st, sp, q, s);
     }
 }
 
-const KernelTable table = {collide, wrap, boundary, color_gradient, monitor, saturation, init_equilibrium, convert_in, convert_out};
+int field_in(const DevState &st, void *dst, int64_t n, cudaStream_t s) {
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (st.felt == 4) k_field_in<float><<<nb, 256, 0, s>>>(fld<float>(dst), st.stage, n);
+    else k_field_in<double><<<nb, 256, 0, s>>>(fld<double>(dst), st.stage, n);
+    return 1;
+}
+
+int field_out(const DevState &st, const void *src, int64_t n, cudaStream_t s) {
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (st.felt == 4) k_field_out<float><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const float *>(src), n);
+    else k_field_out<double><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const double *>(src), n);
+    return 1;
+}
+
+// ---- ensembles --------------------------------------------------------------------
+template <class S>
+int ens_run_t(const EnsArgs &a, int persistent, int grid, int block, cudaStream_t s) {
+    if (persistent) {
+        void *args[] = {const_cast<EnsArgs *>(&a)};
+        cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ens_persistent<S>, dim3(grid), dim3(block), args, 0, s);
+        return e == cudaSuccess ? 1 : -1;
+    }
+    for (int t = 0; t < a.nsteps; ++t) {
+        if (((a.ntime0 + t) & 1) != 0) k_ens_step<S, true><<<grid, block, 0, s>>>(a);
+        else k_ens_step<S, false><<<grid, block, 0, s>>>(a);
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? a.nsteps : -1;
+}
+
+int ens_run(const EnsArgs &a, int prec, int persistent, int grid, int block, cudaStream_t s) {
+    switch (prec) {
+        case MFLBM_FP32: return ens_run_t<dfloat>(a, persistent, grid, block, s);
+        case MFLBM_FP16: return ens_run_t<__half>(a, persistent, grid, block, s);
+        default: return ens_run_t<double>(a, persistent, grid, block, s);
+    }
+}
+
+template <class S>
+int ens_monitor_t(const EnsArgs &a, const int32_t *seg0, const int32_t *seg1, int nseg, double *out, cudaStream_t s) {
+    k_list_monitor<S><<<nseg, MON_THREADS, 0, s>>>(reinterpret_cast<const S *>(a.A), a.stride, seg0, seg1, nseg, nullptr,
+                                                   nullptr, nullptr, nullptr, nullptr, out, a.P, 0, a.scale);
+    return 1;
+}
+
+int ens_monitor(const EnsArgs &a, int prec, const int32_t *seg0, const int32_t *seg1, int nseg, double *out,
+                cudaStream_t s) {
+    switch (prec) {
+        case MFLBM_FP32: return ens_monitor_t<dfloat>(a, seg0, seg1, nseg, out, s);
+        case MFLBM_FP16: return ens_monitor_t<__half>(a, seg0, seg1, nseg, out, s);
+        default: return ens_monitor_t<double>(a, seg0, seg1, nseg, out, s);
+    }
+}
+
+int ens_init(const EnsArgs &a, int prec, cudaStream_t s) {
+    const int64_t n = 19 * a.stride;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    switch (prec) {
+        case MFLBM_FP32: k_list_init<dfloat><<<nb, 256, 0, s>>>(reinterpret_cast<dfloat *>(a.A), a.stride, a.scale); break;
+        case MFLBM_FP16: k_list_init<__half><<<nb, 256, 0, s>>>(reinterpret_cast<__half *>(a.A), a.stride, a.scale); break;
+        default: k_list_init<double><<<nb, 256, 0, s>>>(reinterpret_cast<double *>(a.A), a.stride, a.scale); break;
+    }
+    return 1;
+}
+
+int ens_max_grid(int prec, int block) {
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    cudaError_t e;
+    switch (prec) {
+        case MFLBM_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<dfloat>, block, 0); break;
+        case MFLBM_FP16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<__half>, block, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<double>, block, 0); break;
+    }
+    return e == cudaSuccess ? per * nsm : 0;
+}
+
+const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,
+                           init_equilibrium, convert_in,  convert_out, field_in,      field_out,
+                           ens_run,          ens_monitor, ens_init,   ens_max_grid};
 
 }  // namespace MFLBM_NS
 }  // namespace mflbm

@@ -1,0 +1,187 @@
+// nn_gemm.cu -- BF16 GEMM on the fifth-generation tensor cores (tcgen05, TMEM
+// accumulators), the contraction under every convolution of the warm-start network.
+//
+//   C[M][N] (fp32, ldc) = (accumulate ? C : 0) + A[M][K] * B[N][K]^T
+//   A, B bf16, K contiguous (row strides lda, ldb: multiples of 8 elements), FP32
+//   accumulation in TMEM.  M, N, K arbitrary with N % 16 == 0 and K % 8 == 0: tiles
+//   are zero-filled past the edges and the epilogue masks them.
+//
+// One CTA = 4 warps computes a 128 x BN tile.  K advances in steps of 64 (one 128-byte
+// swizzle row) through a 3-stage shared-memory ring filled with cp.async (16-byte
+// chunks placed at their 128B-swizzled positions); one thread issues four
+// tcgen05.mma (K = 16 each) per stage and commits them to the stage's mbarrier, which
+// gates the refill.  The epilogue reads the accumulator rows of each warp's 32 TMEM
+// lanes with tcgen05.ld.  Every mbarrier wait is bounded; a timeout sets *err.
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/mflbm.h"
+#include "umma.cuh"
+
+namespace mflbm {
+namespace nn {
+
+constexpr int kStages = 3;
+constexpr long long kWaitLimit = 1ll << 22;
+
+template <int BN>
+struct GemmSmem {
+    static constexpr int kA = 128 * 128;   // bytes per stage: 128 rows x 128 B
+    static constexpr int kB = BN * 128;
+    static constexpr int kStage = kA + kB;
+    static constexpr int kBytes = kStages * kStage + 1024;   // + alignment slack
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restrict__ A, int lda,
+                                                   const __nv_bfloat16 *__restrict__ B, int ldb, float *__restrict__ C,
+                                                   int ldc, int M, int N, int K, int accumulate, int *__restrict__ err) {
+    using namespace umma;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ uint64_t bars[kStages];
+    __shared__ uint32_t tmem_slot;
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+    const int KT = (K + 63) / 64;
+    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, kCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    auto load_stage = [&](int s, int kt) {
+        uint8_t *sa = smem + s * GemmSmem<BN>::kStage;
+        uint8_t *sb = sa + GemmSmem<BN>::kA;
+        const int k0 = kt * 64;
+        // A: 128 rows x 8 chunks
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int idx = tid + i * 128;
+            const int r = idx >> 3, c = idx & 7;
+            const int gr = m0 + r, gk = k0 + c * 8;
+            const bool ok = gr < M && gk < K;
+            const __nv_bfloat16 *src = ok ? A + (int64_t)gr * lda + gk : A;
+            cp_async16(sa + r * 128 + ((c ^ (r & 7)) << 4), src, ok);
+        }
+        // B: BN rows x 8 chunks
+#pragma unroll
+        for (int i = 0; i < (BN * 8 + 127) / 128; ++i) {
+            const int idx = tid + i * 128;
+            if (idx < BN * 8) {
+                const int r = idx >> 3, c = idx & 7;
+                const int gn = n0 + r, gk = k0 + c * 8;
+                const bool ok = gn < N && gk < K;
+                const __nv_bfloat16 *src = ok ? B + (int64_t)gn * ldb + gk : B;
+                cp_async16(sb + r * 128 + ((c ^ (r & 7)) << 4), src, ok);
+            }
+        }
+    };
+
+    bool ok = true;
+    for (int s = 0; s < kStages - 1; ++s) {
+        if (s < KT) load_stage(s, s);
+        cp_async_commit();
+    }
+    const uint32_t idesc = idesc_bf16_f32(128, BN);
+    for (int kt = 0; kt < KT && ok; ++kt) {
+        const int s = kt % kStages;
+        cp_async_wait<kStages - 2>();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + s * GemmSmem<BN>::kStage);
+            const uint32_t sb = sa + GemmSmem<BN>::kA;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                mma_bf16(tmem, desc_sw128(sa + j * 32), desc_sw128(sb + j * 32), idesc, (kt > 0 || j > 0) ? 1u : 0u);
+            mma_commit(&bars[s]);
+        }
+        // refill the stage that MMA kt-1 read once it has completed
+        const int nk = kt + kStages - 1;
+        if (nk < KT) {
+            if (kt >= 1) {
+                const int ps = (kt - 1) % kStages;
+                if (!mbar_wait(&bars[ps], (uint32_t)(((kt - 1) / kStages) & 1), kWaitLimit)) ok = false;
+            }
+            if (ok) load_stage(nk % kStages, nk);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    // all MMAs issued so far complete when the last commit arrives
+    if (ok && KT > 0) {
+        const int ls = (KT - 1) % kStages;
+        if (!mbar_wait(&bars[ls], (uint32_t)(((KT - 1) / kStages) & 1), kWaitLimit)) ok = false;
+    }
+    if (!ok && lane == 0) atomicExch(err, 1);
+    __syncthreads();
+    tc_fence_after();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float v[16];
+            if (KT > 0) {
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = 0.f;
+            }
+            if (row < M) {
+                float *dst = C + (int64_t)row * ldc + n0 + c0;
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (n0 + c0 + i < N) dst[i] = accumulate ? dst[i] + v[i] : v[i];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+template <int BN>
+int launch_gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N, int K,
+                int accumulate, int *err, cudaStream_t s) {
+    const int bytes = GemmSmem<BN>::kBytes;
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+            return MFLBM_ECUDA;
+        configured = true;
+    }
+    dim3 grid((M + 127) / 128, (N + BN - 1) / BN);
+    k_gemm_bf16<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, M, N, K, accumulate, err);
+    return cudaPeekAtLastError() == cudaSuccess ? MFLBM_OK : MFLBM_ECUDA;
+}
+
+}  // namespace nn
+}  // namespace mflbm
+
+using namespace mflbm;
+
+extern "C" int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
+                                      int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t *err, void *stream) {
+    if (!A || !B || !C || !err || M < 0 || N < 0 || K < 0) return MFLBM_EINVAL;
+    if (N % 16 || K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N) return MFLBM_EINVAL;
+    if (((uintptr_t)A | (uintptr_t)B) & 15) return MFLBM_EINVAL;
+    if (M == 0 || N == 0) return MFLBM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const __nv_bfloat16 *a = (const __nv_bfloat16 *)A, *b = (const __nv_bfloat16 *)B;
+    if (N % 128 == 0 || N > 64) return nn::launch_gemm<128>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
+    if (N > 32) return nn::launch_gemm<64>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
+    if (N > 16) return nn::launch_gemm<32>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
+    return nn::launch_gemm<16>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
+}

@@ -10,7 +10,8 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libmflbm.so")
 
-MFLBM_ABI_VERSION = 1
+MFLBM_ABI_VERSION = 2
+LAYOUT_AUTO, LAYOUT_DENSE, LAYOUT_LIST = 0, 1, 2
 MFLBM_OK = 0
 MFLBM_EINVAL = -1
 MFLBM_ECUDA = -2
@@ -45,6 +46,7 @@ class Params(C.Structure):
         ("inlet_bc", C.c_int32), ("outlet_bc", C.c_int32), ("mrt", C.c_int32),
         ("porous_plate_cmd", C.c_int32), ("z_porous_plate", C.c_int32),
         ("precision", C.c_int32), ("strict_fp", C.c_int32), ("device", C.c_int32),
+        ("layout", C.c_int32),
         ("la_nu1", C.c_double), ("la_nu2", C.c_double), ("gamma", C.c_double), ("beta", C.c_double),
         ("sa_inject", C.c_double), ("force_z", C.c_double), ("uin_avg", C.c_double),
         ("rho_in", C.c_double), ("rho_out", C.c_double), ("relaxation", C.c_double),
@@ -78,6 +80,19 @@ PP = C.POINTER(C.c_void_p)
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "mflbm_version": (C.c_int32, []),
+    "mflbm_nn_gemm_bf16": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_int32, P, P]),
+    "mflbm_ensemble_create": (C.c_int32, [C.POINTER(Params), C.c_int32, P, P, C.POINTER(C.c_void_p)]),
+    "mflbm_ensemble_destroy": (None, [P]),
+    "mflbm_ensemble_last_error": (C.c_char_p, [P]),
+    "mflbm_ensemble_init": (C.c_int32, [P]),
+    "mflbm_ensemble_set_active": (C.c_int32, [P, P]),
+    "mflbm_ensemble_run": (C.c_int32, [P, C.c_int32, C.c_int32]),
+    "mflbm_ensemble_flux": (C.c_int32, [P, P, P, P]),
+    "mflbm_ensemble_configure": (C.c_int32, [P, C.c_int32, C.c_int32]),
+    "mflbm_ensemble_tune": (C.c_int32, [P, C.c_int32, P, C.c_int32]),
+    "mflbm_ensemble_info": (C.c_int32, [P, P, P, P, P]),
+    "mflbm_layout": (C.c_int32, [P]),
     "mflbm_create": (C.c_int32, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "mflbm_destroy": (None, [P]),
     "mflbm_last_error": (C.c_char_p, [P]),

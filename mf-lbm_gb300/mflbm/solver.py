@@ -56,6 +56,11 @@ class Solver:
         _capi.check(self.lib, None, rc)
         self.ctx = h
 
+    @property
+    def layout(self):
+        """LAYOUT_DENSE or LAYOUT_LIST once the geometry is set (LAYOUT_AUTO before)."""
+        return self.lib.mflbm_layout(self.ctx)
+
     # --- shapes -------------------------------------------------------------------
     def shape1(self):
         return (self.nz + 2, self.ny + 2, self.nx + 2)

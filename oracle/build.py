@@ -19,6 +19,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "mflbm_oracle.cpp")
+HEADER = os.path.join(HERE, "..", "include", "mflbm.h")
 
 VARIANTS = {
     "liborc_strict.so": ["-O2", "-ffp-contract=off", "-fno-fast-math"],
@@ -35,7 +36,8 @@ def build(force=False, verbose=False):
     procs = []
     for name, flags in VARIANTS.items():
         out = os.path.join(OUT, name)
-        if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
+        newest = max(os.path.getmtime(SRC), os.path.getmtime(HEADER))
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
             continue
         cmd = ["g++", "-std=c++17", "-shared", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function",
                *flags, SRC, "-o", out + ".tmp"]

@@ -37,13 +37,14 @@ def perturbed_pdfs(shape1, seed, rho1=None, amp=1e-3, weights=W):
 
 
 def sp_case(nx=12, ny=10, nz=14, per=(0, 1, 1), inlet=0, outlet=0, force=1e-5, nu=0.1, mrt=1, spheres=3, seed=1,
-            precision=0, strict=1, uin=5e-3, rho_in=1.001, rest="bgk"):
+            precision=0, strict=1, uin=5e-3, rho_in=1.001, rest="bgk", layout=0):
     iper, jper, kper = per
     p = make_params(multiphase=0, nx=nx, ny=ny, nz=nz, iper=iper, jper=jper, kper=kper,
                     wall_x_min=0 if iper else 1, wall_x_max=0 if iper else 1,
                     wall_y_min=0 if jper else 1, wall_y_max=0 if jper else 1,
                     wall_z_min=0, wall_z_max=0, inlet_bc=inlet, outlet_bc=outlet, mrt=mrt, la_nu1=nu,
-                    force_z=force, uin_avg=uin, rho_in=rho_in, rho_out=1.0, precision=precision, strict_fp=strict)
+                    force_z=force, uin_avg=uin, rho_in=rho_in, rho_out=1.0, precision=precision, strict_fp=strict,
+                    layout=layout)
     wg = random_spheres((nz, ny, nx), spheres, 1.5, 3.0, seed) if spheres else np.zeros((nz, ny, nx), np.int8)
     walls, pore, _ = geometry.set_walls(p, wg)
     w_in = geometry.inlet_profile(nx, ny, uin) if inlet == 1 else None
@@ -69,13 +70,13 @@ def smooth_phase(shape4, seed, kind="blob"):
 
 def mp_case(nx=14, ny=12, nz=16, per=(0, 1, 1), inlet=0, outlet=0, force=0.0, spheres=2, seed=3, theta_deg=45.0,
             mrt=2, nu1=1.0 / 6.0, nu2=1.0 / 6.0, gamma=0.01, beta=0.95, strict=1, uin=1e-3, rho_in=1.001,
-            plate=0, zplate=0, sa_inject=1.0):
+            plate=0, zplate=0, sa_inject=1.0, precision=0):
     _, jper, kper = per
     p = make_params(multiphase=1, nx=nx, ny=ny, nz=nz, iper=0, jper=jper, kper=kper, wall_x_min=1, wall_x_max=1,
                     wall_y_min=0 if jper else 1, wall_y_max=0 if jper else 1, wall_z_min=0, wall_z_max=0,
                     inlet_bc=inlet, outlet_bc=outlet, mrt=mrt, la_nu1=nu1, la_nu2=nu2, gamma=gamma, beta=beta,
                     sa_inject=sa_inject, force_z=force, uin_avg=uin, rho_in=rho_in, rho_out=1.0, strict_fp=strict,
-                    porous_plate_cmd=plate, z_porous_plate=zplate)
+                    porous_plate_cmd=plate, z_porous_plate=zplate, precision=precision)
     wg = random_spheres((nz, ny, nx), spheres, 1.5, 3.0, seed) if spheres else np.zeros((nz, ny, nx), np.int8)
     walls, pore, wchan = geometry.set_walls(p, wg)
     solid, fluid = geometry.preprocess(p, wchan, geometry.contact_angle_rad(theta_deg))
@@ -99,3 +100,22 @@ def load_case(sim, case):
                      case.get("phi_convec"))
     if case["params"].multiphase:
         sim.color_gradient()
+
+
+def periodic_ghosts(a, per):
+    """Fill the halo-1 ghost layers of the periodic axes of a (..., nz+2, ny+2, nx+2)
+    array with their periodic images (x, then y, then z, so edges and corners follow)."""
+    a = a.copy()
+    for axis, p in zip((-1, -2, -3), per):
+        if not p:
+            continue
+        n = a.shape[axis] - 2
+        src_hi = [slice(None)] * a.ndim
+        dst_lo = [slice(None)] * a.ndim
+        src_lo = [slice(None)] * a.ndim
+        dst_hi = [slice(None)] * a.ndim
+        src_hi[axis], dst_lo[axis] = slice(n, n + 1), slice(0, 1)
+        src_lo[axis], dst_hi[axis] = slice(1, 2), slice(n + 1, n + 2)
+        a[tuple(dst_lo)] = a[tuple(src_hi)]
+        a[tuple(dst_hi)] = a[tuple(src_lo)]
+    return a

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     src = open(os.path.join(ROOT, "include", "mflbm.h")).read()
-    return sorted(set(re.findall(r"\b(mflbm_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(mflbm_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol():
