@@ -46,10 +46,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5"],
                     help="c2: singlephase packing permeability (default); c1: multiphase tube drainage; "
-                         "c3: multiphase packing drainage; c4: batched permeability ensemble to steady state")
+                         "c3: multiphase packing drainage; c4: batched permeability ensemble to steady state; "
+                         "c5: learned warm start (train the network, then A/B against runs from rest)")
     ap.add_argument("--samples", type=int, default=256, help="c4: ensemble size")
+    ap.add_argument("--train", type=int, default=200, help="c5: training samples")
+    ap.add_argument("--test", type=int, default=6, help="c5: held-out samples")
+    ap.add_argument("--epochs", type=int, default=8, help="c5: training epochs")
+    ap.add_argument("--n5", type=int, default=128, help="c5: sample edge")
+    ap.add_argument("--c3-study", action="store_true",
+                    help="c3: FP64 and FP32 forms over --c3-steps steps, saturation every 500 steps, phi L1 error")
+    ap.add_argument("--c3-steps", type=int, default=20000)
     ap.add_argument("--c4-fp64", action="store_true", help="c4: also run the FP64 ensemble for per-sample k errors")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
     ap.add_argument("--porosity", type=float, default=0.22)
@@ -193,8 +201,11 @@ def convergence_study(args, case, device):
             sim.run(1, 100)          # graph capture outside the clock
             sim.init_equilibrium()
             sim.synchronize()
-            r = run_to_steady(sim, p, check_every=100, tol=args.conv_tol, max_steps=200000)
-        form = {"k": r.k, "steps": r.steps, "seconds": r.seconds, "converged": r.converged, "status": r.status}
+            # FP16's 11-bit significand puts its noise floor above 1e-7: it runs to 1e-5
+            tol = args.conv_tol if prec != 2 else max(args.conv_tol, 1e-5)
+            r = run_to_steady(sim, p, check_every=100, tol=tol, max_steps=200000)
+        form = {"k": r.k, "steps": r.steps, "seconds": r.seconds, "converged": r.converged, "status": r.status,
+                "tol": tol}
         if prec == 0:
             base = r
         else:
@@ -280,12 +291,146 @@ def ensemble_study(args):
     return 0
 
 
+def warmstart_study(args):
+    """c5: train the warm-start network on LBM solutions the solver produces (FP32
+    deviation form to |du|/u < 1e-6), then on held-out samples compare runs to 1e-7 from
+    rest and from the prediction (FP64 and FP32), wall time including inference."""
+    from mflbm import warmstart as ws
+    n = args.n5
+    t0 = time.perf_counter()
+    workers = min(16, os.cpu_count() or 1)
+    train_s = ws.make_samples(n, args.train, seed=101, workers=workers)
+    test_s = ws.make_samples(n, args.test, seed=202, workers=workers)
+    gen_s = time.perf_counter() - t0
+    import torch
+    torch.cuda.set_device(0)
+    nu, fz = 1.0 / 6.0, 1e-6
+    xs, ys, ms = [], [], []
+    t0 = time.perf_counter()
+    data_lu = 0
+    for wg, x in train_s:
+        r, mac, _ = ws.solve(wg, precision=1, tol=1e-6, nu=nu, fz=fz)
+        data_lu += int((wg == 0).sum()) * r.steps
+        xs.append(torch.from_numpy(x).cuda().to(torch.bfloat16))
+        ys.append(torch.from_numpy(ws.target_from_macro(mac, nu, fz)).cuda())
+        ms.append(torch.from_numpy((wg == 0).reshape(-1).astype(np.float32)).cuda())
+    data_s = time.perf_counter() - t0
+    net = ws.Net(n, seed=7)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = ws.train(net, xs, ys, ms, epochs=args.epochs, lr=1e-3, lr_end=1e-4, seed=3)
+    torch.cuda.synchronize()
+    train_s_time = time.perf_counter() - t0
+    rows = []
+    for wg, x in test_s:
+        ref = ws.solve(wg, precision=0, tol=args.conv_tol, nu=nu, fz=fz)[0]
+        r32 = ws.solve(wg, precision=1, tol=args.conv_tol, nu=nu, fz=fz)[0]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        net.forward(torch.from_numpy(x).cuda().to(torch.bfloat16))
+        out = net.out.cpu().numpy()
+        u = ws.velocity_from_output(out, n, nu, fz, wg)
+        infer = time.perf_counter() - t1
+        w64, _, set64 = ws.solve(wg, precision=0, tol=args.conv_tol, init_u=u, nu=nu, fz=fz)
+        w32, _, set32 = ws.solve(wg, precision=1, tol=args.conv_tol, init_u=u, nu=nu, fz=fz)
+        k0 = nu * float(np.mean(u[2])) / fz
+        rows.append({"porosity": float((wg == 0).mean()), "k_fp64_rest": ref.k, "steps_fp64_rest": ref.steps,
+                     "s_fp64_rest": ref.seconds, "steps_fp32_rest": r32.steps, "s_fp32_rest": r32.seconds,
+                     "k_err_fp32_rest": abs(r32.k - ref.k) / ref.k,
+                     "steps_fp64_warm": w64.steps, "s_fp64_warm": w64.seconds + infer + set64,
+                     "k_err_fp64_warm": abs(w64.k - ref.k) / ref.k,
+                     "steps_fp32_warm": w32.steps, "s_fp32_warm": w32.seconds + infer + set32,
+                     "k_err_fp32_warm": abs(w32.k - ref.k) / ref.k,
+                     "k_err_prediction_only": abs(k0 - ref.k) / ref.k, "inference_s": infer})
+    def agg(key, f=np.mean):
+        return float(f([r[key] for r in rows]))
+    line = {"metric": METRIC, "value": agg("s_fp64_rest") / agg("s_fp32_warm"), "unit": "x wall-time speed-up "
+            "(FP64 from rest / FP32 + warm start, to the same tolerance)", "n_gpus": 1, "steps": None, "warmup": 0,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
+            "data": "synthetic",
+            "config": {"workload": f"learned warm start: {n}^3 sphere packings, porosity U[0.15,0.35], F_z=1e-6, tau=1, "
+                                   f"{args.train} training samples (FP32 LBM to 1e-6), {args.test} held-out samples, "
+                                   f"convergence {args.conv_tol} every 100 steps",
+                       "generate_s": gen_s, "training_data_s": data_s, "training_data_mlups": data_lu / data_s / 1e6,
+                       "train_s": train_s_time, "epochs": args.epochs, "loss_per_epoch": hist,
+                       "mean": {k: agg(k) for k in rows[0]}, "max_k_err_fp32_warm": agg("k_err_fp32_warm", np.max),
+                       "max_k_err_fp64_warm": agg("k_err_fp64_warm", np.max),
+                       "steps_ratio_fp64_rest_over_warm": agg("steps_fp64_rest") / agg("steps_fp64_warm"),
+                       "time_ratio_fp64_rest_over_fp64_warm": agg("s_fp64_rest") / agg("s_fp64_warm"),
+                       "time_ratio_fp64_rest_over_fp32_rest": agg("s_fp64_rest") / agg("s_fp32_rest"),
+                       "samples": rows}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def drainage_study(args):
+    """c3 at scale: the FP64 form and the FP32 mixed form of the same drainage from the
+    same initial state; saturation (FP64 device sums) every 500 steps and, at the end,
+    the phi-field L1 error of the mixed form against FP64 over the interior nodes."""
+    import copy
+    import torch
+    from mflbm import Solver, workloads
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, precision=0)
+    gen_s = time.perf_counter() - t0
+    res = {}
+    every = 500
+    for prec in (0, 1):
+        p = copy.copy(case["params"])
+        p.precision = prec
+        with Solver(p) as sim:
+            setup(sim, case)
+            sim.run(1, 2)
+            setup(sim, case)
+            sim.synchronize()
+            sat = []
+            run_s = 0.0
+            done = 0
+            while done < args.c3_steps:
+                k = min(every, args.c3_steps - done)
+                t1 = time.perf_counter()
+                sim.run(1 + done, k)
+                sim.synchronize()
+                run_s += time.perf_counter() - t1
+                done += k
+                v1, v2 = sim.saturation()
+                sat.append((done, v1 / (v1 + v2)))
+            phi = sim.macro()["phi"][4:-4, 4:-4, 4:-4].copy()
+        res[prec] = (sat, phi, run_s)
+    fluid = case["walls"][2:-2, 2:-2, 2:-2] == 0
+    dphi = np.abs(res[1][1] - res[0][1])[fluid]
+    s64 = np.array([x[1] for x in res[0][0]])
+    s32 = np.array([x[1] for x in res[1][0]])
+    pore = case["pore"]
+    line = {"metric": METRIC, "value": pore * args.c3_steps / res[1][2] / 1e6, "unit": "MLUPS", "n_gpus": 1,
+            "steps": args.c3_steps, "warmup": 2, "ms_per_step": 1e3 * res[1][2] / args.c3_steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"multiphase drainage, {args.n}^2x{args.n} sphere packing porosity 0.22 + 32-layer "
+                                   "buffers, inlet velocity 5e-5, gamma=0.01, theta=30; FP32 mixed form vs FP64",
+                       "lattice": [case["params"].nx, case["params"].ny, case["params"].nz], "fluid_nodes": pore,
+                       "generate_s": gen_s, "fp64_mlups": pore * args.c3_steps / res[0][2] / 1e6,
+                       "fp32_mlups": pore * args.c3_steps / res[1][2] / 1e6,
+                       "wall_s": {"fp64": res[0][2], "fp32": res[1][2]},
+                       "saturation_every_500": {"step": [x[0] for x in res[0][0]], "fp64": s64.tolist(),
+                                                "fp32": s32.tolist()},
+                       "max_abs_saturation_diff": float(np.abs(s64 - s32).max()),
+                       "phi_L1_fp32_vs_fp64": float(dphi.mean()), "phi_max_abs_diff": float(dphi.max()),
+                       "timed": "host clock around graph-replayed runs of 500 steps, saturation sums outside"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "c3" and args.c3_study:
+        return drainage_study(args)
     if args.workload == "c4":
         return ensemble_study(args)
+    if args.workload == "c5":
+        return warmstart_study(args)
     world, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)

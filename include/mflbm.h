@@ -297,6 +297,43 @@ int32_t mflbm_ensemble_info(const mflbm_ensemble *ens, int64_t *active_nodes, in
  * N % 16 == 0, K % 8 == 0, lda, ldb % 8 == 0, A and B 16-byte aligned. */
 int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
                            int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t *err, void *stream);
+/* The same with the K range split over ksplit CTAs per output tile (long reductions);
+ * work holds ksplit * M * N floats. */
+int32_t mflbm_nn_gemm_bf16_splitk(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
+                                  int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t ksplit, float *work,
+                                  int32_t *err, void *stream);
+
+/* Channels-last activations [D][H][W][C] (bf16 unless stated), 3x3x3 periodic stencil.
+ * col[v][tap*Cin + c] = X[v + d_tap][c], zero for k in [27*Cin, Kp). */
+int32_t mflbm_nn_im2col(const void *X, int32_t D, int32_t H, int32_t W, int32_t Cin, int32_t Kp, void *col,
+                        void *stream);
+/* adjoint of im2col: dX[v][c] = sum over taps of dcol[v - d_tap][tap*Cin + c] (fp32) */
+int32_t mflbm_nn_col2im(const float *dcol, int32_t D, int32_t H, int32_t W, int32_t Cin, int32_t Kp, float *dX,
+                        void *stream);
+/* out[r][c] (bf16, ld_out) = in[c][r] (fp32 when in_f32, else bf16), zero-padded to Rp x Cp */
+int32_t mflbm_nn_transpose_bf16(const void *in, int32_t in_f32, int64_t ld_in, int64_t R, int64_t C, void *out,
+                                int64_t ld_out, int64_t Rp, int64_t Cp, void *stream);
+/* y = act(acc + bias): pre (fp32, nullable), Y (bf16, nullable), Yf (fp32, nullable); relu 0/1 */
+int32_t mflbm_nn_bias_act(const float *acc, const float *bias, float *pre, void *Y, float *Yf, int64_t nvox,
+                          int32_t N, int32_t ld_acc, int32_t relu, void *stream);
+int32_t mflbm_nn_relu_back(float *g, const float *pre, int64_t n, void *stream);
+int32_t mflbm_nn_bias_grad(const float *g, float *db, int64_t nvox, int32_t N, void *stream);
+int32_t mflbm_nn_avgpool2(const void *X, void *Y, int32_t D, int32_t H, int32_t W, int32_t C, void *stream);
+int32_t mflbm_nn_avgpool2_back(const float *dY, float *dX, int32_t D, int32_t H, int32_t W, int32_t C, void *stream);
+/* Y (C1 + C2 channels, fine grid D x H x W) = [nearest x2 upsampling of Xc, S] */
+int32_t mflbm_nn_up2_concat(const void *Xc, int32_t C1, const void *S, int32_t C2, void *Y, int32_t D, int32_t H,
+                            int32_t W, void *stream);
+int32_t mflbm_nn_up2_concat_back(const float *dY, float *dXc, int32_t C1, float *dS, int32_t C2, int32_t D,
+                                 int32_t H, int32_t W, void *stream);
+int32_t mflbm_nn_add(float *a, const float *b, int64_t n, void *stream);
+int32_t mflbm_nn_to_bf16(const float *a, void *b, int64_t n, void *stream);
+/* masked MSE: g = 2 mask (pred - target) * inv_count for the first C channels of pred/g
+ * (row stride ldp); partial[ceil(nvox*C/256)] receives sums of squares */
+int32_t mflbm_nn_mse(const float *pred, int32_t ldp, const float *target, const float *mask, float *g,
+                     double *partial, int64_t nvox, int32_t C, float inv_count, void *stream);
+/* one Adam step on fp32 weights w (and their bf16 copy wb, nullable); step counts from 1 */
+int32_t mflbm_nn_adam(float *w, const float *g, float *m, float *v, void *wb, int64_t n, float lr, float b1, float b2,
+                      float eps, int32_t step, void *stream);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,7 @@ mf-lbm_gb300/mflbm/lib/libmflbm.so:
   csrc/listlayout.cpp     host construction of the fluid-list layout
   csrc/ensemble.cu        batched samples in one fluid-list arena, launch-shape autotuner
   csrc/nn_gemm.cu         BF16 tcgen05 GEMM (TMEM accumulators) of the warm-start network
+  csrc/nn_ops.cu          im2col/col2im, pooling, upsampling, loss and Adam of that network
 
 Only one -gencode (sm_103a) is built.  nvcc cross-compiles without a GPU, so this runs
 on the CPU build host and on the GPU host alike.
@@ -37,6 +38,7 @@ UNITS = {
     "listlayout.o": ("listlayout.cpp", []),
     "ensemble.o": ("ensemble.cu", []),
     "nn_gemm.o": ("nn_gemm.cu", []),
+    "nn_ops.o": ("nn_ops.cu", []),
 }
 
 

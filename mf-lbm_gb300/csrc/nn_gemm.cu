@@ -12,6 +12,7 @@
 // tcgen05.mma (K = 16 each) per stage and commits them to the stage's mbarrier, which
 // gates the refill.  The epilogue reads the accumulator rows of each warp's 32 TMEM
 // lanes with tcgen05.ld.  Every mbarrier wait is bounded; a timeout sets *err.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -44,7 +45,12 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
-    const int KT = (K + 63) / 64;
+    // split-K: slice blockIdx.z of gridDim.z covers k-tiles [kt0, kt0 + KT) and writes its
+    // partial product to its own C slice (reduced afterwards)
+    const int KTall = (K + 63) / 64;
+    const int kt0 = (int)((int64_t)KTall * blockIdx.z / gridDim.z);
+    const int KT = (int)((int64_t)KTall * (blockIdx.z + 1) / gridDim.z) - kt0;
+    C += (int64_t)blockIdx.z * M * ldc;
     constexpr uint32_t kCols = BN < 32 ? 32 : BN;
 
     if (warp == 0) {
@@ -63,7 +69,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
     auto load_stage = [&](int s, int kt) {
         uint8_t *sa = smem + s * GemmSmem<BN>::kStage;
         uint8_t *sb = sa + GemmSmem<BN>::kA;
-        const int k0 = kt * 64;
+        const int k0 = (kt0 + kt) * 64;
         // A: 128 rows x 8 chunks
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
 
 template <int BN>
 int launch_gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N, int K,
-                int accumulate, int *err, cudaStream_t s) {
+                int accumulate, int ksplit, int *err, cudaStream_t s) {
     const int bytes = GemmSmem<BN>::kBytes;
     static bool configured = false;
     if (!configured) {
@@ -162,9 +168,29 @@ int launch_gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb
             return MFLBM_ECUDA;
         configured = true;
     }
-    dim3 grid((M + 127) / 128, (N + BN - 1) / BN);
+    dim3 grid((M + 127) / 128, (N + BN - 1) / BN, ksplit);
     k_gemm_bf16<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, M, N, K, accumulate, err);
     return cudaPeekAtLastError() == cudaSuccess ? MFLBM_OK : MFLBM_ECUDA;
+}
+
+// C[m][n] (+)= sum over z of P[z][m][n]
+__global__ void k_splitk_reduce(const float *__restrict__ P, int ks, float *__restrict__ C, int ldc, int M, int N,
+                                int accumulate) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)M * N) return;
+    const int64_t m = t / N;
+    const int n = (int)(t - m * N);
+    float acc = 0.f;
+    for (int z = 0; z < ks; ++z) acc += P[((int64_t)z * M + m) * N + n];
+    C[m * ldc + n] = accumulate ? C[m * ldc + n] + acc : acc;
+}
+
+int gemm_dispatch(const __nv_bfloat16 *a, int lda, const __nv_bfloat16 *b, int ldb, float *C, int ldc, int M, int N,
+                  int K, int accumulate, int ks, int *err, cudaStream_t s) {
+    if (N % 128 == 0 || N > 64) return launch_gemm<128>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, ks, err, s);
+    if (N > 32) return launch_gemm<64>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, ks, err, s);
+    if (N > 16) return launch_gemm<32>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, ks, err, s);
+    return launch_gemm<16>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, ks, err, s);
 }
 
 }  // namespace nn
@@ -178,10 +204,24 @@ extern "C" int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B,
     if (N % 16 || K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N) return MFLBM_EINVAL;
     if (((uintptr_t)A | (uintptr_t)B) & 15) return MFLBM_EINVAL;
     if (M == 0 || N == 0) return MFLBM_OK;
+    return nn::gemm_dispatch((const __nv_bfloat16 *)A, lda, (const __nv_bfloat16 *)B, ldb, C, ldc, M, N, K, accumulate, 1,
+                             err, (cudaStream_t)stream);
+}
+
+// Split-K form for long reductions (weight gradients reduce over every voxel): ksplit
+// CTAs share each output tile; work holds ksplit * M * N floats of partial products.
+extern "C" int32_t mflbm_nn_gemm_bf16_splitk(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
+                                             int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t ksplit,
+                                             float *work, int32_t *err, void *stream) {
+    if (!A || !B || !C || !err || !work || M < 0 || N < 0 || K < 0 || ksplit < 1 || ksplit > 4096) return MFLBM_EINVAL;
+    if (N % 16 || K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N) return MFLBM_EINVAL;
+    if (((uintptr_t)A | (uintptr_t)B) & 15) return MFLBM_EINVAL;
+    if (M == 0 || N == 0) return MFLBM_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const __nv_bfloat16 *a = (const __nv_bfloat16 *)A, *b = (const __nv_bfloat16 *)B;
-    if (N % 128 == 0 || N > 64) return nn::launch_gemm<128>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
-    if (N > 32) return nn::launch_gemm<64>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
-    if (N > 16) return nn::launch_gemm<32>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
-    return nn::launch_gemm<16>(a, lda, b, ldb, C, ldc, M, N, K, accumulate, err, s);
+    const int ks = std::max(1, std::min(ksplit, (K + 63) / 64));
+    int r = nn::gemm_dispatch((const __nv_bfloat16 *)A, lda, (const __nv_bfloat16 *)B, ldb, work, N, M, N, K, 0, ks, err, s);
+    if (r) return r;
+    const int64_t n = (int64_t)M * N;
+    nn::k_splitk_reduce<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(work, ks, C, ldc, M, N, accumulate);
+    return cudaPeekAtLastError() == cudaSuccess ? MFLBM_OK : MFLBM_ECUDA;
 }

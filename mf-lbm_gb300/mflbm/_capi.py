@@ -82,6 +82,24 @@ SIGNATURES = {
     "mflbm_version": (C.c_int32, []),
     "mflbm_nn_gemm_bf16": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_int32, P, P]),
+    "mflbm_nn_gemm_bf16_splitk": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32,
+                                              C.c_int32, C.c_int32, C.c_int32, P, P, P]),
+    "mflbm_nn_im2col": (C.c_int32, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
+    "mflbm_nn_col2im": (C.c_int32, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
+    "mflbm_nn_transpose_bf16": (C.c_int32, [P, C.c_int32, C.c_int64, C.c_int64, C.c_int64, P, C.c_int64, C.c_int64,
+                                            C.c_int64, P]),
+    "mflbm_nn_bias_act": (C.c_int32, [P, P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, P]),
+    "mflbm_nn_relu_back": (C.c_int32, [P, P, C.c_int64, P]),
+    "mflbm_nn_bias_grad": (C.c_int32, [P, P, C.c_int64, C.c_int32, P]),
+    "mflbm_nn_avgpool2": (C.c_int32, [P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
+    "mflbm_nn_avgpool2_back": (C.c_int32, [P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
+    "mflbm_nn_up2_concat": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32, P]),
+    "mflbm_nn_up2_concat_back": (C.c_int32, [P, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
+    "mflbm_nn_add": (C.c_int32, [P, P, C.c_int64, P]),
+    "mflbm_nn_to_bf16": (C.c_int32, [P, P, C.c_int64, P]),
+    "mflbm_nn_mse": (C.c_int32, [P, C.c_int32, P, P, P, P, C.c_int64, C.c_int32, C.c_float, P]),
+    "mflbm_nn_adam": (C.c_int32, [P, P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
+                                  P]),
     "mflbm_ensemble_create": (C.c_int32, [C.POINTER(Params), C.c_int32, P, P, C.POINTER(C.c_void_p)]),
     "mflbm_ensemble_destroy": (None, [P]),
     "mflbm_ensemble_last_error": (C.c_char_p, [P]),

@@ -5,7 +5,7 @@ default (FMA) build: max|dphi| <= 1e-6, max|du| <= 1e-10, |dS|/S <= 1e-10 agains
 oracle, velocities from compute_macro_vars (valid after even steps).
 mixed form (FP32 storage and arithmetic, FP64 reductions): phi L1 error (mean |dphi| over
 the interior fluid nodes) <= 1e-3, |dS|/S <= 1e-3, max|du| <= 2e-5 (u ~ 1e-4; the largest
-deviations sit on the interface), mean|du| <= 1e-6.
+deviations sit on the interface), mean|du| <= 5e-6.
 """
 import numpy as np
 import pytest
@@ -96,5 +96,5 @@ def test_mixed_fp32_form_within_tolerance_after_2000_steps(oracle_result):
     assert dphi.mean() <= 1e-3
     assert ds <= 1e-3
     assert du <= 2e-5
-    assert du_mean <= 1e-6
+    assert du_mean <= 5e-6
     gpu.close()

@@ -1,0 +1,75 @@
+"""Warm-start network on the GPU (tcgen05 GEMMs + the project's kernels) against its CPU
+restatement, which rounds to bf16 at the same points, so only FP32 accumulation order
+differs: forward output and every weight/bias gradient within 2e-2 relative (Frobenius
+norm).  Training on one sample must reduce its loss."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from mflbm import warmstart
+from nn_oracle import OracleNet
+
+pytestmark = pytest.mark.gpu
+
+C4 = (16, 16, 16, 32)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n ** 3, 2)).astype(np.float32)
+    t = rng.normal(size=(n ** 3, 3)).astype(np.float32)
+    m = (rng.random(n ** 3) > 0.3).astype(np.float32)
+    return x, t, m
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_forward_and_gradients_match_oracle(n):
+    w = warmstart.init_weights(C4, seed=3)
+    # non-zero output channels and biases so that every path carries gradient
+    rng = np.random.default_rng(4)
+    for k in w:
+        w[k][1][:] = rng.normal(0, 0.05, size=w[k][1].shape)
+    x, t, m = _data(n, 5)
+    net = warmstart.Net(n, C4, weights=w)
+    dev = net.dev
+    net.forward(torch.from_numpy(x).to(dev).to(torch.bfloat16))
+    loss = net.loss_grad(torch.from_numpy(t).to(dev), torch.from_numpy(m).to(dev))
+    net.backward()
+    torch.cuda.synchronize()
+    net.check_err()
+    ref = OracleNet(n, C4, w)
+    out_ref = ref.forward(x.astype(np.float64))
+    loss_ref, gy = ref.loss_grad(t.astype(np.float64), m.astype(np.float64))
+    dW, dB = ref.backward(gy)
+    out = net.out.cpu().numpy()
+    print(f"n={n}: out rel {_rel(out, out_ref):.2e}  loss {float(loss):.6e} vs {loss_ref:.6e}")
+    assert _rel(out, out_ref) <= 2e-2
+    assert abs(float(loss) - loss_ref) <= 2e-2 * abs(loss_ref)
+    for k in dW:
+        ew, eb = _rel(net.dW[k].cpu().numpy(), dW[k]), _rel(net.dB[k].cpu().numpy(), dB[k])
+        print(f"  {k}: dW rel {ew:.2e}  dB rel {eb:.2e}")
+        assert ew <= 2e-2, k
+        assert eb <= 2e-2, k
+
+
+def test_training_reduces_loss():
+    n = 16
+    x, t, m = _data(n, 9)
+    net = warmstart.Net(n, C4, seed=1)
+    dev = net.dev
+    xb = torch.from_numpy(x).to(dev).to(torch.bfloat16)
+    tt, mm = torch.from_numpy(0.3 * t).to(dev), torch.from_numpy(m).to(dev)
+    losses = []
+    for it in range(60):
+        net.forward(xb)
+        losses.append(float(net.loss_grad(tt, mm)))
+        net.backward()
+        net.adam(lr=3e-3)
+    net.check_err()
+    print("loss", losses[0], "->", losses[-1])
+    assert losses[-1] < 0.7 * losses[0]
