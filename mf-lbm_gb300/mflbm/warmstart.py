@@ -7,7 +7,7 @@ im2col + BF16 GEMM on the tcgen05 tensor cores with FP32 accumulation
 (mflbm_nn_gemm_bf16); pooling, upsampling, loss and Adam are the project's own kernels.
 PyTorch only allocates the device buffers.  The LBM initialised from the prediction
 (equilibrium at rho = 1 and the predicted u) still runs to the same convergence
-criterion, so the plain method is both the fallback and the judge of the result.
+criterion, so the plain method is both the fallback and the arbiter of the result.
 
 Architecture (channels c = (c1, c2, c3, c4), grid n divisible by 8):
     e1 = conv(x, 2 -> c1)            n      p1 = pool(e1)

@@ -58,12 +58,14 @@ def test_forward_and_gradients_match_oracle(n):
 
 
 def test_training_reduces_loss():
+    # a target the network can represent: a smooth function of the second input channel
     n = 16
-    x, t, m = _data(n, 9)
+    x, _, m = _data(n, 9)
+    t = (0.5 * x[:, 1:2] * np.array([[1.0, -0.5, 0.25]])).astype(np.float32)
     net = warmstart.Net(n, C4, seed=1)
     dev = net.dev
     xb = torch.from_numpy(x).to(dev).to(torch.bfloat16)
-    tt, mm = torch.from_numpy(0.3 * t).to(dev), torch.from_numpy(m).to(dev)
+    tt, mm = torch.from_numpy(t).to(dev), torch.from_numpy(m).to(dev)
     losses = []
     for it in range(60):
         net.forward(xb)
@@ -72,4 +74,4 @@ def test_training_reduces_loss():
         net.adam(lr=3e-3)
     net.check_err()
     print("loss", losses[0], "->", losses[-1])
-    assert losses[-1] < 0.7 * losses[0]
+    assert losses[-1] < 0.2 * losses[0]
