@@ -355,6 +355,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     c->st.fold.fz = P.force_z;
     c->st.fold32 = fold_rates<float>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
     c->st.fold32.fz = (float)P.force_z;
+    c->st.unit = fold_is_unit(c->st.fold) ? 1 : 0;
     c->st.multiphase = p.multiphase;
     c->st.prec = p.precision;
     c->st.felt = (p.multiphase && p.precision == MFLBM_FP32) ? 4 : 8;

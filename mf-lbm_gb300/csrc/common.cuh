@@ -101,6 +101,13 @@ template <class R> struct MrtFold {
     R fz;                      // body force along z (singlephase)
 };
 
+// the fold's non-conserved even-order moment coefficients all vanish (s_e = s_e2 =
+// s_pi = s_nu = 1), so the collision may skip those moments
+template <class R> inline bool fold_is_unit(const MrtFold<R> &c) {
+    return c.e_m == R(0) && c.e2_m == R(0) && c.x3_m == R(0) && c.xi_m == R(0) && c.w_m == R(0) && c.wi_m == R(0) &&
+           c.o_m == R(0);
+}
+
 template <class R>
 __host__ __device__ __forceinline__ MrtFold<R> fold_rates(double s_e, double s_e2, double s_q, double s_nu, double s_pi,
                                                           double s_t) {
@@ -188,6 +195,7 @@ struct EnsArgs {
     int32_t nsteps;          // steps per persistent launch
     unsigned int *bar;       // [2] arrival count, generation
     int32_t *err;            // set when a barrier wait gives up
+    int32_t unit;            // 1: the unit-rate collision (tau = 1, MRT preset 1) applies
 };
 
 // FP16 deviation storage: value = w_q * ref + half_value * scale, ref = the rest

@@ -268,6 +268,7 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
         a.fold.fz = P.force_z;
         a.fold32 = fold_rates<float>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
         a.fold32.fz = (float)P.force_z;
+        a.unit = fold_is_unit(a.fold) ? 1 : 0;
     }
     e->block = 128;
     e->persistent = 0;

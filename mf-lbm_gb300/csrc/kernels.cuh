@@ -260,7 +260,10 @@ __device__ __forceinline__ void mrt_collide(R (&ft)[19], R den, R fx, R fy, R fz
 // FXY = false: the force has only a z component (singlephase body force).
 // OWN_DEN = true: the density is the sum of the 19 PDFs (singlephase); otherwise the
 // caller supplies it (rho1 + rho2 of the colour model).
-template <class R, bool FXY, bool OWN_DEN>
+// UNIT = true: s_e = s_e2 = s_pi = s_nu = 1 (tau = 1 with MRT preset 1), so the
+// coefficients of the non-conserved even-order moments (e_m, e2_m, x3_m, xi_m, w_m, wi_m,
+// o_m) are zero and those moments are not formed.
+template <class R, bool FXY, bool OWN_DEN, bool UNIT = false>
 __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R fy, R fz, const MrtFold<R> &c) {
     const R f0 = ft[0];
     const R p1 = ft[1] + ft[2], d1 = ft[1] - ft[2];
@@ -290,11 +293,11 @@ __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R
     const R dxy = p4 + p5, dxz = p6 + p7, dyz = p8 + p9;
     const R ds = dxy + dxz + dyz;
     const R den = OWN_DEN ? f0 + a + ds : den_in;
-    const R m_e = R(-30.0) * f0 - R(11.0) * a + R(8.0) * ds;
-    const R m_e2 = R(12.0) * f0 - R(4.0) * a + ds;
-    const R s6 = R(2.0) * p1 - p2 - p3;
-    const R s7 = dxy + dxz - R(2.0) * dyz;
-    const R s8 = p2 - p3, s9 = dxy - dxz;
+    const R m_e = UNIT ? R(0.0) : R(-30.0) * f0 - R(11.0) * a + R(8.0) * ds;
+    const R m_e2 = UNIT ? R(0.0) : R(12.0) * f0 - R(4.0) * a + ds;
+    const R s6 = UNIT ? R(0.0) : R(2.0) * p1 - p2 - p3;
+    const R s7 = UNIT ? R(0.0) : dxy + dxz - R(2.0) * dyz;
+    const R s8 = UNIT ? R(0.0) : p2 - p3, s9 = UNIT ? R(0.0) : dxy - dxz;
     // odd-order non-conserved moments from the pair differences
     const R qx = jx - R(5.0) * d1, qy = jy - R(5.0) * d2, qz = jz - R(5.0) * d3;
     const R tx = d4 - d5 - d6 + d7;
@@ -302,23 +305,24 @@ __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R
     const R tz = d6 + d7 - d8 - d9;
     // relaxed, forced and scaled moments
     const R rho_s = den * R(1.0 / 19.0);
-    const R e_s = c.e_m * m_e + c.e_den * den + c.e_u2 * u2 + c.e_f * Fu;
-    const R e2_s = c.e2_m * m_e2 + c.e2_u2 * u2 + c.e2_f * Fu;
+    const R e_s = UNIT ? c.e_den * den + c.e_u2 * u2 + c.e_f * Fu : c.e_m * m_e + c.e_den * den + c.e_u2 * u2 + c.e_f * Fu;
+    const R e2_s = UNIT ? c.e2_u2 * u2 + c.e2_f * Fu : c.e2_m * m_e2 + c.e2_u2 * u2 + c.e2_f * Fu;
     const R jx_s = R(0.1) * (FXY ? jx + fx : jx);
     const R jy_s = R(0.1) * (FXY ? jy + fy : jy);
     const R jz_s = R(0.1) * (jz + fz);
     const R qx_s = FXY ? c.q_m * qx + c.q_u * ux + c.q_f * fx : c.q_m * qx + c.q_u * ux;
     const R qy_s = FXY ? c.q_m * qy + c.q_u * uy + c.q_f * fy : c.q_m * qy + c.q_u * uy;
     const R qz_s = c.q_m * qz + c.q_u * uz + c.q_f * fz;
-    const R x3_s = c.x3_m * (s6 + s7) + c.x3_eq * (R(3.0) * uxx - u2) + c.x3_f * (R(2.0) * fux - fuy - fuz);
-    const R xi_s = c.xi_m * (R(-2.0) * s6 + s7) + c.xi_f * (R(-2.0) * fux + fuy + fuz);
-    const R w_s = c.w_m * (s8 + s9) + c.w_eq * (uyy - uzz) + c.w_f * (fuy - fuz);
-    const R wi_s = c.wi_m * (R(-2.0) * s8 + s9) + c.wi_f * (fuz - fuy);
-    const R xy_s = FXY ? c.o_m * (p4 - p5) + c.o_eq * (ux * uy) + c.o_f * (fx * uy + fy * ux) : c.o_m * (p4 - p5) + c.o_eq * (ux * uy);
-    const R yz_s = FXY ? c.o_m * (p8 - p9) + c.o_eq * (uy * uz) + c.o_f * (fy * uz + fz * uy)
-                       : c.o_m * (p8 - p9) + c.o_eq * (uy * uz) + c.o_f * (fz * uy);
-    const R zx_s = FXY ? c.o_m * (p6 - p7) + c.o_eq * (ux * uz) + c.o_f * (fx * uz + fz * ux)
-                       : c.o_m * (p6 - p7) + c.o_eq * (ux * uz) + c.o_f * (fz * ux);
+    const R x3_s = (UNIT ? R(0.0) : c.x3_m * (s6 + s7)) + c.x3_eq * (R(3.0) * uxx - u2) + c.x3_f * (R(2.0) * fux - fuy - fuz);
+    const R xi_s = (UNIT ? R(0.0) : c.xi_m * (R(-2.0) * s6 + s7)) + c.xi_f * (R(-2.0) * fux + fuy + fuz);
+    const R w_s = (UNIT ? R(0.0) : c.w_m * (s8 + s9)) + c.w_eq * (uyy - uzz) + c.w_f * (fuy - fuz);
+    const R wi_s = (UNIT ? R(0.0) : c.wi_m * (R(-2.0) * s8 + s9)) + c.wi_f * (fuz - fuy);
+    const R om_xy = UNIT ? R(0.0) : c.o_m * (p4 - p5);
+    const R om_yz = UNIT ? R(0.0) : c.o_m * (p8 - p9);
+    const R om_zx = UNIT ? R(0.0) : c.o_m * (p6 - p7);
+    const R xy_s = FXY ? om_xy + c.o_eq * (ux * uy) + c.o_f * (fx * uy + fy * ux) : om_xy + c.o_eq * (ux * uy);
+    const R yz_s = FXY ? om_yz + c.o_eq * (uy * uz) + c.o_f * (fy * uz + fz * uy) : om_yz + c.o_eq * (uy * uz) + c.o_f * (fz * uy);
+    const R zx_s = FXY ? om_zx + c.o_eq * (ux * uz) + c.o_f * (fx * uz + fz * ux) : om_zx + c.o_eq * (ux * uz) + c.o_f * (fz * ux);
     const R tx_s = c.t_m * tx, ty_s = c.t_m * ty, tz_s = c.t_m * tz;
     // back-transform
     const R sum1 = rho_s - R(11.0) * e_s - R(4.0) * e2_s;
@@ -378,7 +382,7 @@ __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R
 // odd : ft_q <- f_q(x - e_q) ... f_opp(q)(x + e_q) <- ft_q
 // even: ft_q <- f_opp(q)(x)  ... f_q(x) <- ft_q
 // ---------------------------------------------------------------------------------
-template <class S, bool ODD>
+template <class S, bool ODD, bool UNIT>
 __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
                                                  const Layout L, const StepParams P,
                                                  const MrtFold<typename Store<S>::R> cf, const float scale) {
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
     mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
 #else
     // force_z travels in the same coefficient set, already converted to R on the host
-    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+    mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
 #endif
     const R sc = R(scale);
     if (ODD) {
@@ -1382,7 +1386,7 @@ __global__ void k_convert_out(double *__restrict__ dst, const S *__restrict__ sr
 // dense kernel's (k_sp_step), so the strict flavour stays bit-identical to the oracle.
 // ---------------------------------------------------------------------------------
 // one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
-template <class S, bool ODD>
+template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                              const int64_t nf, const int64_t t, const StepParams &P,
                                              const MrtFold<typename Store<S>::R> &cf, const float scale) {
@@ -1405,7 +1409,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
                   ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
     mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
 #else
-    mrt_collide_pairs<R, false, true>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+    mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
 #endif
     const R sc = R(scale);
     if (ODD) {
@@ -1418,13 +1422,13 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
     }
 }
 
-template <class S, bool ODD>
+template <class S, bool ODD, bool UNIT>
 __global__ void __launch_bounds__(128) k_sp_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                                  const int nf, const StepParams P,
                                                  const MrtFold<typename Store<S>::R> cf, const float scale) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
-    sp_list_node<S, ODD>(A, stride, nb, nf, t, P, cf, scale);
+    sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1437,21 +1441,21 @@ template <class R> __device__ __forceinline__ const MrtFold<R> &ens_fold(const E
 template <> __device__ __forceinline__ const MrtFold<double> &ens_fold<double>(const EnsArgs &a) { return a.fold; }
 template <> __device__ __forceinline__ const MrtFold<float> &ens_fold<float>(const EnsArgs &a) { return a.fold32; }
 
-template <class S, bool ODD>
+template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void ens_sweep(const EnsArgs &a) {
     const int nt = *a.ntiles;
     for (int tile = blockIdx.x; tile < nt; tile += gridDim.x) {
         const EnsTile T = a.tiles[tile];
         if ((int)threadIdx.x < T.count)
-            sp_list_node<S, ODD>(reinterpret_cast<S *>(a.A), a.stride, a.nb, a.nf, (int64_t)T.start + threadIdx.x, a.P,
+            sp_list_node<S, ODD, UNIT>(reinterpret_cast<S *>(a.A), a.stride, a.nb, a.nf, (int64_t)T.start + threadIdx.x, a.P,
                                  ens_fold<typename Store<S>::R>(a), a.scale);
     }
 }
 
 // one step over the active tiles (grid-stride over the tile table)
-template <class S, bool ODD>
+template <class S, bool ODD, bool UNIT>
 __global__ void k_ens_step(const EnsArgs a) {
-    ens_sweep<S, ODD>(a);
+    ens_sweep<S, ODD, UNIT>(a);
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  Sense by
@@ -1490,11 +1494,11 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *bar, int32_t *err) {
 }
 
 // nsteps AA steps in one cooperative launch, a grid barrier between consecutive steps
-template <class S>
+template <class S, bool UNIT>
 __global__ void k_ens_persistent(const EnsArgs a) {
     for (int s = 0; s < a.nsteps; ++s) {
-        if (((a.ntime0 + s) & 1) != 0) ens_sweep<S, true>(a);
-        else ens_sweep<S, false>(a);
+        if (((a.ntime0 + s) & 1) != 0) ens_sweep<S, true, UNIT>(a);
+        else ens_sweep<S, false, UNIT>(a);
         if (s + 1 < a.nsteps && !grid_barrier(a.bar, a.err)) return;
     }
 }

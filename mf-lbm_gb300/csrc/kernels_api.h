@@ -48,6 +48,7 @@ struct DevState {
     const int32_t *lseg;   // [nz+1] first fluid index of every z slice
     MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
     MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
+    int unit;                // 1: fold_is_unit(fold), the collision skips the zero terms
 };
 
 struct KernelTable {

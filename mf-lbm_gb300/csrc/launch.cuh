@@ -27,10 +27,13 @@ template <class S>
 int collide_list(const DevState &st, bool odd, cudaStream_t s) {
     const unsigned nb = (unsigned)((st.nfl + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::R>(st);
-    if (odd)
-        k_sp_list<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
-    else
-        k_sp_list<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+    if (st.unit) {
+        if (odd) k_sp_list<S, true, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+        else k_sp_list<S, false, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+    } else {
+        if (odd) k_sp_list<S, true, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+        else k_sp_list<S, false, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
+    }
     return 1;
 }
 
@@ -40,10 +43,13 @@ int collide_t(const DevState &st, bool odd, cudaStream_t s) {
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::R>(st);
-    if (odd)
-        k_sp_step<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
-    else
-        k_sp_step<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
+    if (st.unit) {
+        if (odd) k_sp_step<S, true, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
+        else k_sp_step<S, false, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
+    } else {
+        if (odd) k_sp_step<S, true, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
+        else k_sp_step<S, false, false><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
+    }
     return 1;
 }
 
@@ -347,12 +353,19 @@ template <class S>
 int ens_run_t(const EnsArgs &a, int persistent, int grid, int block, cudaStream_t s) {
     if (persistent) {
         void *args[] = {const_cast<EnsArgs *>(&a)};
-        cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ens_persistent<S>, dim3(grid), dim3(block), args, 0, s);
+        const void *fn = a.unit ? (const void *)k_ens_persistent<S, true> : (const void *)k_ens_persistent<S, false>;
+        cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, s);
         return e == cudaSuccess ? 1 : -1;
     }
     for (int t = 0; t < a.nsteps; ++t) {
-        if (((a.ntime0 + t) & 1) != 0) k_ens_step<S, true><<<grid, block, 0, s>>>(a);
-        else k_ens_step<S, false><<<grid, block, 0, s>>>(a);
+        const bool odd = ((a.ntime0 + t) & 1) != 0;
+        if (a.unit) {
+            if (odd) k_ens_step<S, true, true><<<grid, block, 0, s>>>(a);
+            else k_ens_step<S, false, true><<<grid, block, 0, s>>>(a);
+        } else {
+            if (odd) k_ens_step<S, true, false><<<grid, block, 0, s>>>(a);
+            else k_ens_step<S, false, false><<<grid, block, 0, s>>>(a);
+        }
     }
     return cudaPeekAtLastError() == cudaSuccess ? a.nsteps : -1;
 }
@@ -398,9 +411,9 @@ int ens_max_grid(int prec, int block) {
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     cudaError_t e;
     switch (prec) {
-        case MFLBM_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<dfloat>, block, 0); break;
-        case MFLBM_FP16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<__half>, block, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<double>, block, 0); break;
+        case MFLBM_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<dfloat, false>, block, 0); break;
+        case MFLBM_FP16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<__half, false>, block, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<double, false>, block, 0); break;
     }
     return e == cudaSuccess ? per * nsm : 0;
 }

@@ -146,3 +146,27 @@ class OracleNet:
         ge1 = pool_back(gp1, n, c1) + gs1
         self.conv_back("e1", ge1)
         return self.dW, self.dB
+
+
+class OracleAdam:
+    """Adam (Kingma & Ba 2015) on the FP64 weights {name: [W, b]}, the update of the GPU's
+    k_adam without its bf16 weight copy."""
+
+    def __init__(self, weights, lr, b1=0.9, b2=0.999, eps=1e-8):
+        self.w = {k: [np.array(v[0], dtype=np.float64), np.array(v[1], dtype=np.float64)] for k, v in weights.items()}
+        self.m = {k: [np.zeros_like(v[0]), np.zeros_like(v[1])] for k, v in self.w.items()}
+        self.v = {k: [np.zeros_like(v[0]), np.zeros_like(v[1])] for k, v in self.w.items()}
+        self.lr, self.b1, self.b2, self.eps, self.t = lr, b1, b2, eps, 0
+
+    def step(self, dW, dB):
+        self.t += 1
+        for k in self.w:
+            for j, g in enumerate((dW[k], dB[k])):
+                self.m[k][j] = self.b1 * self.m[k][j] + (1 - self.b1) * g
+                self.v[k][j] = self.b2 * self.v[k][j] + (1 - self.b2) * g * g
+                mh = self.m[k][j] / (1 - self.b1 ** self.t)
+                vh = self.v[k][j] / (1 - self.b2 ** self.t)
+                self.w[k][j] -= self.lr * mh / (np.sqrt(vh) + self.eps)
+
+    def weights(self):
+        return {k: (v[0], v[1]) for k, v in self.w.items()}

@@ -124,3 +124,20 @@ def test_auto_falls_back_to_dense_and_list_request_rejected():
     with Solver(case["params"]) as s:
         s.set_geometry(case["walls"])
         assert s.layout == LAYOUT_DENSE
+
+
+def test_unit_rate_collision_matches_oracle():
+    # tau = 1 with MRT preset 1 takes the unit-rate collision (zero-coefficient moments skipped)
+    kw = dict(per=(1, 1, 1), spheres=3, force=1e-5, nu=1.0 / 6.0)
+    case = _case(kw, strict=0)
+    gpu = Solver(case["params"])
+    load_case(gpu, case)
+    orc = Oracle(case["params"], variant="fast")
+    load_case(orc, case)
+    gpu.run(1, 20)
+    orc.run(1, 20)
+    fl = _fluid(case)
+    a, b = _inner(gpu.download_state()["f"]), _inner(orc.download_state()["f"])
+    assert np.abs(a[:, fl] - b[:, fl]).max() <= 1e-14
+    gpu.close()
+    orc.close()
