@@ -136,6 +136,15 @@ typedef struct mflbm_ctx mflbm_ctx;
 /* Library ABI version (MFLBM_ABI_VERSION). */
 int32_t mflbm_version(void);
 
+/* Singlephase state from a velocity field (a warm start; no counterpart in the
+ * reference): u, v, w are halo-1 FP64 arrays (NULL: zero), and every fluid slot gets
+ * base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2) with base_q the reference's equilibrium
+ * weights w_q (rest_base = 0, initialization_new at rho = 1) or the rest state of the
+ * reference MRT collision, 4/21, 13/126, 1/63 (rest_base = 1); solid slots get base_q.
+ * Requires mflbm_set_geometry.  Synchronises. */
+int32_t mflbm_init_velocity(mflbm_ctx *ctx, const double *u, const double *v, const double *w,
+                            int32_t rest_base);
+
 /* Storage layout in use: MFLBM_LAYOUT_DENSE or MFLBM_LAYOUT_LIST, or
  * MFLBM_LAYOUT_AUTO while a singlephase context has no geometry yet.
  * No counterpart in the reference. */
@@ -334,6 +343,20 @@ int32_t mflbm_nn_mse(const float *pred, int32_t ldp, const float *target, const 
 /* one Adam step on fp32 weights w (and their bf16 copy wb, nullable); step counts from 1 */
 int32_t mflbm_nn_adam(float *w, const float *g, float *m, float *v, void *wb, int64_t n, float lr, float b1, float b2,
                       float eps, int32_t step, void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * geometry_preprocessing_new on the GPU (multiphase_3D/0.src/Geometry_preprocessing.F90:
+ * 9-512 for one rank): from the global wall array after channel walls (nx*ny*nz int8,
+ * Fortran order, 1 = solid) to the solid- and fluid-boundary lists of mflbm_set_geometry,
+ * in the reference's order, theta (radians, after the reference's transform) on every
+ * fluid-boundary node.  Pass NULL lists (or too small capacities) to learn the counts
+ * in *n_solid / *n_fluid (MFLBM_ERANGE when a list did not fit).  Periodic dimensions
+ * must be at least 10 cells.  Errors: mflbm_preprocess_last_error().
+ * --------------------------------------------------------------------------------- */
+int32_t mflbm_preprocess_geometry(const mflbm_params *params, const int8_t *walls, double theta,
+                                  mflbm_solid_bnd *solid, int32_t solid_cap, int32_t *n_solid,
+                                  mflbm_fluid_bnd *fluid, int32_t fluid_cap, int32_t *n_fluid);
+const char *mflbm_preprocess_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -12,6 +12,7 @@ mf-lbm_gb300/mflbm/lib/libmflbm.so:
   csrc/ensemble.cu        batched samples in one fluid-list arena, launch-shape autotuner
   csrc/nn_gemm.cu         BF16 tcgen05 GEMM (TMEM accumulators) of the warm-start network
   csrc/nn_ops.cu          im2col/col2im, pooling, upsampling, loss and Adam of that network
+  csrc/preprocess.cu      geometry_preprocessing_new on the GPU (boundary-node lists)
 
 Only one -gencode (sm_103a) is built.  nvcc cross-compiles without a GPU, so this runs
 on the CPU build host and on the GPU host alike.
@@ -39,6 +40,7 @@ UNITS = {
     "ensemble.o": ("ensemble.cu", []),
     "nn_gemm.o": ("nn_gemm.cu", []),
     "nn_ops.o": ("nn_ops.cu", []),
+    "preprocess.o": ("preprocess.cu", []),
 }
 
 

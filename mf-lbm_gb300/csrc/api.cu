@@ -666,6 +666,25 @@ int32_t mflbm_init_equilibrium(mflbm_ctx *c, const double *phi) {
     return MFLBM_OK;
 }
 
+int32_t mflbm_init_velocity(mflbm_ctx *c, const double *u, const double *v, const double *w, int32_t rest_base) {
+    int r = ready(c);
+    if (r) return r;
+    const mflbm_params &p = c->p;
+    if (p.multiphase) return fail(c, MFLBM_EINVAL, "mflbm_init_velocity is singlephase only");
+    CK(c, cudaSetDevice(c->dev));
+    const size_t b1 = sizeof(double) * n1(p);
+    double *dst[3] = {c->st.u, c->st.v, c->st.w};
+    const double *src[3] = {u, v, w};
+    for (int a = 0; a < 3; ++a) {
+        if (src[a]) CK(c, cudaMemcpyAsync(dst[a], src[a], b1, cudaMemcpyHostToDevice, c->stream));
+        else CK(c, cudaMemsetAsync(dst[a], 0, b1, c->stream));
+    }
+    c->kt->init_velocity(c->st, rest_base ? 1 : 0, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
 int32_t mflbm_step(mflbm_ctx *c, int32_t ntime) {
     int r = ready(c);
     if (r) return r;

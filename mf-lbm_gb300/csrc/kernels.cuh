@@ -36,6 +36,12 @@ __host__ __device__ constexpr double WEQ(int q) { return q == 0 ? w_equ_0 : (q <
 // keeps deviations from this state so that a fluid at rest stores zeros.
 __host__ __device__ constexpr double WREST(int q) { return q == 0 ? 4.0 / 21.0 : (q <= 6 ? 13.0 / 126.0 : 1.0 / 63.0); }
 
+// direction tables for run-time q (boundary-node lists): offsets and weight class
+// (0 rest, 1 axis, 2 diagonal); indexed 0..18
+__constant__ signed char c_ex[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+__constant__ signed char c_ey[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+__constant__ signed char c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+
 // neighbour offset of direction q in the padded PDF layout
 __device__ __forceinline__ int64_t qoff(const Layout &L, int q) {
     return (int64_t)EX(q) + (int64_t)EY(q) * L.pitch + (int64_t)EZ(q) * L.pz;
@@ -1012,11 +1018,9 @@ __global__ void k_extrap_phi(T *__restrict__ phi, const SolidBnd *__restrict__ s
     T acc = T(0.0);
     for (int n = 0; n < s.i_fluid_num; ++n) {
         const int ie = s.nbr[n];
-        int dx = 0, dy = 0, dz = 0;
-        T w = T(0.0);
-#pragma unroll
-        for (int q = 1; q < 19; ++q)
-            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = T(WEQ(q)); }
+        // ie is 1..18 (validated on upload)
+        const int dx = c_ex[ie], dy = c_ey[ie], dz = c_ez[ie];
+        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
         acc = acc + phi[L.i4(s.ix + dx, s.iy + dy, s.iz + dz)] * w;
     }
     phi[L.i4(s.ix, s.iy, s.iz)] = acc / T(s.la_weight);
@@ -1101,11 +1105,9 @@ __global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__
     T ax = T(0.0), ay = T(0.0), az = T(0.0);
     for (int n = 0; n < s.i_fluid_num; ++n) {
         const int ie = s.nbr[n];
-        int dx = 0, dy = 0, dz = 0;
-        T w = T(0.0);
-#pragma unroll
-        for (int q = 1; q < 19; ++q)
-            if (q == ie) { dx = EX(q); dy = EY(q); dz = EZ(q); w = T(WEQ(q)); }
+        // ie is 1..18 (validated on upload)
+        const int dx = c_ex[ie], dy = c_ey[ie], dz = c_ez[ie];
+        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
         const int64_t nb = L.i2(s.ix + dx, s.iy + dy, s.iz + dz);
         ax = ax + cnx[nb] * w;
         ay = ay + cny[nb] * w;
@@ -1630,6 +1632,54 @@ __global__ void __launch_bounds__(MON_THREADS) k_list_monitor(const S *__restric
         out[(int64_t)6 * nseg + b] = r;
         out[(int64_t)7 * nseg + b] = m;
     }
+}
+
+// ---------------------------------------------------------------------------------
+// Singlephase state from a velocity field (warm start): in every fluid slot
+//   f_q = base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2),   u from the halo-1 arrays u, v, w
+// with base_q = w_q (the reference's equilibrium at rho = 1) or the MRT rest state
+// W_q (rest_base = 1); solid slots get base_q.  Dense layout: every cell of the halo-1 box
+// (ghost velocities are whatever the arrays hold); fluid list: fluid slots from their
+// cell, link slots base_q.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double feq_vel(int q, double ux, double uy, double uz, int rest_base) {
+    const double wq = WEQ(q);
+    const double cu = (double)c_ex[q] * ux + (double)c_ey[q] * uy + (double)c_ez[q] * uz;
+    const double usq = ux * ux + uy * uy + uz * uz;
+    const double base = rest_base ? WREST(q) : wq;
+    return base + wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+}
+
+template <class S>
+__global__ void k_init_vel_dense(S *__restrict__ f, const double *__restrict__ u, const double *__restrict__ v,
+                                 const double *__restrict__ w, const int8_t *__restrict__ walls, const Layout L,
+                                 int rest_base, float scale) {
+    using St = Store<S>;
+    const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb) return;
+    const int i = (int)(t % (L.nx + 2));
+    const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
+    const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    const bool solid = walls[L.i2(i, j, k)] != 0;
+    const double ux = solid ? 0.0 : u[t], uy = solid ? 0.0 : v[t], uz = solid ? 0.0 : w[t];
+    const int64_t c = L.cell(i, j, k);
+    for (int q = 0; q < 19; ++q) St::st64(f, (int64_t)q * L.qs + c, feq_vel(q, ux, uy, uz, rest_base), WREST(q), scale);
+}
+
+template <class S>
+__global__ void k_init_vel_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ cell1, const int nf,
+                                const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ w,
+                                int rest_base, float scale) {
+    using St = Store<S>;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= stride) return;
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    if (t < nf) {
+        const int32_t c = cell1[t];
+        ux = u[c]; uy = v[c]; uz = w[c];
+    }
+    for (int q = 0; q < 19; ++q) St::st64(A, (int64_t)q * stride + t, feq_vel(q, ux, uy, uz, rest_base), WREST(q), scale);
 }
 
 // FP64 host image <-> field array of type T (phi, gradient fields of the mixed form)

@@ -85,6 +85,8 @@ struct KernelTable {
     int (*ens_init)(const EnsArgs &a, int prec, cudaStream_t);
     // largest co-resident grid of the persistent kernel for this block size
     int (*ens_max_grid)(int prec, int block);
+    // singlephase state from the velocity field in st.u, st.v, st.w (halo 1)
+    int (*init_velocity)(const DevState &, int rest_base, cudaStream_t);
 };
 
 const KernelTable *kernels_fast();

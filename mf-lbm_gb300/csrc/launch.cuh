@@ -418,9 +418,31 @@ int ens_max_grid(int prec, int block) {
     return e == cudaSuccess ? per * nsm : 0;
 }
 
+template <class S>
+int init_velocity_t(const DevState &st, int rest_base, cudaStream_t s) {
+    if (st.list) {
+        k_init_vel_list<S><<<(unsigned)((st.lstride + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.cell1, st.nfl,
+                                                                                 st.u, st.v, st.w, rest_base, st.scale);
+    } else {
+        const Layout &L = st.L;
+        const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        k_init_vel_dense<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), st.u, st.v, st.w, st.walls, L,
+                                                                         rest_base, st.scale);
+    }
+    return 1;
+}
+
+int init_velocity(const DevState &st, int rest_base, cudaStream_t s) {
+    switch (st.prec) {
+        case MFLBM_FP32: return init_velocity_t<dfloat>(st, rest_base, s);
+        case MFLBM_FP16: return init_velocity_t<__half>(st, rest_base, s);
+        default: return init_velocity_t<double>(st, rest_base, s);
+    }
+}
+
 const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,
                            init_equilibrium, convert_in,  convert_out, field_in,      field_out,
-                           ens_run,          ens_monitor, ens_init,   ens_max_grid};
+                           ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity};
 
 }  // namespace MFLBM_NS
 }  // namespace mflbm

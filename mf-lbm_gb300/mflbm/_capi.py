@@ -80,6 +80,8 @@ PP = C.POINTER(C.c_void_p)
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "mflbm_version": (C.c_int32, []),
+    "mflbm_preprocess_geometry": (C.c_int32, [C.POINTER(Params), P, C.c_double, P, C.c_int32, P, P, C.c_int32, P]),
+    "mflbm_preprocess_last_error": (C.c_char_p, []),
     "mflbm_nn_gemm_bf16": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_int32, P, P]),
     "mflbm_nn_gemm_bf16_splitk": (C.c_int32, [P, C.c_int32, P, C.c_int32, P, C.c_int32, C.c_int32, C.c_int32,
@@ -111,6 +113,7 @@ SIGNATURES = {
     "mflbm_ensemble_tune": (C.c_int32, [P, C.c_int32, P, C.c_int32]),
     "mflbm_ensemble_info": (C.c_int32, [P, P, P, P, P]),
     "mflbm_layout": (C.c_int32, [P]),
+    "mflbm_init_velocity": (C.c_int32, [P, P, P, P, C.c_int32]),
     "mflbm_create": (C.c_int32, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "mflbm_destroy": (None, [P]),
     "mflbm_last_error": (C.c_char_p, [P]),

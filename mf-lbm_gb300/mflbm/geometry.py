@@ -240,6 +240,28 @@ def preprocess(p, walls_channel, theta_rad):
     return solid, fluid
 
 
+def preprocess_gpu(p, walls_channel, theta_rad, lib=None):
+    """preprocess() on the GPU through mflbm_preprocess_geometry: the same lists, bit for
+    bit, in a fraction of the time for large grids (periodic dimensions >= 10)."""
+    import ctypes as C
+    from . import _capi
+    lib = lib or _capi.load()
+    w = np.ascontiguousarray(walls_channel, dtype=np.int8)
+    assert w.shape == (p.nz, p.ny, p.nx)
+    ns, nf = C.c_int32(), C.c_int32()
+    rc = lib.mflbm_preprocess_geometry(C.byref(p), w.ctypes.data, float(theta_rad), None, 0, C.byref(ns), None, 0,
+                                       C.byref(nf))
+    if rc and rc != _capi.MFLBM_ERANGE:
+        raise _capi.MflbmError(rc, lib.mflbm_preprocess_last_error().decode())
+    solid = np.zeros(ns.value, dtype=SOLID_DTYPE)
+    fluid = np.zeros(nf.value, dtype=FLUID_DTYPE)
+    rc = lib.mflbm_preprocess_geometry(C.byref(p), w.ctypes.data, float(theta_rad), solid.ctypes.data, solid.size,
+                                       C.byref(ns), fluid.ctypes.data, fluid.size, C.byref(nf))
+    if rc:
+        raise _capi.MflbmError(rc, lib.mflbm_preprocess_last_error().decode())
+    return solid, fluid
+
+
 def contact_angle_rad(theta_deg):
     """theta transform of read_parameter_multi (IO_multiphase.F90:467-468)."""
     theta = 180.0 - theta_deg

@@ -94,6 +94,21 @@ class Solver:
             assert phi.shape == self.shape4()
         self._check(self.lib.mflbm_init_equilibrium(self.ctx, _ptr(phi)))
 
+    def init_velocity(self, u=None, v=None, w=None, rest_base=True):
+        """State from a velocity field: interior arrays (nz, ny, nx) or halo-1 arrays; the
+        ghost layer of interior arrays is filled periodically."""
+        arrs = []
+        for a in (u, v, w):
+            if a is None:
+                arrs.append(None)
+                continue
+            a = np.asarray(a, dtype=np.float64)
+            if a.shape == (self.nz, self.ny, self.nx):
+                a = np.pad(a, 1, mode="wrap")
+            assert a.shape == self.shape1()
+            arrs.append(np.ascontiguousarray(a))
+        self._check(self.lib.mflbm_init_velocity(self.ctx, *[_ptr(a) for a in arrs], int(bool(rest_base))))
+
     def upload_state(self, f, g=None, phi=None, f_convec=None, g_convec=None, phi_convec=None):
         fp, f = _ptr_array(f)
         gp, g = _ptr_array(g)

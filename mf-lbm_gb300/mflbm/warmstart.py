@@ -323,10 +323,17 @@ def make_samples(n, count, seed, por_lo=0.15, por_hi=0.35, workers=0):
     return [_make_sample(j) for j in jobs]
 
 
-def solve(wg, precision=1, tol=1e-7, init_u=None, max_steps=400000, nu=1.0 / 6.0, fz=1e-6, device=0):
+def solve(wg, precision=1, tol=1e-7, init_u=None, rest_base=False, max_steps=400000, nu=1.0 / 6.0, fz=1e-6,
+          device=0):
     """Steady singlephase run of one periodic sample (fluid-list layout); returns the
-    SteadyResult and the solver's macro fields.  init_u = (u, v, w) starts from the
-    equilibrium at that velocity instead of rest."""
+    SteadyResult, the solver's macro fields and the set-up time.
+
+    Without init_u and rest_base the run starts as the reference does (equilibrium at
+    rest with the BGK weights).  rest_base starts from the rest state of the reference's
+    MRT collision instead; init_u = (u, v, w) (interior arrays, the steady velocity as
+    compute_macro_vars reports it) adds the equilibrium velocity terms, with F_z/2 added to
+    w in the fluid because the stored post-collision momentum leads the reported velocity
+    by half the body force."""
     import time as _t
     from . import geometry
     from .permeability import run_to_steady
@@ -338,10 +345,13 @@ def solve(wg, precision=1, tol=1e-7, init_u=None, max_steps=400000, nu=1.0 / 6.0
     with Solver(p) as sim:
         sim.set_geometry(walls)
         t0 = _t.perf_counter()
-        if init_u is None:
+        if init_u is None and not rest_base:
             sim.init_equilibrium()
+        elif init_u is None:
+            sim.init_velocity(None, None, None, rest_base=True)
         else:
-            sim.upload_state(equilibrium_state(*init_u, n, n, n))
+            fluid = (wg == 0)
+            sim.init_velocity(init_u[0], init_u[1], init_u[2] + 0.5 * fz * fluid, rest_base=True)
         setup = _t.perf_counter() - t0
         r = run_to_steady(sim, p, check_every=100, tol=tol, max_steps=max_steps)
         mac = sim.macro()

@@ -94,3 +94,47 @@ def test_training_follows_oracle_and_fits_a_constant_field():
     net2.check_err()
     print("constant target loss", losses[0], "->", losses[-1])
     assert losses[-1] < 0.2 * losses[0]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_restart_from_converged_velocity_converges_at_once(precision):
+    """A run started from the equilibrium at the converged velocity of a previous run
+    needs a small fraction of the steps from rest and reproduces k (the upload path of the
+    warm start reaches the sweep)."""
+    from mflbm import geometry
+    wg = geometry.sphere_packing((48, 48, 48), 0.3, mean_r=8.0, sd_r=2.0, seed=5)
+    r0, mac, _ = warmstart.solve(wg, precision=precision, tol=1e-7)
+    u = [mac[k][1:-1, 1:-1, 1:-1] for k in ("u", "v", "w")]
+    r1, _, _ = warmstart.solve(wg, precision=precision, tol=1e-7, init_u=u)
+    print(f"precision {precision}: from rest {r0.steps} steps, restarted {r1.steps} steps, "
+          f"k {r0.k:.8e} / {r1.k:.8e}")
+    assert r1.converged
+    assert r1.steps < r0.steps
+    assert abs(r1.k - r0.k) / r0.k <= 1e-3
+
+
+def test_init_velocity_matches_equilibrium_formula():
+    from mflbm import Solver, geometry
+    from mflbm.solver import make_params
+    n = 20
+    wg = geometry.sphere_packing((n, n, n), 0.35, mean_r=4.0, sd_r=1.0, seed=2)
+    rng = np.random.default_rng(3)
+    u = [1e-3 * rng.normal(size=(n, n, n)) for _ in range(3)]
+    ex = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+    ey = np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1])
+    ez = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1])
+    wq = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    wr = np.array([4 / 21] + [13 / 126] * 6 + [1 / 63] * 12)
+    for layout in (1, 2):
+        p = make_params(multiphase=0, nx=n, ny=n, nz=n, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
+                        wall_y_min=0, wall_y_max=0, mrt=1, la_nu1=1 / 6, force_z=1e-6, layout=layout)
+        walls, _, _ = geometry.set_walls(p, wg)
+        with Solver(p) as sim:
+            sim.set_geometry(walls)
+            sim.init_velocity(*u, rest_base=True)
+            f = sim.download_state()["f"][:, 1:-1, 1:-1, 1:-1]
+        fl = wg == 0
+        cu = ex[:, None] * u[0][fl] + ey[:, None] * u[1][fl] + ez[:, None] * u[2][fl]
+        usq = u[0][fl] ** 2 + u[1][fl] ** 2 + u[2][fl] ** 2
+        ref = wr[:, None] + wq[:, None] * (3 * cu + 4.5 * cu * cu - 1.5 * usq)
+        assert np.abs(f[:, fl] - ref).max() <= 1e-16, layout
