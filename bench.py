@@ -301,8 +301,9 @@ def warmstart_study(args):
     deviation form to |du|/u < 1e-6), then on held-out samples compare runs to 1e-7 from
     rest and from the prediction (FP64 and FP32), wall time including inference.  "rest"
     is the reference's start (equilibrium at rest, BGK weights); the warm start places the
-    predicted velocity on the rest state of the MRT collision, and the "mrt_rest" rows
-    (that rest state without the prediction) separate the two contributions."""
+    predicted velocity and density on the rest state of the MRT collision with consistent
+    bounce-back slots, and the "mrt_rest" rows (that rest state at the sample's mean
+    density, no prediction) separate the two contributions."""
     from mflbm import warmstart as ws
     n = args.n5
     t0 = time.perf_counter()
@@ -320,7 +321,7 @@ def warmstart_study(args):
         r, mac, _ = ws.solve(wg, precision=1, tol=1e-6, nu=nu, fz=fz)
         data_lu += int((wg == 0).sum()) * r.steps
         xs.append(torch.from_numpy(x).cuda().to(torch.bfloat16))
-        ys.append(torch.from_numpy(ws.target_from_macro(mac, nu, fz)).cuda())
+        ys.append(torch.from_numpy(ws.target_from_macro(mac, nu, fz, ws.mean_density(wg))).cuda())
         ms.append(torch.from_numpy((wg == 0).reshape(-1).astype(np.float32)).cuda())
     data_s = time.perf_counter() - t0
     net = ws.Net(n, seed=7)
@@ -338,9 +339,10 @@ def warmstart_study(args):
         net.forward(torch.from_numpy(x).cuda().to(torch.bfloat16))
         out = net.out.cpu().numpy()
         u = ws.velocity_from_output(out, n, nu, fz, wg)
+        rho = ws.density_from_output(out, n, wg, ws.mean_density(wg))
         infer = time.perf_counter() - t1
-        w64, _, set64 = ws.solve(wg, precision=0, tol=args.conv_tol, init_u=u, nu=nu, fz=fz)
-        w32, _, set32 = ws.solve(wg, precision=1, tol=args.conv_tol, init_u=u, nu=nu, fz=fz)
+        w64, _, set64 = ws.solve(wg, precision=0, tol=args.conv_tol, init_u=u, init_rho=rho, nu=nu, fz=fz)
+        w32, _, set32 = ws.solve(wg, precision=1, tol=args.conv_tol, init_u=u, init_rho=rho, nu=nu, fz=fz)
         # ablation: the MRT rest state without the predicted velocity
         b32, _, setb = ws.solve(wg, precision=1, tol=args.conv_tol, rest_base=True, nu=nu, fz=fz)
         k0 = nu * float(np.mean(u[2])) / fz
@@ -385,7 +387,7 @@ def drainage_study(args):
     from mflbm import Solver, workloads
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, precision=0)
+    case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, precision=0, gpu_preprocess=True)
     gen_s = time.perf_counter() - t0
     res = {}
     every = 500

@@ -136,14 +136,15 @@ typedef struct mflbm_ctx mflbm_ctx;
 /* Library ABI version (MFLBM_ABI_VERSION). */
 int32_t mflbm_version(void);
 
-/* Singlephase state from a velocity field (a warm start; no counterpart in the
- * reference): u, v, w are halo-1 FP64 arrays (NULL: zero), and every fluid slot gets
- * base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2) with base_q the reference's equilibrium
- * weights w_q (rest_base = 0, initialization_new at rho = 1) or the rest state of the
- * reference MRT collision, 4/21, 13/126, 1/63 (rest_base = 1); solid slots get base_q.
- * Requires mflbm_set_geometry.  Synchronises. */
-int32_t mflbm_init_velocity(mflbm_ctx *ctx, const double *u, const double *v, const double *w,
-                            int32_t rest_base);
+/* Singlephase state from density and velocity fields (a warm start; no counterpart in
+ * the reference): rho, u, v, w are halo-1 FP64 arrays (rho NULL: 1, velocity NULL: 0).
+ * Every fluid slot gets rho (base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2)) with base_q the
+ * reference's equilibrium weights w_q (rest_base = 0, initialization_new) or the rest
+ * state of the reference MRT collision, 4/21, 13/126, 1/63 (rest_base = 1).  A solid slot
+ * that a fluid neighbour pushes into (bounce-back link) gets that neighbour's population
+ * toward it; other solid slots get base_q.  Requires mflbm_set_geometry.  Synchronises. */
+int32_t mflbm_init_velocity(mflbm_ctx *ctx, const double *rho, const double *u, const double *v,
+                            const double *w, int32_t rest_base);
 
 /* Storage layout in use: MFLBM_LAYOUT_DENSE or MFLBM_LAYOUT_LIST, or
  * MFLBM_LAYOUT_AUTO while a singlephase context has no geometry yet.
@@ -220,6 +221,16 @@ int32_t mflbm_macro(mflbm_ctx *ctx, double *u, double *v, double *w, double *rho
  * *status = MFLBM_FAILED when a sum is NaN or sqrt(umax^2) > 0.5, else MFLBM_RUNNING.
  * Sums accumulate in FP64 in every precision mode. */
 int32_t mflbm_monitor(mflbm_ctx *ctx, double *profiles, double *scalars, int32_t *status);
+
+/* The other monitors of the multiphase loop (Main_multiphase.F90:184-195):
+ * kind 0: phi_old <- phi, the set-up of steady_state_option 2 (Init_multiphase.F90:340-351);
+ * kind 1: monitor_multiphase_steady_capillarypressure (Monitor.F90:370-462),
+ *         out[6] = pc, pre_w, pre_nw, umax, count_w, count_nw;
+ * kind 2: monitor_multiphase_steady_phasefield (:287-365), out[2] = max |phi - phi_old| over
+ *         the fluid nodes, umax; then phi_old <- phi;
+ * kind 3: monitor_breakthrough (:472-507), out[1] = fluid nodes with phi > 0 at z = nz - 1.
+ * Kinds 1 and 2 run compute_macro_vars first.  FP64 sums in every precision. */
+int32_t mflbm_steady_monitor(mflbm_ctx *ctx, int32_t kind, double *out);
 
 /* cal_saturation (multiphase_3D/0.src/Monitor.F90:512-550): vol1, vol2 sums. */
 int32_t mflbm_saturation(mflbm_ctx *ctx, double *vol1, double *vol2);

@@ -36,6 +36,8 @@ struct mflbm_ctx {
     void *pdf = nullptr;          // PDF storage (dense planes or fluid-list arrays)
     size_t pdf_bytes = 0;
     std::vector<void *> list_bufs;  // neighbour table, cell map, link table, slice starts
+    void *phi_old = nullptr;        // steady_state_option 2 (allocated on first use)
+    double *steady_part = nullptr;  // 7 * nz partials
     // graphs of whole even+odd step pairs
     cudaGraphExec_t g_pair = nullptr, g_block = nullptr;
     int block_pairs = 8;
@@ -666,22 +668,75 @@ int32_t mflbm_init_equilibrium(mflbm_ctx *c, const double *phi) {
     return MFLBM_OK;
 }
 
-int32_t mflbm_init_velocity(mflbm_ctx *c, const double *u, const double *v, const double *w, int32_t rest_base) {
+int32_t mflbm_init_velocity(mflbm_ctx *c, const double *rho, const double *u, const double *v, const double *w,
+                            int32_t rest_base) {
     int r = ready(c);
     if (r) return r;
     const mflbm_params &p = c->p;
     if (p.multiphase) return fail(c, MFLBM_EINVAL, "mflbm_init_velocity is singlephase only");
     CK(c, cudaSetDevice(c->dev));
     const size_t b1 = sizeof(double) * n1(p);
-    double *dst[3] = {c->st.u, c->st.v, c->st.w};
-    const double *src[3] = {u, v, w};
-    for (int a = 0; a < 3; ++a) {
+    double *dst[4] = {c->st.u, c->st.v, c->st.w, c->st.rho};
+    const double *src[4] = {u, v, w, rho};
+    for (int a = 0; a < 4; ++a) {
         if (src[a]) CK(c, cudaMemcpyAsync(dst[a], src[a], b1, cudaMemcpyHostToDevice, c->stream));
-        else CK(c, cudaMemsetAsync(dst[a], 0, b1, c->stream));
+        else if (a < 3) CK(c, cudaMemsetAsync(dst[a], 0, b1, c->stream));
     }
-    c->kt->init_velocity(c->st, rest_base ? 1 : 0, c->stream);
+    c->kt->init_velocity(c->st, rho ? c->st.rho : nullptr, rest_base ? 1 : 0, c->stream);
     CK(c, cudaPeekAtLastError());
     CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
+int32_t mflbm_steady_monitor(mflbm_ctx *c, int32_t kind, double *out) {
+    int r = ready(c);
+    if (r) return r;
+    const mflbm_params &p = c->p;
+    if (!p.multiphase) return fail(c, MFLBM_EINVAL, "steady-state monitors are multiphase");
+    if (kind < 0 || kind > 3 || (kind > 0 && !out)) return fail(c, MFLBM_EINVAL, "kind must be 0..3 and out non-NULL");
+    CK(c, cudaSetDevice(c->dev));
+    if (!c->steady_part && (r = dalloc(c, &c->steady_part, 7 * (int64_t)p.nz))) return r;
+    if ((kind == 0 || kind == 2) && !c->phi_old) {
+        if ((r = dalloc_bytes(c, &c->phi_old, (size_t)c->st.felt * n4(p)))) return r;
+        CK(c, cudaMemcpyAsync(c->phi_old, c->st.phi, (size_t)c->st.felt * n4(p), cudaMemcpyDeviceToDevice, c->stream));
+        if (kind == 0) return MFLBM_OK;
+    }
+    if (kind == 0) {
+        CK(c, cudaMemcpyAsync(c->phi_old, c->st.phi, (size_t)c->st.felt * n4(p), cudaMemcpyDeviceToDevice, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        return MFLBM_OK;
+    }
+    c->kt->monitor(c->st, c->stream);   // compute_macro_vars
+    c->kt->steady(c->st, kind == 2 ? c->phi_old : nullptr, c->steady_part, p.nz - 1, kind == 2 ? 1 : 0, c->stream);
+    CK(c, cudaPeekAtLastError());
+    std::vector<double> h((size_t)7 * p.nz);
+    CK(c, cudaMemcpyAsync(h.data(), c->steady_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    double dphi = 0.0, umax2 = 0.0, pw = 0.0, iw = 0.0, pnw = 0.0, inw = 0.0, brk = 0.0;
+    for (int k = 0; k < p.nz; ++k) {
+        dphi = std::max(dphi, h[k]);
+        umax2 = std::max(umax2, h[(size_t)p.nz + k]);
+        pw += h[(size_t)2 * p.nz + k];
+        iw += h[(size_t)3 * p.nz + k];
+        pnw += h[(size_t)4 * p.nz + k];
+        inw += h[(size_t)5 * p.nz + k];
+        brk += h[(size_t)6 * p.nz + k];
+    }
+    const double eps = 1.110223025e-16;   // Module.F90:8
+    if (kind == 1) {
+        const double pre_w = pw / (iw + eps), pre_nw = pnw / (inw + eps);
+        out[0] = (pre_nw - pre_w) / 3.0;
+        out[1] = pre_w;
+        out[2] = pre_nw;
+        out[3] = std::sqrt(umax2);
+        out[4] = iw;
+        out[5] = inw;
+    } else if (kind == 2) {
+        out[0] = dphi;
+        out[1] = std::sqrt(umax2);
+    } else {
+        out[0] = brk;
+    }
     return MFLBM_OK;
 }
 

@@ -41,6 +41,8 @@ __host__ __device__ constexpr double WREST(int q) { return q == 0 ? 4.0 / 21.0 :
 __constant__ signed char c_ex[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
 __constant__ signed char c_ey[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
 __constant__ signed char c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+__constant__ signed char c_opp[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+__device__ __forceinline__ int OPP_RT(int q) { return c_opp[q]; }
 
 // neighbour offset of direction q in the padded PDF layout
 __device__ __forceinline__ int64_t qoff(const Layout &L, int q) {
@@ -1635,25 +1637,26 @@ __global__ void __launch_bounds__(MON_THREADS) k_list_monitor(const S *__restric
 }
 
 // ---------------------------------------------------------------------------------
-// Singlephase state from a velocity field (warm start): in every fluid slot
-//   f_q = base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2),   u from the halo-1 arrays u, v, w
-// with base_q = w_q (the reference's equilibrium at rho = 1) or the MRT rest state
-// W_q (rest_base = 1); solid slots get base_q.  Dense layout: every cell of the halo-1 box
-// (ghost velocities are whatever the arrays hold); fluid list: fluid slots from their
-// cell, link slots base_q.
+// Singlephase state from density and velocity fields (warm start): every fluid slot gets
+//   f_q = rho (base_q + w_q (3 e.u + 4.5 (e.u)^2 - 1.5 u^2))
+// with base_q = w_q (the reference's equilibrium) or the MRT rest state W_q
+// (rest_base = 1), rho and u from the halo-1 arrays (rho NULL: 1).  A solid slot that a
+// fluid node pushes into (bounce-back link: slot q of solid s, pushed by the fluid node
+// s + e_q in direction opp(q)) gets that node's f_opp(q), the value it holds in a settled
+// flow; every other solid slot gets base_q.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ double feq_vel(int q, double ux, double uy, double uz, int rest_base) {
+__device__ __forceinline__ double feq_vel(int q, double rho, double ux, double uy, double uz, int rest_base) {
     const double wq = WEQ(q);
     const double cu = (double)c_ex[q] * ux + (double)c_ey[q] * uy + (double)c_ez[q] * uz;
     const double usq = ux * ux + uy * uy + uz * uz;
     const double base = rest_base ? WREST(q) : wq;
-    return base + wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+    return rho * (base + wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq));
 }
 
 template <class S>
-__global__ void k_init_vel_dense(S *__restrict__ f, const double *__restrict__ u, const double *__restrict__ v,
-                                 const double *__restrict__ w, const int8_t *__restrict__ walls, const Layout L,
-                                 int rest_base, float scale) {
+__global__ void k_init_vel_dense(S *__restrict__ f, const double *__restrict__ rho, const double *__restrict__ u,
+                                 const double *__restrict__ v, const double *__restrict__ w,
+                                 const int8_t *__restrict__ walls, const Layout L, int rest_base, float scale) {
     using St = Store<S>;
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1661,25 +1664,121 @@ __global__ void k_init_vel_dense(S *__restrict__ f, const double *__restrict__ u
     const int i = (int)(t % (L.nx + 2));
     const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
     const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
-    const bool solid = walls[L.i2(i, j, k)] != 0;
-    const double ux = solid ? 0.0 : u[t], uy = solid ? 0.0 : v[t], uz = solid ? 0.0 : w[t];
     const int64_t c = L.cell(i, j, k);
-    for (int q = 0; q < 19; ++q) St::st64(f, (int64_t)q * L.qs + c, feq_vel(q, ux, uy, uz, rest_base), WREST(q), scale);
+    if (walls[L.i2(i, j, k)] == 0) {
+        const double r = rho ? rho[t] : 1.0;
+        for (int q = 0; q < 19; ++q)
+            St::st64(f, (int64_t)q * L.qs + c, feq_vel(q, r, u[t], v[t], w[t], rest_base), WREST(q), scale);
+        return;
+    }
+    for (int q = 0; q < 19; ++q) {
+        double val = rest_base ? WREST(q) : WEQ(q);
+        const int ni = i + c_ex[q], nj = j + c_ey[q], nk = k + c_ez[q];
+        if (q > 0 && ni >= 0 && ni <= L.nx + 1 && nj >= 0 && nj <= L.ny + 1 && nk >= 0 && nk <= L.nz + 1 &&
+            walls[L.i2(ni, nj, nk)] == 0) {
+            const int64_t m = L.i1(ni, nj, nk);
+            val = feq_vel(OPP_RT(q), rho ? rho[m] : 1.0, u[m], v[m], w[m], rest_base);
+        }
+        St::st64(f, (int64_t)q * L.qs + c, val, WREST(q), scale);
+    }
 }
 
+// list layout, pass 1: every slot of every direction array (fluid nodes from their cell,
+// links and padding base_q)
 template <class S>
 __global__ void k_init_vel_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ cell1, const int nf,
-                                const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ w,
-                                int rest_base, float scale) {
+                                const double *__restrict__ rho, const double *__restrict__ u,
+                                const double *__restrict__ v, const double *__restrict__ w, int rest_base, float scale) {
     using St = Store<S>;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= stride) return;
-    double ux = 0.0, uy = 0.0, uz = 0.0;
+    double r = 1.0, ux = 0.0, uy = 0.0, uz = 0.0;
     if (t < nf) {
         const int32_t c = cell1[t];
+        r = rho ? rho[c] : 1.0;
         ux = u[c]; uy = v[c]; uz = w[c];
+        for (int q = 0; q < 19; ++q) St::st64(A, (int64_t)q * stride + t, feq_vel(q, r, ux, uy, uz, rest_base), WREST(q), scale);
+    } else {
+        for (int q = 0; q < 19; ++q) St::st64(A, (int64_t)q * stride + t, rest_base ? WREST(q) : WEQ(q), WREST(q), scale);
     }
-    for (int q = 0; q < 19; ++q) St::st64(A, (int64_t)q * stride + t, feq_vel(q, ux, uy, uz, rest_base), WREST(q), scale);
+}
+
+// list layout, pass 2: the link slots a fluid node pushes into (nb[d][x] >= nf holds
+// that node's f_d in array opp(d))
+template <class S>
+__global__ void k_init_vel_links(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
+                                 const int32_t *__restrict__ cell1, const int nf, const double *__restrict__ rho,
+                                 const double *__restrict__ u, const double *__restrict__ v,
+                                 const double *__restrict__ w, int rest_base, float scale) {
+    using St = Store<S>;
+    const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nf) return;
+    const int32_t c = cell1[x];
+    const double r = rho ? rho[c] : 1.0;
+    for (int d = 1; d < 19; ++d) {
+        const int32_t slot = nb[(int64_t)(d - 1) * nf + x];
+        if (slot >= nf)
+            St::st64(A, (int64_t)OPP_RT(d) * stride + slot, feq_vel(d, r, u[c], v[c], w[c], rest_base), WREST(d), scale);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Steady-state and breakthrough monitors of the multiphase model
+// (multiphase_3D/0.src/Monitor.F90:287-507); one block per z slice, partials
+// out[m * nz + k - 1]: m = 0 max |phi - phi_old|, 1 max |u|^2, 2 sum rho (phi < -0.99),
+// 3 count (phi < -0.99), 4 sum rho (phi > 0.99), 5 count (phi > 0.99), 6 count of fluid
+// nodes with phi > 0 (only slice obs_z).  Fluid nodes only; u, v, w, rho from
+// compute_macro_vars.  copy_old: phi_old <- phi afterwards (interior).
+// ---------------------------------------------------------------------------------
+constexpr int STEADY_NQ = 7;
+
+template <class T>
+__global__ void __launch_bounds__(MON_THREADS) k_steady(const T *__restrict__ phi, T *__restrict__ phi_old,
+                                                        const double *__restrict__ rho, const double *__restrict__ u,
+                                                        const double *__restrict__ v, const double *__restrict__ w,
+                                                        const int8_t *__restrict__ walls, double *__restrict__ out,
+                                                        const Layout L, int obs_z, int copy_old) {
+    const int k = blockIdx.x + 1;
+    const int64_t n = (int64_t)L.nx * L.ny;
+    double acc[STEADY_NQ];
+#pragma unroll
+    for (int m = 0; m < STEADY_NQ; ++m) acc[m] = 0.0;
+    for (int64_t t = threadIdx.x; t < n; t += MON_THREADS) {
+        const int i = (int)(t % L.nx) + 1, j = (int)(t / L.nx) + 1;
+        const int wi = walls[L.i2(i, j, k)];
+        const int64_t i4 = L.i4(i, j, k), i1 = L.i1(i, j, k);
+        const double ph = (double)phi[i4];
+        if (wi == 0) {
+            if (phi_old) {
+                const double d = fabs(ph - (double)phi_old[i4]);
+                acc[0] = acc[0] < d ? d : acc[0];
+            }
+            const double uu = u[i1] * u[i1] + v[i1] * v[i1] + w[i1] * w[i1];
+            acc[1] = acc[1] < uu ? uu : acc[1];
+            if (ph < -0.99) { acc[2] += rho[i1]; acc[3] += 1.0; }
+            if (ph > 0.99) { acc[4] += rho[i1]; acc[5] += 1.0; }
+            if (k == obs_z && ph > 0.0) acc[6] += 1.0;
+        }
+        if (copy_old && phi_old) phi_old[i4] = phi[i4];
+    }
+    __shared__ double red[MON_THREADS / 32][STEADY_NQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int m = 0; m < STEADY_NQ; ++m) {
+        double x = acc[m];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = m <= 1 ? ((x < y) ? y : x) : x + y;
+        }
+        if (lane == 0) red[wid][m] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < STEADY_NQ) {
+        const int m = threadIdx.x;
+        double x = red[0][m];
+        for (int q = 1; q < MON_THREADS / 32; ++q) x = m <= 1 ? ((x < red[q][m]) ? red[q][m] : x) : x + red[q][m];
+        out[(int64_t)m * L.nz + (k - 1)] = x;
+    }
 }
 
 // FP64 host image <-> field array of type T (phi, gradient fields of the mixed form)

@@ -85,8 +85,10 @@ struct KernelTable {
     int (*ens_init)(const EnsArgs &a, int prec, cudaStream_t);
     // largest co-resident grid of the persistent kernel for this block size
     int (*ens_max_grid)(int prec, int block);
-    // singlephase state from the velocity field in st.u, st.v, st.w (halo 1)
-    int (*init_velocity)(const DevState &, int rest_base, cudaStream_t);
+    // singlephase state from rho (device halo-1 array, nullable) and st.u, st.v, st.w
+    int (*init_velocity)(const DevState &, const double *rho, int rest_base, cudaStream_t);
+    // steady-state / breakthrough partials into out[7 * nz] (phi_old nullable)
+    int (*steady)(const DevState &, void *phi_old, double *out, int obs_z, int copy_old, cudaStream_t);
 };
 
 const KernelTable *kernels_fast();

@@ -419,30 +419,45 @@ int ens_max_grid(int prec, int block) {
 }
 
 template <class S>
-int init_velocity_t(const DevState &st, int rest_base, cudaStream_t s) {
+int init_velocity_t(const DevState &st, const double *rho, int rest_base, cudaStream_t s) {
     if (st.list) {
         k_init_vel_list<S><<<(unsigned)((st.lstride + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.cell1, st.nfl,
-                                                                                 st.u, st.v, st.w, rest_base, st.scale);
-    } else {
-        const Layout &L = st.L;
-        const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
-        k_init_vel_dense<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), st.u, st.v, st.w, st.walls, L,
-                                                                         rest_base, st.scale);
+                                                                                 rho, st.u, st.v, st.w, rest_base,
+                                                                                 st.scale);
+        k_init_vel_links<S><<<(unsigned)((st.nfl + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.cell1,
+                                                                             st.nfl, rho, st.u, st.v, st.w, rest_base,
+                                                                             st.scale);
+        return 2;
     }
+    const Layout &L = st.L;
+    const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    k_init_vel_dense<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), rho, st.u, st.v, st.w, st.walls, L,
+                                                                     rest_base, st.scale);
     return 1;
 }
 
-int init_velocity(const DevState &st, int rest_base, cudaStream_t s) {
+int init_velocity(const DevState &st, const double *rho, int rest_base, cudaStream_t s) {
     switch (st.prec) {
-        case MFLBM_FP32: return init_velocity_t<dfloat>(st, rest_base, s);
-        case MFLBM_FP16: return init_velocity_t<__half>(st, rest_base, s);
-        default: return init_velocity_t<double>(st, rest_base, s);
+        case MFLBM_FP32: return init_velocity_t<dfloat>(st, rho, rest_base, s);
+        case MFLBM_FP16: return init_velocity_t<__half>(st, rho, rest_base, s);
+        default: return init_velocity_t<double>(st, rho, rest_base, s);
     }
+}
+
+int steady(const DevState &st, void *phi_old, double *out, int obs_z, int copy_old, cudaStream_t s) {
+    if (mp_fp32(st))
+        k_steady<float><<<st.L.nz, MON_THREADS, 0, s>>>(fld<float>(st.phi), fld<float>(phi_old), st.rho, st.u, st.v,
+                                                        st.w, st.walls, out, st.L, obs_z, copy_old);
+    else
+        k_steady<double><<<st.L.nz, MON_THREADS, 0, s>>>(fld<double>(st.phi), fld<double>(phi_old), st.rho, st.u, st.v,
+                                                         st.w, st.walls, out, st.L, obs_z, copy_old);
+    return 1;
 }
 
 const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,
                            init_equilibrium, convert_in,  convert_out, field_in,      field_out,
-                           ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity};
+                           ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity,
+                           steady};
 
 }  // namespace MFLBM_NS
 }  // namespace mflbm

@@ -113,7 +113,8 @@ SIGNATURES = {
     "mflbm_ensemble_tune": (C.c_int32, [P, C.c_int32, P, C.c_int32]),
     "mflbm_ensemble_info": (C.c_int32, [P, P, P, P, P]),
     "mflbm_layout": (C.c_int32, [P]),
-    "mflbm_init_velocity": (C.c_int32, [P, P, P, P, C.c_int32]),
+    "mflbm_init_velocity": (C.c_int32, [P, P, P, P, P, C.c_int32]),
+    "mflbm_steady_monitor": (C.c_int32, [P, C.c_int32, P]),
     "mflbm_create": (C.c_int32, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "mflbm_destroy": (None, [P]),
     "mflbm_last_error": (C.c_char_p, [P]),

@@ -11,6 +11,9 @@ multiphase (multiphase_3D/0.src/Monitor.F90:157-260)
   pre.dat                     (I10,3(1x,e14.7))  open z only: inlet, outlet pressure and drop
   profile/monitor<I10.8>.dat  (5(1x,e14.7))      every ntime_monitor_profile steps
   steady_monitor_saturation_error.dat (steady_state_option 3)
+  steady_monitor_capillary_pressure_error.dat (I10,6(1x,e14.7))  steady_state_option 1
+  steady_monitor_max_phi_change.dat            (I10,2(1x,e14.7))  steady_state_option 2
+  (multiphase_3D/0.src/Monitor.F90:287-507 with Solver.steady_monitor)
 singlephase (singlephase_3D/0.src/Monitor.F90:109-165)
   flowrate_time.dat           (I10,2(1x,E14.6))  ntime, flowrate, umax
   pre.dat, profile/monitor<I10.8>.dat (3(1x,e14.7)),
@@ -167,3 +170,36 @@ class MonitorFiles:
             if rel < self.criteria and ntime > self.ntime_monitor:
                 end = CONVERGED
         return end
+
+
+def write_capillary_pressure(mf, ntime, out):
+    """monitor_multiphase_steady_capillarypressure's record and end indicator
+    (Monitor.F90:434-459) from Solver.steady_monitor(1)."""
+    pc, pre_w, pre_nw, umax = out[0], out[1], out[2], out[3]
+    mf.previous, mf.current = mf.current, pc
+    temp = abs(mf.current - mf.previous) / (abs(mf.current) + EPS)
+    mf._append("steady_monitor_capillary_pressure_error.dat", record(ntime, [temp, pc, pre_w, pre_nw, temp, umax]))
+    if math.isnan(umax) or math.isnan(pc):
+        return FAILED
+    if umax >= 0.5:
+        return FAILED
+    return CONVERGED if (temp < mf.criteria and ntime > mf.ntime_monitor) else RUNNING
+
+
+def write_phase_field_change(mf, ntime, out, ntime_relaxation=0):
+    """monitor_multiphase_steady_phasefield's record and end indicator (Monitor.F90:340-360)
+    from Solver.steady_monitor(2)."""
+    d_phi, umax = out[0], out[1]
+    if ntime <= ntime_relaxation:
+        return RUNNING
+    if math.isnan(umax) or math.isnan(d_phi):
+        return FAILED
+    mf._append("steady_monitor_max_phi_change.dat", record(ntime, [d_phi, umax]))
+    if umax >= 0.5:
+        return FAILED
+    return CONVERGED if (d_phi < mf.criteria and ntime > mf.ntime_monitor) else RUNNING
+
+
+def breakthrough(count):
+    """monitor_breakthrough (Monitor.F90:500-503): end once fluid 1 reaches z = nz - 1."""
+    return CONVERGED if count >= 1 else RUNNING

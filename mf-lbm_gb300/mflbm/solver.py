@@ -94,11 +94,11 @@ class Solver:
             assert phi.shape == self.shape4()
         self._check(self.lib.mflbm_init_equilibrium(self.ctx, _ptr(phi)))
 
-    def init_velocity(self, u=None, v=None, w=None, rest_base=True):
-        """State from a velocity field: interior arrays (nz, ny, nx) or halo-1 arrays; the
-        ghost layer of interior arrays is filled periodically."""
+    def init_velocity(self, u=None, v=None, w=None, rho=None, rest_base=True):
+        """State from density and velocity fields: interior arrays (nz, ny, nx) or halo-1
+        arrays; the ghost layer of interior arrays is filled periodically."""
         arrs = []
-        for a in (u, v, w):
+        for a in (rho, u, v, w):
             if a is None:
                 arrs.append(None)
                 continue
@@ -170,6 +170,14 @@ class Solver:
         st = C.c_int32()
         self._check(self.lib.mflbm_monitor(self.ctx, _ptr(prof), _ptr(scal), C.byref(st)))
         return prof.reshape(nq, self.nz), scal, st.value
+
+    def steady_monitor(self, kind):
+        """mflbm_steady_monitor: 0 snapshot phi_old, 1 capillary pressure (pc, pre_w, pre_nw,
+        umax, count_w, count_nw), 2 phase-field change (d_phi_max, umax), 3 breakthrough
+        count at z = nz - 1."""
+        out = np.zeros(6)
+        self._check(self.lib.mflbm_steady_monitor(self.ctx, kind, _ptr(out)))
+        return out[:{0: 0, 1: 6, 2: 2, 3: 1}[kind]]
 
     def saturation(self):
         a, b = C.c_double(), C.c_double()

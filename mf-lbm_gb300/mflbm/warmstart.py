@@ -17,7 +17,8 @@ Architecture (channels c = (c1, c2, c3, c4), grid n divisible by 8):
     d3 = conv([up(b), e3], c4+c3 -> c3)     n/4
     d2 = conv([up(d3), e2], c3+c2 -> c2)    n/2
     d1 = conv([up(d2), e1], c2+c1 -> c1)    n
-    y  = conv(d1, c1 -> 16), no activation; channels 0..2 are (u, v, w)
+    y  = conv(d1, c1 -> 16), no activation; channels 0..2 are (u, v, w), 3 the density
+         deviation from the sample's mean density
 ReLU after every convolution but the last.
 """
 import ctypes as C
@@ -27,8 +28,10 @@ import numpy as np
 
 from . import _capi
 
-NOUT = 16          # output channels of the last GEMM (N % 16); 0..2 carry the velocity
+NOUT = 16          # output channels of the last GEMM (N % 16); 0..2 velocity, 3 density
 U_SCALE = 10.0     # target = u * nu / F_z / U_SCALE
+RHO_SCALE = 1e4    # target channel 3 = (rho - mean_density) * RHO_SCALE
+NTARGET = 4
 
 
 def _kp(cin):
@@ -52,8 +55,8 @@ def init_weights(c=(16, 32, 64, 128), seed=0):
         std = math.sqrt(2.0 / (27 * cin))
         w[:, :27 * cin] = rng.normal(0.0, std, size=(cout, 27 * cin)).astype(np.float32)
         if name == "y":
-            w[3:] = 0.0
-            w[:3] *= 0.1
+            w[NTARGET:] = 0.0
+            w[:NTARGET] *= 0.1
         out[name] = (w, np.zeros(cout, dtype=np.float32))
     return out
 
@@ -120,7 +123,7 @@ class Net:
         self.ksplit = 256
         self.work = torch.empty(self.ksplit * maxk * maxc, dtype=f32, device=self.dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        self.partial = torch.empty((nv * 3 + 255) // 256, dtype=torch.float64, device=self.dev)
+        self.partial = torch.empty((nv * NTARGET + 255) // 256, dtype=torch.float64, device=self.dev)
         self.stream = C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
     # ---- helpers -----------------------------------------------------------------------
@@ -224,13 +227,14 @@ class Net:
         self._conv_back("e1", self.g["e1"], False)
 
     def loss_grad(self, target, mask):
-        """Masked MSE of channels 0..2 against target (n^3, 3) fp32; sets self.g['y'];
-        returns the loss as a device tensor (no synchronisation)."""
+        """Masked MSE of the first target.shape[1] channels against target (n^3, C) fp32;
+        sets self.g['y']; returns the loss as a device tensor."""
         nv = self.n ** 3
         L, p, s = self.lib, self._p, self.stream
+        nc = int(target.shape[1])
         self.g["y"].zero_()
-        cnt = max(1.0, float(mask.sum().item()) * 3.0)
-        self._ck(L.mflbm_nn_mse(p(self.out), NOUT, p(target), p(mask), p(self.g["y"]), p(self.partial), nv, 3,
+        cnt = max(1.0, float(mask.sum().item()) * nc)
+        self._ck(L.mflbm_nn_mse(p(self.out), NOUT, p(target), p(mask), p(self.g["y"]), p(self.partial), nv, nc,
                                 1.0 / cnt, s), "mse")
         return self.partial.sum() / cnt
 
@@ -268,10 +272,35 @@ def features(walls_global):
     return x.reshape(-1, 2)
 
 
-def target_from_macro(macro, nu, fz):
-    """(n^3, 3) scaled velocity from Solver.macro() (halo-1 arrays) in voxel order."""
+def mean_density(walls_global):
+    """Mean fluid density of the settled flow of a periodic sample started from the
+    reference's equilibrium at rest.  The mass that takes part in the update is the fluid
+    nodes' plus the bounce-back link slots'; it starts as N_fluid + sum over links of the
+    BGK weight w_q and settles as rho (N_fluid + sum over links of the MRT rest weight W_q)."""
+    fl = walls_global == 0
+    ex, ey, ez = (np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0]),
+                  np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1]),
+                  np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1]))
+    wb = [1 / 3] + [1 / 18] * 6 + [1 / 36] * 12
+    wm = [4 / 21] + [13 / 126] * 6 + [1 / 63] * 12
+    sb = sm = 0.0
+    for q in range(1, 19):
+        nfl = np.roll(fl, shift=(-ez[q], -ey[q], -ex[q]), axis=(0, 1, 2))
+        c = float(np.count_nonzero(~fl & nfl))
+        sb += c * wb[q]
+        sm += c * wm[q]
+    nf = float(fl.sum())
+    return (nf + sb) / (nf + sm)
+
+
+def target_from_macro(macro, nu, fz, rho_mean):
+    """(n^3, 4) targets from Solver.macro() (halo-1 arrays) in voxel order: the scaled
+    velocity and the scaled density deviation (zero in the solid)."""
     u = [macro[k][1:-1, 1:-1, 1:-1] for k in ("u", "v", "w")]
-    return (np.stack(u, axis=-1) * (nu / fz / U_SCALE)).reshape(-1, 3).astype(np.float32)
+    rho = macro["rho"][1:-1, 1:-1, 1:-1]
+    dr = np.where(rho != 0.0, rho - rho_mean, 0.0) * RHO_SCALE
+    t = np.concatenate([np.stack(u, axis=-1) * (nu / fz / U_SCALE), dr[..., None]], axis=-1)
+    return t.reshape(-1, NTARGET).astype(np.float32)
 
 
 def velocity_from_output(out, n, nu, fz, walls_global):
@@ -279,6 +308,13 @@ def velocity_from_output(out, n, nu, fz, walls_global):
     o = out[:, :3].reshape(n, n, n, 3) * (U_SCALE * fz / nu)
     fluid = (walls_global == 0)
     return [o[..., a] * fluid for a in range(3)]
+
+
+def density_from_output(out, n, walls_global, rho_mean):
+    """Network output -> density (nz, ny, nx): the sample's mean density plus the
+    predicted deviation in the fluid, 1 in the solid."""
+    fluid = (walls_global == 0)
+    return np.where(fluid, rho_mean + out[:, 3].reshape(n, n, n) / RHO_SCALE, 1.0)
 
 
 def equilibrium_state(u, v, w, nx, ny, nz):
@@ -323,17 +359,18 @@ def make_samples(n, count, seed, por_lo=0.15, por_hi=0.35, workers=0):
     return [_make_sample(j) for j in jobs]
 
 
-def solve(wg, precision=1, tol=1e-7, init_u=None, rest_base=False, max_steps=400000, nu=1.0 / 6.0, fz=1e-6,
-          device=0):
+def solve(wg, precision=1, tol=1e-7, init_u=None, init_rho=None, rest_base=False, max_steps=400000, nu=1.0 / 6.0,
+          fz=1e-6, device=0):
     """Steady singlephase run of one periodic sample (fluid-list layout); returns the
     SteadyResult, the solver's macro fields and the set-up time.
 
     Without init_u and rest_base the run starts as the reference does (equilibrium at
-    rest with the BGK weights).  rest_base starts from the rest state of the reference's
-    MRT collision instead; init_u = (u, v, w) (interior arrays, the steady velocity as
-    compute_macro_vars reports it) adds the equilibrium velocity terms, with F_z/2 added to
-    w in the fluid because the stored post-collision momentum leads the reported velocity
-    by half the body force."""
+    rest with the BGK weights).  Otherwise it starts from the rest state of the
+    reference's MRT collision at density init_rho (default: the sample's mean_density),
+    plus the equilibrium velocity terms of init_u = (u, v, w) (interior arrays, the steady
+    velocity as compute_macro_vars reports it: F_z/2 is added to w in the fluid because
+    the stored post-collision momentum leads it by half the body force), with the
+    bounce-back link slots set consistently (mflbm_init_velocity)."""
     import time as _t
     from . import geometry
     from .permeability import run_to_steady
@@ -345,13 +382,16 @@ def solve(wg, precision=1, tol=1e-7, init_u=None, rest_base=False, max_steps=400
     with Solver(p) as sim:
         sim.set_geometry(walls)
         t0 = _t.perf_counter()
-        if init_u is None and not rest_base:
+        if init_u is None and init_rho is None and not rest_base:
             sim.init_equilibrium()
-        elif init_u is None:
-            sim.init_velocity(None, None, None, rest_base=True)
         else:
             fluid = (wg == 0)
-            sim.init_velocity(init_u[0], init_u[1], init_u[2] + 0.5 * fz * fluid, rest_base=True)
+            rho = init_rho if init_rho is not None else np.where(fluid, mean_density(wg), 1.0)
+            if init_u is None:
+                init_u = (None, None, 0.5 * fz * fluid)
+            else:
+                init_u = (init_u[0], init_u[1], init_u[2] + 0.5 * fz * fluid)
+            sim.init_velocity(*init_u, rho=rho, rest_base=True)
         setup = _t.perf_counter() - t0
         r = run_to_steady(sim, p, check_every=100, tol=tol, max_steps=max_steps)
         mac = sim.macro()

@@ -14,9 +14,10 @@ from .init import initial_phase
 from .solver import make_params
 
 
-def _assemble_multiphase(p, walls_global, theta_deg, interface_z0, option=1):
+def _assemble_multiphase(p, walls_global, theta_deg, interface_z0, option=1, gpu_preprocess=False):
     walls, pore, wchan = geometry.set_walls(p, walls_global)
-    solid, fluid = geometry.preprocess(p, wchan, geometry.contact_angle_rad(theta_deg))
+    prep = geometry.preprocess_gpu if gpu_preprocess else geometry.preprocess
+    solid, fluid = prep(p, wchan, geometry.contact_angle_rad(theta_deg))
     w_in = geometry.inlet_profile(p.nx, p.ny, p.uin_avg) if p.inlet_bc == 1 else None
     phi = initial_phase(p, option, interface_z0)
     return dict(params=p, walls=walls, pore=pore, solid=solid, fluid=fluid, w_in=w_in, phi=phi)
@@ -54,7 +55,8 @@ def packing_permeability(n=256, porosity=0.22, seed=2024, precision=0, strict_fp
     return dict(params=p, walls=walls, pore=pore, walls_global=wg)
 
 
-def packing_drainage(nxy=512, nzp=512, buffer=32, porosity=0.22, seed=7, strict_fp=0, device=0, precision=0):
+def packing_drainage(nxy=512, nzp=512, buffer=32, porosity=0.22, seed=7, strict_fp=0, device=0, precision=0,
+                     gpu_preprocess=False):
     """Multiphase drainage of a sphere packing: nxy x nxy x nzp packing plus open inlet and
     outlet buffers of `buffer` layers; walls on the x and y faces; phi = +1 in the inlet
     buffer; injection velocity 5e-5, viscosity ratio 1, gamma = 0.01, contact angle 30 deg."""
@@ -68,7 +70,7 @@ def packing_drainage(nxy=512, nzp=512, buffer=32, porosity=0.22, seed=7, strict_
                                    periodic=(False, False, False))
     wg = np.zeros((nz, nxy, nxy), dtype=np.int8)
     wg[buffer:buffer + nzp] = pack
-    return _assemble_multiphase(p, wg, theta_deg=30.0, interface_z0=float(buffer))
+    return _assemble_multiphase(p, wg, theta_deg=30.0, interface_z0=float(buffer), gpu_preprocess=gpu_preprocess)
 
 
 def packing_ensemble(n_samples=256, edge_lo=48, edge_hi=160, por_lo=0.15, por_hi=0.35, seed=11, precision=1,
