@@ -251,15 +251,16 @@ def ensemble_study(args):
     steps), converged samples leaving the sweep; value = fluid-node updates per second,
     samples/s in config.  With --c4-fp64 the FP64 ensemble of the same seeds gives the
     per-sample permeability error of the storage form."""
-    import torch
     from mflbm import workloads
-    from mflbm.ensemble import Ensemble, run_to_steady, tune_cached
     world, rank, local = dist_env()
-    torch.cuda.set_device(local)
     prec = args.precision if args.precision else 1
     t0 = time.perf_counter()
-    case = workloads.packing_ensemble(n_samples=args.samples, precision=prec, device=local)
+    case = workloads.packing_ensemble(n_samples=args.samples, precision=prec, device=local,
+                                      workers=min(16, os.cpu_count() or 1))
     gen_s = time.perf_counter() - t0
+    import torch
+    from mflbm.ensemble import Ensemble, run_to_steady, tune_cached
+    torch.cuda.set_device(local)
     res = {}
     k64 = args.c4_fp64_samples if args.c4_fp64_samples > 0 else args.samples
     for pr in ([prec, 0] if args.c4_fp64 else [prec]):

@@ -73,13 +73,24 @@ def packing_drainage(nxy=512, nzp=512, buffer=32, porosity=0.22, seed=7, strict_
     return _assemble_multiphase(p, wg, theta_deg=30.0, interface_z0=float(buffer), gpu_preprocess=gpu_preprocess)
 
 
+def _ensemble_sample(args):
+    e, por, sd = args
+    q = make_params(multiphase=0, nx=e, ny=e, nz=e, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
+                    wall_y_min=0, wall_y_max=0, wall_z_min=0, wall_z_max=0, mrt=1)
+    wg = geometry.sphere_packing((e, e, e), float(por), mean_r=8.0, sd_r=2.0, seed=int(sd))
+    walls, pore, _ = geometry.set_walls(q, wg)
+    return (e, e, e, walls), int(pore)
+
+
 def packing_ensemble(n_samples=256, edge_lo=48, edge_hi=160, por_lo=0.15, por_hi=0.35, seed=11, precision=1,
-                     device=0, force_z=1e-6):
+                     device=0, force_z=1e-6, workers=0):
     """Batched permeability ensemble: cubic samples with edges drawn uniformly from
     [edge_lo, edge_hi], porosity uniform in [por_lo, por_hi], each a seeded sphere packing
     (lognormal radii mean 8, sd 2, isolated pores removed), periodic x, y, z, body force
     along z, tau = 1, MRT preset 1.  Returns the common params and the sample list
-    (nx, ny, nz, halo-2 walls) for mflbm.ensemble.Ensemble, plus the fluid counts."""
+    (nx, ny, nz, halo-2 walls) for mflbm.ensemble.Ensemble, plus the fluid counts.
+    workers > 1 builds the samples in a spawn-started process pool (call before any GPU
+    work)."""
     rng = np.random.default_rng(seed)
     edges = rng.integers(edge_lo, edge_hi + 1, size=n_samples)
     pors = rng.uniform(por_lo, por_hi, size=n_samples)
@@ -87,13 +98,13 @@ def packing_ensemble(n_samples=256, edge_lo=48, edge_hi=160, por_lo=0.15, por_hi
     p = make_params(multiphase=0, nx=8, ny=8, nz=8, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
                     wall_y_min=0, wall_y_max=0, wall_z_min=0, wall_z_max=0, inlet_bc=0, outlet_bc=0, mrt=1,
                     la_nu1=1.0 / 6.0, force_z=force_z, precision=precision, device=device)
-    samples, nf = [], []
-    for e, por, sd in zip(edges, pors, seeds):
-        e = int(e)
-        q = make_params(multiphase=0, nx=e, ny=e, nz=e, iper=1, jper=1, kper=1, wall_x_min=0, wall_x_max=0,
-                        wall_y_min=0, wall_y_max=0, wall_z_min=0, wall_z_max=0, mrt=1)
-        wg = geometry.sphere_packing((e, e, e), float(por), mean_r=8.0, sd_r=2.0, seed=int(sd))
-        walls, pore, _ = geometry.set_walls(q, wg)
-        samples.append((e, e, e, walls))
-        nf.append(int(pore))
+    jobs = [(int(e), float(por), int(sd)) for e, por, sd in zip(edges, pors, seeds)]
+    if workers > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_ensemble_sample, jobs)
+    else:
+        res = [_ensemble_sample(j) for j in jobs]
+    samples = [r[0] for r in res]
+    nf = [r[1] for r in res]
     return dict(params=p, samples=samples, nf=np.array(nf, dtype=np.int64), edges=edges, porosity=pors)
