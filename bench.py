@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--test", type=int, default=6, help="c5: held-out samples")
     ap.add_argument("--epochs", type=int, default=8, help="c5: training epochs")
     ap.add_argument("--n5", type=int, default=128, help="c5: sample edge")
+    ap.add_argument("--c5-data-tol", type=float, default=1e-7, help="c5: convergence of the training solutions")
     ap.add_argument("--c3-study", action="store_true",
                     help="c3: FP64 and FP32 forms over --c3-steps steps, saturation every 500 steps, phi L1 error")
     ap.add_argument("--c3-steps", type=int, default=20000)
@@ -299,7 +300,7 @@ def ensemble_study(args):
 
 def warmstart_study(args):
     """c5: train the warm-start network on LBM solutions the solver produces (FP32
-    deviation form to |du|/u < 1e-6), then on held-out samples compare runs to 1e-7 from
+    deviation form to |du|/u < --c5-data-tol), then on held-out samples compare runs to 1e-7 from
     rest and from the prediction (FP64 and FP32), wall time including inference.  "rest"
     is the reference's start (equilibrium at rest, BGK weights); the warm start places the
     predicted velocity and density on the rest state of the MRT collision with consistent
@@ -319,7 +320,7 @@ def warmstart_study(args):
     t0 = time.perf_counter()
     data_lu = 0
     for wg, x in train_s:
-        r, mac, _ = ws.solve(wg, precision=1, tol=1e-6, nu=nu, fz=fz)
+        r, mac, _ = ws.solve(wg, precision=1, tol=args.c5_data_tol, nu=nu, fz=fz)
         data_lu += int((wg == 0).sum()) * r.steps
         xs.append(torch.from_numpy(x).cuda().to(torch.bfloat16))
         ys.append(torch.from_numpy(ws.target_from_macro(mac, nu, fz, ws.mean_density(wg))).cuda())
@@ -364,7 +365,7 @@ def warmstart_study(args):
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
             "data": "synthetic",
             "config": {"workload": f"learned warm start: {n}^3 sphere packings, porosity U[0.15,0.35], F_z=1e-6, tau=1, "
-                                   f"{args.train} training samples (FP32 LBM to 1e-6), {args.test} held-out samples, "
+                                   f"{args.train} training samples (FP32 LBM to {args.c5_data_tol}), {args.test} held-out samples, "
                                    f"convergence {args.conv_tol} every 100 steps",
                        "generate_s": gen_s, "training_data_s": data_s, "training_data_mlups": data_lu / data_s / 1e6,
                        "train_s": train_s_time, "epochs": args.epochs, "loss_per_epoch": hist,

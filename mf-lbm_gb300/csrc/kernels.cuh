@@ -1077,7 +1077,11 @@ __global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restric
         const T nwx = T(b.nwx), nwy = T(b.nwy), nwz = T(b.nwz), sin_t = T(b.sin_t);
         const T tmpCos = T(b.cos_t);
         const T tmp1 = nwx * cnx0 + nwy * cny0 + nwz * cnz0;
-        const T tmp2 = T(1.0) / sqrt(T(1.0) - tmp1 * tmp1);
+        // FP32 form: unit vectors normalised in FP32 can give |nw.n| a few ulp above 1, where
+        // the reference's 1/sqrt(1 - (nw.n)^2) has no value; FP64 keeps the formula as is
+        T one_m = T(1.0) - tmp1 * tmp1;
+        if (sizeof(T) == 4 && one_m < T(1e-6)) one_m = T(1e-6);
+        const T tmp2 = T(1.0) / sqrt(one_m);
         const T coe1 = sin_t * tmp1 * tmp2;
         const T coe2 = sin_t * tmp2;
         const T cnxp = (tmpCos - coe1) * nwx + coe2 * cnx0;
