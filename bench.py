@@ -289,6 +289,14 @@ def ensemble_study(args):
                        "fluid_updates": r.fluid_updates, "generate_s": gen_s, "launch": tune.get("chosen"),
                        "tuner": tune.get("candidates")},
             "clocks": clocks, "gpu_launches": None}
+    per = []
+    for i in range(args.samples):
+        row = {"edge": int(case["edges"][i]), "porosity": float(case["porosity"][i]), "steps": int(r.steps[i]),
+               "k": float(r.k[i])}
+        if args.c4_fp64 and i < k64:
+            row.update(steps_fp64=int(res[0][0].steps[i]), k_fp64=float(res[0][0].k[i]))
+        per.append(row)
+    line["config"]["per_sample"] = per
     if args.c4_fp64:
         r64 = res[0][0]
         err = np.abs(r.k[:k64] - r64.k) / np.abs(r64.k)
@@ -433,7 +441,8 @@ def drainage_study(args):
             "config": {"workload": f"multiphase drainage, {args.n}^2x{args.n} sphere packing porosity 0.22 + 32-layer "
                                    "buffers, inlet velocity 5e-5, gamma=0.01, theta=30; FP32 mixed form vs FP64",
                        "lattice": [case["params"].nx, case["params"].ny, case["params"].nz], "fluid_nodes": pore,
-                       "generate_s": gen_s, "fp64_mlups": pore * args.c3_steps / res[0][2] / 1e6,
+                       "generate_s": gen_s, "fp64_mlups": pore * res[0][3] / res[0][2] / 1e6, "fp64_steps": res[0][3],
+                       "phi_compared_at_step": n64,
                        "fp32_mlups": pore * args.c3_steps / res[1][2] / 1e6,
                        "wall_s": {"fp64": res[0][2], "fp32": res[1][2]},
                        "saturation_every_500": {"step": [x[0] for x in res[1][0]], "fp64": s64.tolist(),
