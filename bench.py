@@ -34,10 +34,11 @@ for sub in ("mf-lbm_gb300", "oracle"):
 import numpy as np  # noqa: E402
 
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
-BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1}
+BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
 BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1}
-DTYPE = {0: "f64", 1: "f32", 2: "f16"}
+# 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe
+DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff"}
 
 
 def parse():
@@ -46,7 +47,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "c5net"],
                     help="c2: singlephase packing permeability (default); c1: multiphase tube drainage; "
                          "c3: multiphase packing drainage; c4: batched permeability ensemble to steady state; "
                          "c5: learned warm start (train the network, then A/B against runs from rest)")
@@ -66,7 +67,9 @@ def parse():
                     help="c4: run the FP64 reference on the first K samples only (0: all)")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
     ap.add_argument("--porosity", type=float, default=0.22)
-    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="0 FP64, 1 FP32 (deviations for singlephase), 2 FP16 deviations, "
+                         "3 FP64 storage with the double-word collision (singlephase)")
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
     ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -197,7 +200,7 @@ def convergence_study(args, case, device):
     from mflbm.permeability import run_to_steady
     out = {"tol": args.conv_tol, "check_every": 100, "forms": {}}
     base = None
-    for prec in (0, 1, 2):
+    for prec in (0, 3, 1, 2):
         p = copy.copy(case["params"])
         p.precision = prec
         with Solver(p) as sim:
@@ -390,6 +393,91 @@ def warmstart_study(args):
     return 0
 
 
+def network_step_bench(args):
+    """c5net: one training step of the warm-start network (forward, masked MSE, backward,
+    Adam) on one --n5^3 sample, K steps timed with CUDA events on the network's stream.
+    The roofline is that of the largest tcgen05 GEMM (the forward convolution of the last
+    decoder level, n^3 x 1344 x 16), timed alone on the same stream: HBM-bound, its
+    algorithmic bytes are the im2col matrix, the weights and the FP32 output."""
+    import torch
+    from mflbm import _capi, geometry
+    from mflbm import warmstart as ws
+    torch.cuda.set_device(0)
+    n = args.n5
+    wg = geometry.sphere_packing((n, n, n), 0.25, mean_r=8.0, sd_r=2.0, seed=11)
+    x = torch.from_numpy(ws.features(wg)).cuda().to(torch.bfloat16)
+    rng = np.random.default_rng(5)
+    target = torch.from_numpy(0.1 * rng.normal(size=(n ** 3, ws.NTARGET)).astype(np.float32)).cuda()
+    mask = torch.from_numpy((wg == 0).reshape(-1).astype(np.float32)).cuda()
+    net = ws.Net(n, seed=7)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        net.forward(x)
+        net.loss_grad(target, mask)
+        net.backward()
+        net.adam(lr=1e-4)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    c0 = net.calls
+    step()
+    calls_per_step = net.calls - c0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    net.check_err()
+    # the largest forward GEMM alone
+    name = "d1"
+    cin, cout = next((s[1], s[2]) for s in net.specs if s[0] == name)
+    kp, nv = ws._kp(cin), n ** 3
+    L, p, s = net.lib, net._p, net.stream
+    reps = 20
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(reps):
+        rc = L.mflbm_nn_gemm_bf16(p(net.col[name]), kp, p(net.Wb[name]), kp, p(net.acc), cout, nv, cout, kp, 0,
+                                  p(net.err), s)
+        if rc:
+            raise _capi.MflbmError(rc, "gemm")
+    g1.record(stream)
+    torch.cuda.synchronize()
+    net.check_err()
+    gemm_s = g0.elapsed_time(g1) / reps / 1e3
+    gbytes = nv * kp * 2 + cout * kp * 2 + nv * cout * 4
+    gflop = 2.0 * nv * kp * cout
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    splitk = len(net.specs)     # one split-K weight-gradient GEMM (two launches) per layer
+    line = {"metric": "warm-start network training steps per second", "value": 1e3 / ms, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic",
+            "config": {"workload": f"warm-start network training step, one {n}^3 sample, channels {net.c}, "
+                                   f"forward + masked MSE + backward + Adam",
+                       "l2": "activations and im2col matrices (GBs) far above the 129 MB L2: no flush needed"},
+            "roofline": {"bound": "hbm", "kernel": f"k_gemm_bf16 ({nv} x {kp} x {cout}, layer {name} forward)",
+                         "achieved": gbytes / gemm_s / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": gbytes / gemm_s / 1e9 / hbm, "traffic": None,
+                         "tensor_tflops": gflop / gemm_s / 1e12, "tensor_frac": gflop / gemm_s / 1e12 / bf16,
+                         "avg_launch_ms": gemm_s * 1e3, "peak_source": "measured (MEASURED_PEAKS.json)"},
+            "gpu_launches": (calls_per_step + splitk) * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def drainage_study(args):
     """c3 at scale: the FP64 form and the FP32 mixed form of the same drainage from the
     same initial state; saturation (FP64 device sums) every 500 steps and, at the end,
@@ -464,6 +552,8 @@ def main():
         return ensemble_study(args)
     if args.workload == "c5":
         return warmstart_study(args)
+    if args.workload == "c5net":
+        return network_step_bench(args)
     world, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -532,7 +622,7 @@ def main():
 
     layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
     collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
-    elt = 8 if args.precision == 0 else (4 if args.precision == 1 else 2)
+    elt = 8 if args.precision in (0, 3) else (4 if args.precision == 1 else 2)
     state_bytes = (2 if p.multiphase else 1) * 19 * elt * (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
     bpl = BYTES_PER_LU_MP[args.precision] if p.multiphase else BYTES_PER_LU[args.precision]
     peaks = {}
@@ -547,7 +637,8 @@ def main():
     if os.path.exists(tf):
         try:
             t = json.load(open(tf))
-            key = f"{DTYPE[args.precision]}_{layout}"
+            # the double-word form moves the FP64 form's bytes
+            key = f"{DTYPE[0 if args.precision == 3 else args.precision]}_{layout}"
             traffic = t[key] * pore if (key in t and not p.multiphase) else None
         except Exception:
             traffic = None

@@ -82,6 +82,8 @@ int cuda_fail(mflbm_ctx *c, cudaError_t e, const char *what) {
     } while (0)
 
 int64_t n1(const mflbm_params &p) { return (int64_t)(p.nx + 2) * (p.ny + 2) * (p.nz + 2); }
+// the PDFs are stored as FP64 (the plain form and the double-word collision form)
+bool f64_storage(const mflbm_params &p) { return p.precision == MFLBM_FP64 || p.precision == MFLBM_FP64FF; }
 int64_t n2(const mflbm_params &p) { return (int64_t)(p.nx + 4) * (p.ny + 4) * (p.nz + 4); }
 int64_t n4(const mflbm_params &p) { return (int64_t)(p.nx + 8) * (p.ny + 8) * (p.nz + 8); }
 int64_t nplane(const mflbm_params &p) { return (int64_t)(p.nx + 2) * (p.ny + 2); }
@@ -103,6 +105,10 @@ int validate(const mflbm_params *p, std::string &err) {
         if (p->mrt < 1 || p->mrt > 4) { err = "mrt must be 1..4"; return MFLBM_EINVAL; }
         if (p->precision == MFLBM_FP16) {
             err = "multiphase supports MFLBM_FP64 and MFLBM_FP32 storage (FP16 deviations cannot hold a vanishing species)";
+            return MFLBM_EINVAL;
+        }
+        if (p->precision == MFLBM_FP64FF) {
+            err = "MFLBM_FP64FF (double-word collision) is singlephase";
             return MFLBM_EINVAL;
         }
         if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
@@ -132,7 +138,7 @@ int validate(const mflbm_params *p, std::string &err) {
         err = "Inlet pressure + outlet convective BC is not supported";
         return MFLBM_EINVAL;
     }
-    if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FP16) { err = "unknown precision"; return MFLBM_EINVAL; }
+    if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FP64FF) { err = "unknown precision"; return MFLBM_EINVAL; }
     if (p->layout < MFLBM_LAYOUT_AUTO || p->layout > MFLBM_LAYOUT_LIST) { err = "unknown layout"; return MFLBM_EINVAL; }
     if (p->layout == MFLBM_LAYOUT_LIST && (p->multiphase || p->inlet_bc != 0 || p->outlet_bc != 0)) {
         err = "the fluid-list layout is singlephase without inlet/outlet boundary conditions";
@@ -357,6 +363,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     c->st.fold.fz = P.force_z;
     c->st.fold32 = fold_rates<float>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
     c->st.fold32.fz = (float)P.force_z;
+    c->st.foldff = fold_to_ff(c->st.fold);
     c->st.unit = fold_is_unit(c->st.fold) ? 1 : 0;
     c->st.multiphase = p.multiphase;
     c->st.prec = p.precision;
@@ -384,7 +391,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.mon, (int64_t)kMonNQ * p.nz))) goto fail_create;
     // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
     // phase field when that is larger
-    if ((p.precision != MFLBM_FP64 || !p.multiphase) &&
+    if ((!f64_storage(p) || !p.multiphase) &&
         (r = dalloc(c, &c->st.stage, p.multiphase ? std::max(n1(p), n4(p)) : n1(p)))) goto fail_create;
     if (p.multiphase) {
         const size_t fe = (size_t)c->st.felt;
@@ -590,7 +597,7 @@ int32_t mflbm_upload_state(mflbm_ctx *c, const double *const *f, const double *c
         const double *const *src = s == 0 ? f : g;
         char *base = (char *)(s == 0 ? c->st.f : c->st.g);
         for (int q = 0; q < 19; ++q) {
-            if (p.precision == MFLBM_FP64 && !c->st.list) {
+            if (f64_storage(p) && !c->st.list) {
                 char *dst = base + ((size_t)q * L.qs + L.xo) * c->elt;
                 CK(c, cudaMemcpy2DAsync(dst, (size_t)L.pitch * 8, src[q], (size_t)(p.nx + 2) * 8, (size_t)(p.nx + 2) * 8,
                                         (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyHostToDevice, c->stream));
@@ -628,7 +635,7 @@ int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, d
         const char *base = (const char *)(s == 0 ? c->st.f : c->st.g);
         for (int q = 0; q < 19; ++q) {
             if (!dstv[q]) continue;
-            if (p.precision == MFLBM_FP64 && !c->st.list) {
+            if (f64_storage(p) && !c->st.list) {
                 const char *src = base + ((size_t)q * L.qs + L.xo) * c->elt;
                 CK(c, cudaMemcpy2DAsync(dstv[q], (size_t)(p.nx + 2) * 8, src, (size_t)L.pitch * 8, (size_t)(p.nx + 2) * 8,
                                         (size_t)(p.ny + 2) * (p.nz + 2), cudaMemcpyDeviceToHost, c->stream));

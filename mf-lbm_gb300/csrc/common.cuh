@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
+#include "ffloat.cuh"
 
 namespace mflbm {
 
@@ -140,6 +141,22 @@ __host__ __device__ __forceinline__ MrtFold<R> fold_rates(double s_e, double s_e
     return c;
 }
 
+// an FP64 fold as double words (host)
+inline MrtFold<ff> fold_to_ff(const MrtFold<double> &d) {
+    MrtFold<ff> c;
+    c.e_m = ff(d.e_m); c.e_den = ff(d.e_den); c.e_u2 = ff(d.e_u2); c.e_f = ff(d.e_f);
+    c.e2_m = ff(d.e2_m); c.e2_u2 = ff(d.e2_u2); c.e2_f = ff(d.e2_f);
+    c.q_m = ff(d.q_m); c.q_u = ff(d.q_u); c.q_f = ff(d.q_f);
+    c.x3_m = ff(d.x3_m); c.x3_eq = ff(d.x3_eq); c.x3_f = ff(d.x3_f);
+    c.xi_m = ff(d.xi_m); c.xi_f = ff(d.xi_f);
+    c.w_m = ff(d.w_m); c.w_eq = ff(d.w_eq); c.w_f = ff(d.w_f);
+    c.wi_m = ff(d.wi_m); c.wi_f = ff(d.wi_f);
+    c.o_m = ff(d.o_m); c.o_eq = ff(d.o_eq); c.o_f = ff(d.o_f);
+    c.t_m = ff(d.t_m);
+    c.fz = ff(d.fz);
+    return c;
+}
+
 // The same fold evaluated in the arithmetic type R, for the per-node rates of the
 // multiphase collision (omega depends on phi).  Divisions by the constant norms are
 // multiplications by their reciprocals (default build only; a division costs about ten
@@ -190,6 +207,7 @@ struct EnsArgs {
     StepParams P;
     MrtFold<double> fold;
     MrtFold<float> fold32;
+    MrtFold<ff> foldff;
     float scale;
     int32_t ntime0;          // ntime of the first step of the launch
     int32_t nsteps;          // steps per persistent launch

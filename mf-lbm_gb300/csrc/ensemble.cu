@@ -147,7 +147,8 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
     if (common->multiphase) return efail(nullptr, MFLBM_EINVAL, "ensembles are singlephase");
     if (common->inlet_bc != 0 || common->outlet_bc != 0)
         return efail(nullptr, MFLBM_EINVAL, "ensembles have no inlet/outlet boundary conditions");
-    if (common->precision < MFLBM_FP64 || common->precision > MFLBM_FP16) return efail(nullptr, MFLBM_EINVAL, "unknown precision");
+    if (common->precision < MFLBM_FP64 || common->precision > MFLBM_FP64FF)
+        return efail(nullptr, MFLBM_EINVAL, "unknown precision");
     if (!(common->la_nu1 > 0.0)) return efail(nullptr, MFLBM_EINVAL, "la_nu1 must be positive");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return efail(nullptr, MFLBM_ENODEV, "no CUDA device");
@@ -268,6 +269,7 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
         a.fold.fz = P.force_z;
         a.fold32 = fold_rates<float>(P.s_e, P.s_e2, P.s_q, P.s_nu, P.s_pi, P.s_t);
         a.fold32.fz = (float)P.force_z;
+        a.foldff = fold_to_ff(a.fold);
         a.unit = fold_is_unit(a.fold) ? 1 : 0;
     }
     e->block = 128;

@@ -1,0 +1,115 @@
+// ffloat.cuh -- double-word ("float-float") arithmetic on the FP32 pipe.
+//
+// A value is the unevaluated sum hi + lo of two FP32 numbers, |lo| of the order of
+// ulp(hi): about 48 significant bits.  GB300 issues 64 FP32 operations per FP64 operation,
+// and an add or a multiply in this form costs 6-8 FP32 operations, so a collision that
+// keeps FP64 storage but computes in this form runs on the FP32 pipe several times faster
+// than on the FP64 pipe.  The building blocks are the error-free transformations of the
+// literature:
+//   TwoSum   (Knuth, TAOCP vol. 2, sec. 4.2.2)  s + e = a + b exactly, 6 operations
+//   Fast2Sum (Dekker 1971)                       the same when |a| >= |b|, 3 operations
+//   TwoProd  (with a fused multiply-add)         p + e = a * b exactly, 2 operations
+// combined as in Joldes, Muller and Popescu, "Tight and rigorous error bounds for basic
+// building blocks of double-word arithmetic", ACM TOMS 44(2), 2017: the sum is their
+// sloppy sum without the final renormalisation (absolute error about 2^-47 (|x| + |y|),
+// the bound that matters for populations that are differenced later), the products are
+// the FMA-based ones with the lo*lo term dropped and one Fast2Sum.  Every operation is a
+// _rn intrinsic, so no contraction (--fmad) or re-association can break a transformation,
+// and the default and strict builds give identical results.
+#pragma once
+#include <cstdint>
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#endif
+
+namespace mflbm {
+
+struct ff {
+    float hi, lo;
+    ff() = default;
+    __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ explicit constexpr ff(float h) : hi(h), lo(0.0f) {}
+    // the FP64 value rounded to hi, the remainder rounded to lo (constant-folded for
+    // literals; on the host for run parameters)
+    __host__ __device__ explicit constexpr ff(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+};
+
+__host__ __device__ constexpr ff ff_const(double d) { return ff(d); }
+
+// the arithmetic needs the CUDA rounding intrinsics (device code, or a host build that
+// supplies them)
+#if defined(__CUDACC__) || defined(FFLOAT_HOST_INTRINSICS)
+
+__device__ __forceinline__ ff ff_fast2sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// x + y: TwoSum of the high parts, the low parts and the rounding error summed in FP32;
+// the result is left unnormalised (the next operation tolerates |lo| of a few ulp(hi)).
+__device__ __forceinline__ ff operator+(ff x, ff y) {
+    const ff s = ff_two_sum(x.hi, y.hi);
+    return ff{s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo))};
+}
+__device__ __forceinline__ ff operator-(ff x) { return ff{-x.hi, -x.lo}; }
+__device__ __forceinline__ ff operator-(ff x, ff y) { return x + (-y); }
+
+// x * y (normalised result)
+__device__ __forceinline__ ff operator*(ff x, ff y) {
+    const float ch = __fmul_rn(x.hi, y.hi);
+    float cl = __fmaf_rn(x.hi, y.hi, -ch);
+    cl = __fmaf_rn(x.hi, y.lo, cl);
+    cl = __fmaf_rn(x.lo, y.hi, cl);
+    return ff_fast2sum(ch, cl);
+}
+
+// x * k for an FP32 number k (normalised result)
+__device__ __forceinline__ ff ff_mulf(ff x, float k) {
+    const float ch = __fmul_rn(x.hi, k);
+    float cl = __fmaf_rn(x.hi, k, -ch);
+    cl = __fmaf_rn(x.lo, k, cl);
+    return ff_fast2sum(ch, cl);
+}
+
+// x * 2^n: exact
+__device__ __forceinline__ ff ff_pow2(ff x, float p2) { return ff{__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)}; }
+
+// FP64 -> double word on the integer pipe.  hi is the FP64 significand truncated to 24
+// bits (the exponent rebased from 1023 to 127), lo the next 23 bits rounded to nearest,
+// built exactly as (2^E + m ulp) - 2^E: |d - (hi + lo)| <= 2^-47 |d|.  Magnitudes outside
+// [2^-103, 2^128) (zero, FP32-subnormal range, infinities, NaN) take the hardware
+// conversion with lo = 0.
+__device__ __forceinline__ ff ff_from_f64(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const unsigned sgn = hw & 0x80000000u;
+    const unsigned a = hw & 0x7fffffffu;
+    const unsigned ed = a >> 20;
+    if (ed - 920u > 230u) return ff{__double2float_rn(d), 0.0f};
+    const float hi = __uint_as_float(__funnelshift_l(lw, a - (896u << 20), 3) | sgn);
+    const unsigned m = ((lw >> 6) & 0x7fffffu) + ((lw >> 5) & 1u);
+    const unsigned eb = (ed - 919u) << 23;
+    const float lo = __fsub_rn(__uint_as_float(eb + m), __uint_as_float(eb));
+    return ff{hi, __uint_as_float(__float_as_uint(lo) | sgn)};
+}
+
+// FP32 -> FP64 exactly on the integer pipe (normal numbers; zero, subnormals, infinities
+// and NaN take the hardware conversion)
+__device__ __forceinline__ double f64_of_f32(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned a = u & 0x7fffffffu;
+    if (a - 0x00800000u >= 0x7f000000u) return (double)x;
+    return __hiloint2double((int)(((a >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
+}
+
+// double word -> FP64: both parts exact, one FP64 add rounds the sum to nearest
+__device__ __forceinline__ double f64_of_ff(ff x) { return __dadd_rn(f64_of_f32(x.hi), f64_of_f32(x.lo)); }
+#endif
+
+}  // namespace mflbm

@@ -8,6 +8,7 @@
 //                      bit-identical to an IEEE FP64 restatement of the Fortran.
 // The host layer picks the flavour per context (mflbm_params.strict_fp).
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 #include "kernels_api.h"
 
@@ -122,17 +123,28 @@ template <> struct Store<__half> {
     }
 };
 
+// f64ff: FP64 storage whose collision sweep computes in double-word arithmetic on the
+// FP32 pipe (ffloat.cuh); the sweep converts on load and store.  Every other kernel of
+// this form runs on the storage as `double`.
+struct f64ff { double v; };
+template <> struct Store<f64ff> {
+    using R = ff;
+    static constexpr bool kDev = false;
+};
+
 // load/store of the collision sweep: deviations for the deviation forms, values else
 template <class S>
 __device__ __forceinline__ typename Store<S>::R ld_sweep(const S *p, int64_t o, int q, typename Store<S>::R inv) {
     using R = typename Store<S>::R;
-    if constexpr (Store<S>::kDev) return Store<S>::ldd(p, o, inv);
+    if constexpr (std::is_same<S, f64ff>::value) return ff_from_f64(p[o].v);
+    else if constexpr (Store<S>::kDev) return Store<S>::ldd(p, o, inv);
     else return Store<S>::ld(p, o, R(WREST(q)), inv);
 }
 template <class S>
 __device__ __forceinline__ void st_sweep(S *p, int64_t o, int q, typename Store<S>::R v, typename Store<S>::R sc) {
     using R = typename Store<S>::R;
-    if constexpr (Store<S>::kDev) Store<S>::std_(p, o, v, sc);
+    if constexpr (std::is_same<S, f64ff>::value) p[o].v = f64_of_ff(v);
+    else if constexpr (Store<S>::kDev) Store<S>::std_(p, o, v, sc);
     else Store<S>::st(p, o, v, R(WREST(q)), sc);
 }
 
@@ -384,6 +396,125 @@ __device__ __forceinline__ void mrt_collide_pairs(R (&ft)[19], R den_in, R fx, R
 }
 
 // ---------------------------------------------------------------------------------
+// The same singlephase collision (mrt_collide_pairs with FXY = false, OWN_DEN = true) in
+// double-word arithmetic (ffloat.cuh) for FP64 storage: every sum, difference and product
+// of the FP64 form, with multiplications by small integers as FP32-factor products and by
+// powers of two exactly.  With the force along z only, the forcing combinations of the
+// FP64 form reduce to +-F_z u_z (2 fux - fuy - fuz = -fuz, -2 fux + fuy + fuz = fuz,
+// fuy - fuz = -fuz, fuz - fuy = fuz).
+// ---------------------------------------------------------------------------------
+template <bool UNIT>
+__device__ __forceinline__ void mrt_collide_ff(ff (&ft)[19], const MrtFold<ff> &c) {
+    const ff f0 = ft[0];
+    const ff p1 = ft[1] + ft[2], d1 = ft[1] - ft[2];
+    const ff p2 = ft[3] + ft[4], d2 = ft[3] - ft[4];
+    const ff p3 = ft[5] + ft[6], d3 = ft[5] - ft[6];
+    const ff p4 = ft[7] + ft[10], d4 = ft[7] - ft[10];
+    const ff p5 = ft[8] + ft[9], d5 = ft[8] - ft[9];
+    const ff p6 = ft[11] + ft[14], d6 = ft[11] - ft[14];
+    const ff p7 = ft[12] + ft[13], d7 = ft[12] - ft[13];
+    const ff p8 = ft[15] + ft[18], d8 = ft[15] - ft[18];
+    const ff p9 = ft[16] + ft[17], d9 = ft[16] - ft[17];
+    const ff jx = d1 + d4 - d5 + d6 - d7;
+    const ff jy = d2 + d4 + d5 + d8 - d9;
+    const ff jz = d3 + d6 + d7 + d8 + d9;
+    const ff &ux = jx, &uy = jy;
+    const ff uz = jz + ff_pow2(c.fz, 0.5f);
+    const ff uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+    const ff u2 = uxx + uyy + uzz;
+    const ff fuz = c.fz * uz;
+    const ff a = p1 + p2 + p3;
+    const ff dxy = p4 + p5, dxz = p6 + p7, dyz = p8 + p9;
+    const ff ds = dxy + dxz + dyz;
+    const ff den = f0 + a + ds;
+    const ff qx = jx - ff_mulf(d1, 5.0f), qy = jy - ff_mulf(d2, 5.0f), qz = jz - ff_mulf(d3, 5.0f);
+    const ff tx = d4 - d5 - d6 + d7;
+    const ff ty = d8 - d4 - d5 - d9;
+    const ff tz = d6 + d7 - d8 - d9;
+    constexpr ff k19 = ff_const(1.0 / 19.0), k01 = ff_const(0.1);
+    const ff rho_s = den * k19;
+    ff e_s = c.e_den * den + c.e_u2 * u2 + c.e_f * fuz;
+    ff e2_s = c.e2_u2 * u2 + c.e2_f * fuz;
+    const ff jx_s = jx * k01, jy_s = jy * k01, jz_s = (jz + c.fz) * k01;
+    const ff qx_s = c.q_m * qx + c.q_u * ux;
+    const ff qy_s = c.q_m * qy + c.q_u * uy;
+    const ff qz_s = c.q_m * qz + c.q_u * uz + c.q_f * c.fz;
+    ff x3_s = c.x3_eq * (ff_mulf(uxx, 3.0f) - u2) - c.x3_f * fuz;
+    ff xi_s = c.xi_f * fuz;
+    ff w_s = c.w_eq * (uyy - uzz) - c.w_f * fuz;
+    ff wi_s = c.wi_f * fuz;
+    ff xy_s = c.o_eq * (ux * uy);
+    ff yz_s = c.o_eq * (uy * uz) + c.o_f * (c.fz * uy);
+    ff zx_s = c.o_eq * (ux * uz) + c.o_f * (c.fz * ux);
+    if constexpr (!UNIT) {
+        const ff m_e = ff_mulf(f0, -30.0f) - ff_mulf(a, 11.0f) + ff_pow2(ds, 8.0f);
+        const ff m_e2 = ff_mulf(f0, 12.0f) - ff_pow2(a, 4.0f) + ds;
+        const ff s6 = ff_pow2(p1, 2.0f) - p2 - p3;
+        const ff s7 = dxy + dxz - ff_pow2(dyz, 2.0f);
+        const ff s8 = p2 - p3, s9 = dxy - dxz;
+        e_s = e_s + c.e_m * m_e;
+        e2_s = e2_s + c.e2_m * m_e2;
+        x3_s = x3_s + c.x3_m * (s6 + s7);
+        xi_s = xi_s + c.xi_m * (s7 - ff_pow2(s6, 2.0f));
+        w_s = w_s + c.w_m * (s8 + s9);
+        wi_s = wi_s + c.wi_m * (s9 - ff_pow2(s8, 2.0f));
+        xy_s = xy_s + c.o_m * (p4 - p5);
+        yz_s = yz_s + c.o_m * (p8 - p9);
+        zx_s = zx_s + c.o_m * (p6 - p7);
+    }
+    const ff tx_s = c.t_m * tx, ty_s = c.t_m * ty, tz_s = c.t_m * tz;
+    // back-transform
+    const ff sum1 = rho_s - ff_mulf(e_s, 11.0f) - ff_pow2(e2_s, 4.0f);
+    const ff sum2 = ff_pow2(x3_s, 2.0f) - ff_pow2(xi_s, 4.0f);
+    const ff sum3 = w_s - ff_pow2(wi_s, 2.0f);
+    const ff sum4 = rho_s + ff_pow2(e_s, 8.0f) + e2_s;
+    const ff sum5 = jx_s + qx_s, sum6 = jy_s + qy_s, sum7 = jz_s + qz_s;
+    const ff sum8 = x3_s + xi_s, sum9 = w_s + wi_s;
+    ft[0] = rho_s - ff_mulf(e_s, 30.0f) + ff_mulf(e2_s, 12.0f);
+    {
+        const ff S = sum1 + sum2, A = jx_s - ff_pow2(qx_s, 4.0f);
+        ft[1] = S + A;
+        ft[2] = S - A;
+    }
+    {
+        const ff Syz = sum1 - ff_pow2(sum2, 0.5f);
+        const ff Sy = Syz + sum3, Ay = jy_s - ff_pow2(qy_s, 4.0f);
+        const ff Sz = Syz - sum3, Az = jz_s - ff_pow2(qz_s, 4.0f);
+        ft[3] = Sy + Ay;
+        ft[4] = Sy - Ay;
+        ft[5] = Sz + Az;
+        ft[6] = Sz - Az;
+    }
+    {
+        const ff b = sum4 + sum8 + sum9;
+        const ff Sp = b + xy_s, Ap = sum5 + sum6 + tx_s - ty_s;
+        const ff Sm = b - xy_s, Am = sum6 - sum5 - tx_s - ty_s;
+        ft[7] = Sp + Ap;
+        ft[10] = Sp - Ap;
+        ft[8] = Sm + Am;
+        ft[9] = Sm - Am;
+    }
+    {
+        const ff b = sum4 + sum8 - sum9;
+        const ff Sp = b + zx_s, Ap = sum5 + sum7 - tx_s + tz_s;
+        const ff Sm = b - zx_s, Am = sum7 - sum5 + tx_s + tz_s;
+        ft[11] = Sp + Ap;
+        ft[14] = Sp - Ap;
+        ft[12] = Sm + Am;
+        ft[13] = Sm - Am;
+    }
+    {
+        const ff b = sum4 - ff_pow2(sum8, 2.0f);
+        const ff Sp = b + yz_s, Ap = sum6 + sum7 + ty_s - tz_s;
+        const ff Sm = b - yz_s, Am = sum7 - sum6 - ty_s - tz_s;
+        ft[15] = Sp + Ap;
+        ft[18] = Sp - Ap;
+        ft[16] = Sm + Am;
+        ft[17] = Sm - Am;
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // singlephase kernel_even / kernel_odd (singlephase_3D/0.src/Kernel.F90:5-400).
 // One thread per interior node; solid nodes are skipped, so their slots carry the
 // implicit full-way bounce-back of the AA pattern.
@@ -409,14 +540,19 @@ __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_
         else
             ft[q] = ld_sweep<S>(f, (int64_t)OPP(q) * L.qs + c, q, inv_scale);
     }
+    if constexpr (std::is_same<R, ff>::value) {
+        mrt_collide_ff<UNIT>(ft, cf);
+    } else {
 #ifdef MFLBM_STRICT
-    const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
-                  ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
-    mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
+        const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
+                      ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+        mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi),
+                       R(P.s_t));
 #else
-    // force_z travels in the same coefficient set, already converted to R on the host
-    mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+        // force_z travels in the same coefficient set, already converted to R on the host
+        mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
 #endif
+    }
     const R sc = R(scale);
     if (ODD) {
         st_sweep<S>(f, c, 0, ft[0], sc);
@@ -1412,13 +1548,18 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
 #pragma unroll
         for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
     }
+    if constexpr (std::is_same<R, ff>::value) {
+        mrt_collide_ff<UNIT>(ft, cf);
+    } else {
 #ifdef MFLBM_STRICT
-    const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] + ft[12] +
-                  ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
-    mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi), R(P.s_t));
+        const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
+                      ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+        mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi),
+                       R(P.s_t));
 #else
-    mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+        mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
 #endif
+    }
     const R sc = R(scale);
     if (ODD) {
         st_sweep<S>(A, t, 0, ft[0], sc);
@@ -1448,6 +1589,7 @@ __global__ void __launch_bounds__(128) k_sp_list(S *__restrict__ A, const int64_
 template <class R> __device__ __forceinline__ const MrtFold<R> &ens_fold(const EnsArgs &a);
 template <> __device__ __forceinline__ const MrtFold<double> &ens_fold<double>(const EnsArgs &a) { return a.fold; }
 template <> __device__ __forceinline__ const MrtFold<float> &ens_fold<float>(const EnsArgs &a) { return a.fold32; }
+template <> __device__ __forceinline__ const MrtFold<ff> &ens_fold<ff>(const EnsArgs &a) { return a.foldff; }
 
 template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void ens_sweep(const EnsArgs &a) {

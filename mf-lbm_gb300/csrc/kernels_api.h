@@ -13,7 +13,7 @@ struct DevState {
     Layout L;
     StepParams P;
     int multiphase;
-    int prec;              // MFLBM_FP64 / FP32 / FP16
+    int prec;              // MFLBM_FP64 / FP32 / FP16 / FP64FF
     float ref, scale;      // FP16 deviation storage: rest density and scale
     double rk_weight2;     // 1/sqrt(2)/36 evaluated on the host
     void *f;               // species 1 PDFs (19 planes)
@@ -48,6 +48,7 @@ struct DevState {
     const int32_t *lseg;   // [nz+1] first fluid index of every z slice
     MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
     MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
+    MrtFold<ff> foldff;      // the same as double words (MFLBM_FP64FF collision)
     int unit;                // 1: fold_is_unit(fold), the collision skips the zero terms
 };
 

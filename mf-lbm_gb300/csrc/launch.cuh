@@ -22,6 +22,7 @@ inline bool mp_fp32(const DevState &st) { return st.multiphase && st.prec == MFL
 template <class R> const MrtFold<R> &fold_of(const DevState &st);
 template <> const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
 template <> const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
+template <> const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldff; }
 
 template <class S>
 int collide_list(const DevState &st, bool odd, cudaStream_t s) {
@@ -74,6 +75,7 @@ int collide(const DevState &st, bool odd, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: return collide_t<dfloat>(st, odd, s);
         case MFLBM_FP16: return collide_t<__half>(st, odd, s);
+        case MFLBM_FP64FF: return collide_t<f64ff>(st, odd, s);
         default: return collide_t<double>(st, odd, s);
     }
 }
@@ -374,6 +376,7 @@ int ens_run(const EnsArgs &a, int prec, int persistent, int grid, int block, cud
     switch (prec) {
         case MFLBM_FP32: return ens_run_t<dfloat>(a, persistent, grid, block, s);
         case MFLBM_FP16: return ens_run_t<__half>(a, persistent, grid, block, s);
+        case MFLBM_FP64FF: return ens_run_t<f64ff>(a, persistent, grid, block, s);
         default: return ens_run_t<double>(a, persistent, grid, block, s);
     }
 }
@@ -413,6 +416,7 @@ int ens_max_grid(int prec, int block) {
     switch (prec) {
         case MFLBM_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<dfloat, false>, block, 0); break;
         case MFLBM_FP16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<__half, false>, block, 0); break;
+        case MFLBM_FP64FF: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<f64ff, false>, block, 0); break;
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<double, false>, block, 0); break;
     }
     return e == cudaSuccess ? per * nsm : 0;

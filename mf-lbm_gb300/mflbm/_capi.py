@@ -25,6 +25,7 @@ MFLBM_FAILED = 3
 MFLBM_FP64 = 0
 MFLBM_FP32 = 1
 MFLBM_FP16 = 2
+MFLBM_FP64FF = 3
 MFLBM_NOALLOC_MAX_NZ = 16384
 
 ERROR_NAMES = {

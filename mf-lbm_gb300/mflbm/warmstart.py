@@ -85,6 +85,7 @@ class Net:
         self.mB = {k: torch.zeros_like(v) for k, v in self.B.items()}
         self.vB = {k: torch.zeros_like(v) for k, v in self.B.items()}
         self.step_count = 0
+        self.calls = 0       # C-ABI calls issued (each launches one kernel, split-K GEMMs two)
         nv = n ** 3
         maxk = max(_kp(cin) for _, cin, _, _ in self.specs)
         self.col = {}        # im2col of every layer (kept for the backward pass)
@@ -128,6 +129,7 @@ class Net:
 
     # ---- helpers -----------------------------------------------------------------------
     def _ck(self, rc, what):
+        self.calls += 1
         if rc:
             raise _capi.MflbmError(rc, what)
 
