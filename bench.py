@@ -34,11 +34,12 @@ for sub in ("mf-lbm_gb300", "oracle"):
 import numpy as np  # noqa: E402
 
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
-BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1}
+BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1, 4: 19 * 8 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
 BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1}
-# 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe
-DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff"}
+# 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe;
+# 4: double-word storage (hi + lo FP32 pair, 8 bytes) and the double-word collision
+DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff", 4: "ff"}
 
 
 def parse():
@@ -67,9 +68,10 @@ def parse():
                     help="c4: run the FP64 reference on the first K samples only (0: all)")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
     ap.add_argument("--porosity", type=float, default=0.22)
-    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="0 FP64, 1 FP32 (deviations for singlephase), 2 FP16 deviations, "
-                         "3 FP64 storage with the double-word collision (singlephase)")
+                         "3 FP64 storage with the double-word collision, 4 double-word storage and collision "
+                         "(3 and 4 singlephase)")
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
     ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -200,7 +202,7 @@ def convergence_study(args, case, device):
     from mflbm.permeability import run_to_steady
     out = {"tol": args.conv_tol, "check_every": 100, "forms": {}}
     base = None
-    for prec in (0, 3, 1, 2):
+    for prec in (0, 3, 4, 1, 2):
         p = copy.copy(case["params"])
         p.precision = prec
         with Solver(p) as sim:
@@ -622,7 +624,7 @@ def main():
 
     layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
     collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
-    elt = 8 if args.precision in (0, 3) else (4 if args.precision == 1 else 2)
+    elt = 8 if args.precision in (0, 3, 4) else (4 if args.precision == 1 else 2)
     state_bytes = (2 if p.multiphase else 1) * 19 * elt * (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
     bpl = BYTES_PER_LU_MP[args.precision] if p.multiphase else BYTES_PER_LU[args.precision]
     peaks = {}
@@ -638,7 +640,7 @@ def main():
         try:
             t = json.load(open(tf))
             # the double-word form moves the FP64 form's bytes
-            key = f"{DTYPE[0 if args.precision == 3 else args.precision]}_{layout}"
+            key = f"{DTYPE[0 if args.precision in (3, 4) else args.precision]}_{layout}"
             traffic = t[key] * pore if (key in t and not p.multiphase) else None
         except Exception:
             traffic = None

@@ -72,6 +72,8 @@ extern "C" {
 #define MFLBM_FP16 2   /* FP16 storage of scaled deviations from the rest state, FP32 collision */
 #define MFLBM_FP64FF 3 /* singlephase: FP64 storage, collision in double-word (two-FP32, about
                           48-bit) arithmetic on the FP32 pipe; every other kernel as MFLBM_FP64 */
+#define MFLBM_FF 4     /* singlephase: double-word storage (hi + lo FP32 pair per population,
+                          8 bytes, about 48 bits) and the double-word collision */
 
 /* PDF storage layout (no counterpart in the reference, which stores every cell).
  * DENSE: one plane per direction over the halo-1 box, as the reference's arrays.
@@ -101,7 +103,7 @@ typedef struct mflbm_params {
                                  singlephase: MRT_collision_parameter_preset               */
     int32_t porous_plate_cmd; /* 0 none, 1 block fluid 1, 2 block fluid 2                  */
     int32_t z_porous_plate;   /* plane index of the porous plate                           */
-    int32_t precision;        /* MFLBM_FP64 / MFLBM_FP32 / MFLBM_FP16 / MFLBM_FP64FF       */
+    int32_t precision;        /* MFLBM_FP64 / FP32 / FP16 / FP64FF / FF                    */
     int32_t strict_fp;        /* 1: no FMA contraction (bit-identical to an IEEE restatement) */
     int32_t device;           /* CUDA device ordinal                                       */
     int32_t layout;           /* PDF storage layout: MFLBM_LAYOUT_AUTO / _DENSE / _LIST        */

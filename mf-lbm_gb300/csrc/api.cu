@@ -107,8 +107,8 @@ int validate(const mflbm_params *p, std::string &err) {
             err = "multiphase supports MFLBM_FP64 and MFLBM_FP32 storage (FP16 deviations cannot hold a vanishing species)";
             return MFLBM_EINVAL;
         }
-        if (p->precision == MFLBM_FP64FF) {
-            err = "MFLBM_FP64FF (double-word collision) is singlephase";
+        if (p->precision == MFLBM_FP64FF || p->precision == MFLBM_FF) {
+            err = "MFLBM_FP64FF and MFLBM_FF (double-word collision) are singlephase";
             return MFLBM_EINVAL;
         }
         if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
@@ -138,7 +138,7 @@ int validate(const mflbm_params *p, std::string &err) {
         err = "Inlet pressure + outlet convective BC is not supported";
         return MFLBM_EINVAL;
     }
-    if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FP64FF) { err = "unknown precision"; return MFLBM_EINVAL; }
+    if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FF) { err = "unknown precision"; return MFLBM_EINVAL; }
     if (p->layout < MFLBM_LAYOUT_AUTO || p->layout > MFLBM_LAYOUT_LIST) { err = "unknown layout"; return MFLBM_EINVAL; }
     if (p->layout == MFLBM_LAYOUT_LIST && (p->multiphase || p->inlet_bc != 0 || p->outlet_bc != 0)) {
         err = "the fluid-list layout is singlephase without inlet/outlet boundary conditions";

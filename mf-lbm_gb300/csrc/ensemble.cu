@@ -147,7 +147,7 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
     if (common->multiphase) return efail(nullptr, MFLBM_EINVAL, "ensembles are singlephase");
     if (common->inlet_bc != 0 || common->outlet_bc != 0)
         return efail(nullptr, MFLBM_EINVAL, "ensembles have no inlet/outlet boundary conditions");
-    if (common->precision < MFLBM_FP64 || common->precision > MFLBM_FP64FF)
+    if (common->precision < MFLBM_FP64 || common->precision > MFLBM_FF)
         return efail(nullptr, MFLBM_EINVAL, "unknown precision");
     if (!(common->la_nu1 > 0.0)) return efail(nullptr, MFLBM_EINVAL, "la_nu1 must be positive");
     int ndev = 0;

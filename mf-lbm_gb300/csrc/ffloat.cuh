@@ -13,7 +13,7 @@
 // building blocks of double-word arithmetic", ACM TOMS 44(2), 2017: the sum is their
 // sloppy sum without the final renormalisation (absolute error about 2^-47 (|x| + |y|),
 // the bound that matters for populations that are differenced later), the products are
-// the FMA-based ones with the lo*lo term dropped and one Fast2Sum.  Every operation is a
+// the FMA-based ones with the lo*lo term dropped, also left unnormalised.  Every operation is a
 // _rn intrinsic, so no contraction (--fmad) or re-association can break a transformation,
 // and the default and strict builds give identical results.
 #pragma once
@@ -60,52 +60,60 @@ __device__ __forceinline__ ff operator+(ff x, ff y) {
 __device__ __forceinline__ ff operator-(ff x) { return ff{-x.hi, -x.lo}; }
 __device__ __forceinline__ ff operator-(ff x, ff y) { return x + (-y); }
 
-// x * y (normalised result)
+// x * y: TwoProd of the high parts with the cross terms folded into its error FMA; the
+// pair (ch, cl) is returned as it stands (|cl| is about ulp(ch), which every consumer
+// accepts, so the renormalising Fast2Sum would only cost three operations)
 __device__ __forceinline__ ff operator*(ff x, ff y) {
     const float ch = __fmul_rn(x.hi, y.hi);
     float cl = __fmaf_rn(x.hi, y.hi, -ch);
     cl = __fmaf_rn(x.hi, y.lo, cl);
     cl = __fmaf_rn(x.lo, y.hi, cl);
-    return ff_fast2sum(ch, cl);
+    return ff{ch, cl};
 }
 
-// x * k for an FP32 number k (normalised result)
+// x * k for an FP32 number k (same form)
 __device__ __forceinline__ ff ff_mulf(ff x, float k) {
     const float ch = __fmul_rn(x.hi, k);
     float cl = __fmaf_rn(x.hi, k, -ch);
     cl = __fmaf_rn(x.lo, k, cl);
-    return ff_fast2sum(ch, cl);
+    return ff{ch, cl};
 }
 
 // x * 2^n: exact
 __device__ __forceinline__ ff ff_pow2(ff x, float p2) { return ff{__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)}; }
 
-// FP64 -> double word on the integer pipe.  hi is the FP64 significand truncated to 24
-// bits (the exponent rebased from 1023 to 127), lo the next 23 bits rounded to nearest,
-// built exactly as (2^E + m ulp) - 2^E: |d - (hi + lo)| <= 2^-47 |d|.  Magnitudes outside
-// [2^-103, 2^128) (zero, FP32-subnormal range, infinities, NaN) take the hardware
-// conversion with lo = 0.
+// FP64 -> double word on the integer pipe only (selects, no FP64 instruction: GB300
+// executes FP64 conversions on its narrow FP64 pipe, and a predicated fallback would still
+// issue them).  hi is the FP64 significand truncated to 24 bits (the exponent rebased from
+// 1023 to 127), lo the next 23 bits rounded to nearest, built exactly as
+// (2^E + m ulp) - 2^E: |d - (hi + lo)| <= 2^-47 |d| for |d| in [2^-103, 2^128).
+// Below 2^-103 lo is 0 (below 2^-126 hi too: the value flushes to a signed zero); at and
+// above 2^128 hi is an infinity, NaN stays NaN.
 __device__ __forceinline__ ff ff_from_f64(double d) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(d);
     const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
     const unsigned sgn = hw & 0x80000000u;
     const unsigned a = hw & 0x7fffffffu;
     const unsigned ed = a >> 20;
-    if (ed - 920u > 230u) return ff{__double2float_rn(d), 0.0f};
-    const float hi = __uint_as_float(__funnelshift_l(lw, a - (896u << 20), 3) | sgn);
+    unsigned hb = __funnelshift_l(lw, a - (896u << 20), 3);
+    const bool nan = a > 0x7ff00000u || (a == 0x7ff00000u && lw != 0u);
+    hb = ed < 897u ? 0u : (ed > 1150u ? (nan ? 0x7fc00000u : 0x7f800000u) : hb);
     const unsigned m = ((lw >> 6) & 0x7fffffu) + ((lw >> 5) & 1u);
     const unsigned eb = (ed - 919u) << 23;
-    const float lo = __fsub_rn(__uint_as_float(eb + m), __uint_as_float(eb));
-    return ff{hi, __uint_as_float(__float_as_uint(lo) | sgn)};
+    float lo = __fsub_rn(__uint_as_float(eb + m), __uint_as_float(eb));
+    lo = (ed - 920u > 230u) ? 0.0f : lo;
+    return ff{__uint_as_float(hb | sgn), __uint_as_float(__float_as_uint(lo) | sgn)};
 }
 
-// FP32 -> FP64 exactly on the integer pipe (normal numbers; zero, subnormals, infinities
-// and NaN take the hardware conversion)
+// FP32 -> FP64 exactly on the integer pipe (selects only): normal numbers exactly, zero and
+// FP32 subnormals (below 2^-126) as a signed zero, infinities and NaN kept
 __device__ __forceinline__ double f64_of_f32(float x) {
     const unsigned u = __float_as_uint(x);
     const unsigned a = u & 0x7fffffffu;
-    if (a - 0x00800000u >= 0x7f000000u) return (double)x;
-    return __hiloint2double((int)(((a >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
+    unsigned h = (a >> 3) + (896u << 20);
+    h = a < 0x00800000u ? 0u : (a >= 0x7f800000u ? (0x7ff00000u | (a >> 3)) : h);
+    const unsigned l = a < 0x00800000u ? 0u : (u << 29);
+    return __hiloint2double((int)(h | (u & 0x80000000u)), (int)l);
 }
 
 // double word -> FP64: both parts exact, one FP64 add rounds the sum to nearest

@@ -71,6 +71,7 @@ struct dfloat { float x; };
 template <class S> struct Store;
 template <> struct Store<double> {
     using R = double;
+    using RS = R;   // arithmetic type of the collision sweep
     static constexpr bool kDev = false;
     __device__ __forceinline__ static R ld(const double *p, int64_t o, R, R) { return p[o]; }
     __device__ __forceinline__ static void st(double *p, int64_t o, R v, R, R) { p[o] = v; }
@@ -81,6 +82,7 @@ template <> struct Store<double> {
 };
 template <> struct Store<float> {
     using R = float;
+    using RS = R;   // arithmetic type of the collision sweep
     static constexpr bool kDev = false;
     __device__ __forceinline__ static R ld(const float *p, int64_t o, R, R) { return p[o]; }
     __device__ __forceinline__ static void st(float *p, int64_t o, R v, R, R) { p[o] = v; }
@@ -91,6 +93,7 @@ template <> struct Store<float> {
 };
 template <> struct Store<dfloat> {
     using R = float;
+    using RS = R;   // arithmetic type of the collision sweep
     static constexpr bool kDev = true;
     __device__ __forceinline__ static R ld(const dfloat *p, int64_t o, R w_ref, R) { return w_ref + p[o].x; }
     __device__ __forceinline__ static void st(dfloat *p, int64_t o, R v, R w_ref, R) { p[o].x = v - w_ref; }
@@ -105,6 +108,7 @@ template <> struct Store<dfloat> {
 };
 template <> struct Store<__half> {
     using R = float;
+    using RS = R;
     static constexpr bool kDev = true;
     // w_ref = w_q * ref density; sc = scale (store) / 1/scale (load)
     __device__ __forceinline__ static R ld(const __half *p, int64_t o, R w_ref, R inv_scale) {
@@ -129,21 +133,50 @@ template <> struct Store<__half> {
 struct f64ff { double v; };
 template <> struct Store<f64ff> {
     using R = ff;
+    using RS = ff;
     static constexpr bool kDev = false;
+};
+
+// ffs: double-word storage (two FP32 per population, hi + lo, about 48 significant bits;
+// 8 bytes like FP64), collision in double-word arithmetic without any conversion in the
+// sweep.  The boundary, monitor, initialisation and conversion kernels see FP64 values
+// (one FP64 add to join a pair, integer operations to split one).
+struct __align__(8) ffs { float hi, lo; };
+template <> struct Store<ffs> {
+    using R = double;
+    using RS = ff;
+    static constexpr bool kDev = false;
+    __device__ __forceinline__ static R ld(const ffs *p, int64_t o, R, R) {
+        const ffs v = p[o];
+        return f64_of_ff(ff{v.hi, v.lo});
+    }
+    __device__ __forceinline__ static void st(ffs *p, int64_t o, R v, R, R) {
+        const ff x = ff_from_f64(v);
+        p[o] = ffs{x.hi, x.lo};
+    }
+    __device__ __forceinline__ static R ldd(const ffs *p, int64_t o, R) { return ld(p, o, R(0), R(0)); }
+    __device__ __forceinline__ static void std_(ffs *p, int64_t o, R v, R) { st(p, o, v, R(0), R(0)); }
+    __device__ __forceinline__ static double ld64(const ffs *p, int64_t o, double, float) { return ld(p, o, 0.0, 0.0); }
+    __device__ __forceinline__ static void st64(ffs *p, int64_t o, double v, double, float) { st(p, o, v, 0.0, 0.0); }
 };
 
 // load/store of the collision sweep: deviations for the deviation forms, values else
 template <class S>
-__device__ __forceinline__ typename Store<S>::R ld_sweep(const S *p, int64_t o, int q, typename Store<S>::R inv) {
-    using R = typename Store<S>::R;
+__device__ __forceinline__ typename Store<S>::RS ld_sweep(const S *p, int64_t o, int q, typename Store<S>::RS inv) {
+    using R = typename Store<S>::RS;
     if constexpr (std::is_same<S, f64ff>::value) return ff_from_f64(p[o].v);
+    else if constexpr (std::is_same<S, ffs>::value) { const ffs v = p[o]; return ff{v.hi, v.lo}; }
     else if constexpr (Store<S>::kDev) return Store<S>::ldd(p, o, inv);
     else return Store<S>::ld(p, o, R(WREST(q)), inv);
 }
 template <class S>
-__device__ __forceinline__ void st_sweep(S *p, int64_t o, int q, typename Store<S>::R v, typename Store<S>::R sc) {
-    using R = typename Store<S>::R;
+__device__ __forceinline__ void st_sweep(S *p, int64_t o, int q, typename Store<S>::RS v, typename Store<S>::RS sc) {
+    using R = typename Store<S>::RS;
     if constexpr (std::is_same<S, f64ff>::value) p[o].v = f64_of_ff(v);
+    else if constexpr (std::is_same<S, ffs>::value) {
+        const ff n = ff_fast2sum(v.hi, v.lo);   // stored normalised
+        p[o] = ffs{n.hi, n.lo};
+    }
     else if constexpr (Store<S>::kDev) Store<S>::std_(p, o, v, sc);
     else Store<S>::st(p, o, v, R(WREST(q)), sc);
 }
@@ -524,9 +557,9 @@ __device__ __forceinline__ void mrt_collide_ff(ff (&ft)[19], const MrtFold<ff> &
 template <class S, bool ODD, bool UNIT>
 __global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
                                                  const Layout L, const StepParams P,
-                                                 const MrtFold<typename Store<S>::R> cf, const float scale) {
+                                                 const MrtFold<typename Store<S>::RS> cf, const float scale) {
     using St = Store<S>;
-    using R = typename St::R;
+    using R = typename St::RS;
     // one thread per fluid node: the sorted fluid-cell list keeps every lane busy
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) return;
@@ -1533,8 +1566,8 @@ __global__ void k_convert_out(double *__restrict__ dst, const S *__restrict__ sr
 template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                              const int64_t nf, const int64_t t, const StepParams &P,
-                                             const MrtFold<typename Store<S>::R> &cf, const float scale) {
-    using R = typename Store<S>::R;
+                                             const MrtFold<typename Store<S>::RS> &cf, const float scale) {
+    using R = typename Store<S>::RS;
     const R inv_scale = R(1.0f / scale);
     R ft[19];
     int32_t nbr[18];
@@ -1574,7 +1607,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
 template <class S, bool ODD, bool UNIT>
 __global__ void __launch_bounds__(128) k_sp_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                                  const int nf, const StepParams P,
-                                                 const MrtFold<typename Store<S>::R> cf, const float scale) {
+                                                 const MrtFold<typename Store<S>::RS> cf, const float scale) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
@@ -1598,7 +1631,7 @@ __device__ __forceinline__ void ens_sweep(const EnsArgs &a) {
         const EnsTile T = a.tiles[tile];
         if ((int)threadIdx.x < T.count)
             sp_list_node<S, ODD, UNIT>(reinterpret_cast<S *>(a.A), a.stride, a.nb, a.nf, (int64_t)T.start + threadIdx.x, a.P,
-                                 ens_fold<typename Store<S>::R>(a), a.scale);
+                                 ens_fold<typename Store<S>::RS>(a), a.scale);
     }
 }
 

@@ -13,7 +13,7 @@ struct DevState {
     Layout L;
     StepParams P;
     int multiphase;
-    int prec;              // MFLBM_FP64 / FP32 / FP16 / FP64FF
+    int prec;              // MFLBM_FP64 / FP32 / FP16 / FP64FF / FF
     float ref, scale;      // FP16 deviation storage: rest density and scale
     double rk_weight2;     // 1/sqrt(2)/36 evaluated on the host
     void *f;               // species 1 PDFs (19 planes)

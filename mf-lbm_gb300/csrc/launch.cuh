@@ -27,7 +27,7 @@ template <> const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldf
 template <class S>
 int collide_list(const DevState &st, bool odd, cudaStream_t s) {
     const unsigned nb = (unsigned)((st.nfl + 127) / 128);
-    const auto &cf = fold_of<typename Store<S>::R>(st);
+    const auto &cf = fold_of<typename Store<S>::RS>(st);
     if (st.unit) {
         if (odd) k_sp_list<S, true, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
         else k_sp_list<S, false, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
@@ -43,7 +43,7 @@ int collide_t(const DevState &st, bool odd, cudaStream_t s) {
     if (st.list) return collide_list<S>(st, odd, s);
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
-    const auto &cf = fold_of<typename Store<S>::R>(st);
+    const auto &cf = fold_of<typename Store<S>::RS>(st);
     if (st.unit) {
         if (odd) k_sp_step<S, true, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
         else k_sp_step<S, false, true><<<nb, 128, 0, s>>>(fs<S>(st), st.cells, st.ncell, st.L, st.P, cf, st.scale);
@@ -76,6 +76,7 @@ int collide(const DevState &st, bool odd, cudaStream_t s) {
         case MFLBM_FP32: return collide_t<dfloat>(st, odd, s);
         case MFLBM_FP16: return collide_t<__half>(st, odd, s);
         case MFLBM_FP64FF: return collide_t<f64ff>(st, odd, s);
+        case MFLBM_FF: return collide_t<ffs>(st, odd, s);
         default: return collide_t<double>(st, odd, s);
     }
 }
@@ -116,6 +117,7 @@ int wrap(const DevState &st, bool pull, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: n_launch = st.multiphase ? wrap_t<float>(st, pull, s) : wrap_t<dfloat>(st, pull, s); break;
         case MFLBM_FP16: n_launch = wrap_t<__half>(st, pull, s); break;
+        case MFLBM_FF: n_launch = wrap_t<ffs>(st, pull, s); break;
         default: n_launch = wrap_t<double>(st, pull, s); break;
     }
     if (st.multiphase && (st.P.jper || st.P.kper)) {
@@ -164,6 +166,7 @@ int boundary(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc, b
                                      : boundary_t<dfloat>(st, before_odd, inlet_bc, outlet_bc, open_z, s);
             break;
         case MFLBM_FP16: n_launch = boundary_t<__half>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
+        case MFLBM_FF: n_launch = boundary_t<ffs>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
         default: n_launch = boundary_t<double>(st, before_odd, inlet_bc, outlet_bc, open_z, s); break;
     }
     if (st.multiphase && st.P.porous_plate_cmd != 0 && st.P.z_porous_plate >= 1 && st.P.z_porous_plate <= st.L.nz) {
@@ -238,6 +241,7 @@ int monitor(const DevState &st, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: return st.multiphase ? monitor_t<float>(st, s) : monitor_t<dfloat>(st, s);
         case MFLBM_FP16: return monitor_t<__half>(st, s);
+        case MFLBM_FF: return monitor_t<ffs>(st, s);
         default: return monitor_t<double>(st, s);
     }
 }
@@ -283,6 +287,7 @@ int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: return st.multiphase ? init_t<float>(st, convec, s) : init_t<dfloat>(st, convec, s);
         case MFLBM_FP16: return init_t<__half>(st, convec, s);
+        case MFLBM_FF: return init_t<ffs>(st, convec, s);
         default: return init_t<double>(st, convec, s);
     }
 }
@@ -324,6 +329,7 @@ int convert_in(const DevState &st, int sp, int q, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: return st.multiphase ? convert_in_t<float>(st, sp, q, s) : convert_in_t<dfloat>(st, sp, q, s);
         case MFLBM_FP16: return convert_in_t<__half>(st, sp, q, s);
+        case MFLBM_FF: return convert_in_t<ffs>(st, sp, q, s);
         default: return convert_in_t<double>(st, sp, q, s);
     }
 }
@@ -332,6 +338,7 @@ int convert_out(const DevState &st, int sp, int q, cudaStream_t s) {
     switch (st.prec) {
         case MFLBM_FP32: return st.multiphase ? convert_out_t<float>(st, sp, q, s) : convert_out_t<dfloat>(st, sp, q, s);
         case MFLBM_FP16: return convert_out_t<__half>(st, sp, q, s);
+        case MFLBM_FF: return convert_out_t<ffs>(st, sp, q, s);
         default: return convert_out_t<double>(st, sp, q, s);
     }
 }
@@ -377,6 +384,7 @@ int ens_run(const EnsArgs &a, int prec, int persistent, int grid, int block, cud
         case MFLBM_FP32: return ens_run_t<dfloat>(a, persistent, grid, block, s);
         case MFLBM_FP16: return ens_run_t<__half>(a, persistent, grid, block, s);
         case MFLBM_FP64FF: return ens_run_t<f64ff>(a, persistent, grid, block, s);
+        case MFLBM_FF: return ens_run_t<ffs>(a, persistent, grid, block, s);
         default: return ens_run_t<double>(a, persistent, grid, block, s);
     }
 }
@@ -393,6 +401,7 @@ int ens_monitor(const EnsArgs &a, int prec, const int32_t *seg0, const int32_t *
     switch (prec) {
         case MFLBM_FP32: return ens_monitor_t<dfloat>(a, seg0, seg1, nseg, out, s);
         case MFLBM_FP16: return ens_monitor_t<__half>(a, seg0, seg1, nseg, out, s);
+        case MFLBM_FF: return ens_monitor_t<ffs>(a, seg0, seg1, nseg, out, s);
         default: return ens_monitor_t<double>(a, seg0, seg1, nseg, out, s);
     }
 }
@@ -403,6 +412,7 @@ int ens_init(const EnsArgs &a, int prec, cudaStream_t s) {
     switch (prec) {
         case MFLBM_FP32: k_list_init<dfloat><<<nb, 256, 0, s>>>(reinterpret_cast<dfloat *>(a.A), a.stride, a.scale); break;
         case MFLBM_FP16: k_list_init<__half><<<nb, 256, 0, s>>>(reinterpret_cast<__half *>(a.A), a.stride, a.scale); break;
+        case MFLBM_FF: k_list_init<ffs><<<nb, 256, 0, s>>>(reinterpret_cast<ffs *>(a.A), a.stride, a.scale); break;
         default: k_list_init<double><<<nb, 256, 0, s>>>(reinterpret_cast<double *>(a.A), a.stride, a.scale); break;
     }
     return 1;
@@ -417,6 +427,7 @@ int ens_max_grid(int prec, int block) {
         case MFLBM_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<dfloat, false>, block, 0); break;
         case MFLBM_FP16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<__half, false>, block, 0); break;
         case MFLBM_FP64FF: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<f64ff, false>, block, 0); break;
+        case MFLBM_FF: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<ffs, false>, block, 0); break;
         default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ens_persistent<double, false>, block, 0); break;
     }
     return e == cudaSuccess ? per * nsm : 0;
@@ -444,6 +455,7 @@ int init_velocity(const DevState &st, const double *rho, int rest_base, cudaStre
     switch (st.prec) {
         case MFLBM_FP32: return init_velocity_t<dfloat>(st, rho, rest_base, s);
         case MFLBM_FP16: return init_velocity_t<__half>(st, rho, rest_base, s);
+        case MFLBM_FF: return init_velocity_t<ffs>(st, rho, rest_base, s);
         default: return init_velocity_t<double>(st, rho, rest_base, s);
     }
 }

@@ -26,6 +26,7 @@ MFLBM_FP64 = 0
 MFLBM_FP32 = 1
 MFLBM_FP16 = 2
 MFLBM_FP64FF = 3
+MFLBM_FF = 4
 MFLBM_NOALLOC_MAX_NZ = 16384
 
 ERROR_NAMES = {

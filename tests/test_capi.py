@@ -55,6 +55,7 @@ def _create(**kw):
     (dict(nx=2), "dimensions"),
     (dict(precision=5), "precision"),
     (dict(multiphase=1, precision=3), "double-word collision"),
+    (dict(multiphase=1, precision=4), "double-word collision"),
 ])
 def test_invalid_parameters_rejected_before_any_device_work(kw, needle):
     rc, msg = _create(**kw)

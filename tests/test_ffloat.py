@@ -2,7 +2,8 @@
 (mf-lbm_gb300/csrc/ffloat.cuh), built for the host with the CUDA rounding intrinsics
 mapped onto IEEE operations, against exact rational arithmetic:
   - FP64 -> (hi, lo) on the integer pipe: |d - (hi + lo)| <= 2^-47 |d|
-  - FP32 -> FP64 on the integer pipe: exact, special values through the fallback
+  - FP32 -> FP64 on the integer pipe: exact for normal numbers, subnormals flush to a
+    signed zero, infinities and NaN kept
   - (hi, lo) -> FP64: hi + lo rounded once
   - sum, difference: absolute error <= 2^-46 (|x| + |y|), also for unnormalised inputs
   - products: relative error <= 2^-45; power-of-two scaling exact
@@ -72,11 +73,14 @@ def test_split_bound_and_round_trip(lib):
 
 
 def test_split_special_values(lib):
-    d = np.array([0.0, -0.0, 1e-35, -1e-40, 1e300, np.inf, -np.inf, np.nan])
+    d = np.array([0.0, -0.0, 1e-35, -1e-40, 1e300, np.inf, -np.inf, np.nan, -np.nan, 2.0 ** -126, 2.0 ** -127])
     hi, lo = split(lib, d)
-    assert np.array_equal(hi[:2], [0.0, 0.0]) and np.all(lo == 0)
-    assert hi[2] == np.float32(1e-35) and hi[3] == np.float32(-1e-40)
-    assert np.isposinf(hi[4]) and np.isposinf(hi[5]) and np.isneginf(hi[6]) and np.isnan(hi[7])
+    assert np.array_equal(hi[:2], [0.0, 0.0]) and np.array_equal(np.signbit(hi[:2]), [False, True])
+    assert np.all(lo[:7] == 0) and np.all(lo[9:] == 0)
+    assert abs(float(hi[2]) - 1e-35) <= 2.0 ** -23 * 1e-35          # hi truncated, lo below range
+    assert hi[3] == 0.0 and np.signbit(hi[3])                         # below 2^-126: signed zero
+    assert np.isposinf(hi[4]) and np.isposinf(hi[5]) and np.isneginf(hi[6]) and np.isnan(hi[7]) and np.isnan(hi[8])
+    assert hi[9] == np.float32(2.0 ** -126) and hi[10] == 0.0
 
 
 def test_f32_to_f64_exact(lib):
@@ -89,6 +93,8 @@ def test_f32_to_f64_exact(lib):
     lib.ffh_f32_to_f64(x, out, x.size)
     with np.errstate(invalid="ignore"):
         ref = x.astype(np.float64)
+    # FP32 subnormals flush to a signed zero
+    ref = np.where(np.abs(ref) < 2.0 ** -126, np.copysign(0.0, ref), ref)
     same = (out == ref) | (np.isnan(out) & np.isnan(ref))
     assert same.all()
     assert np.array_equal(np.signbit(out), np.signbit(ref))

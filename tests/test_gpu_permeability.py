@@ -5,8 +5,8 @@ FP64 (default FMA build): same number of steps to |du|/u < 1e-7 and |dk|/k <= 1e
 FP32 deviation storage: converges to 1e-7, |dk|/k <= 1e-3 against FP64.
 FP16 deviation storage: its rounding noise floor sits above 1e-7, so it is run to 1e-5;
 its 11-bit significand leaves a systematic k error of several 1e-3: |dk|/k <= 2e-2.
-FP64 storage with the double-word collision: the same number of steps as FP64 (+-100,
-one check interval) and |dk|/k <= 1e-8.
+FP64 storage with the double-word collision, and double-word storage with it: the same
+number of steps as FP64 (+-100, one check interval) and |dk|/k <= 1e-8.
 """
 import numpy as np
 import pytest
@@ -48,12 +48,13 @@ def test_fp64_matches_oracle(fp64):
     assert abs(fp64.k - ref.k) / abs(ref.k) <= 1e-9
 
 
-def test_double_word_collision_matches_fp64(fp64):
-    case = _case(3)
+@pytest.mark.parametrize("precision", [3, 4])
+def test_double_word_collision_matches_fp64(fp64, precision):
+    case = _case(precision)
     with Solver(case["params"]) as sim:
         r = _solve(sim, case)
     err = abs(r.k - fp64.k) / abs(fp64.k)
-    print(f"double-word collision: k {r.k:.15e} vs fp64 {fp64.k:.15e} rel {err:.3e} steps {r.steps} vs {fp64.steps}")
+    print(f"double-word precision {precision}: k {r.k:.15e} vs fp64 {fp64.k:.15e} rel {err:.3e} steps {r.steps} vs {fp64.steps}")
     assert r.converged and r.status == 0
     assert abs(r.steps - fp64.steps) <= 100
     assert err <= 1e-8
