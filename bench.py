@@ -360,6 +360,9 @@ def warmstart_study(args):
         infer = time.perf_counter() - t1
         w64, _, set64 = ws.solve(wg, precision=0, tol=args.conv_tol, init_u=u, init_rho=rho, nu=nu, fz=fz)
         w32, _, set32 = ws.solve(wg, precision=1, tol=args.conv_tol, init_u=u, init_rho=rho, nu=nu, fz=fz)
+        # the double-word storage form: FP64-grade k (about 1e-10 of FP64) on the FP32 pipe
+        rff = ws.solve(wg, precision=4, tol=args.conv_tol, nu=nu, fz=fz)[0]
+        wff, _, setff = ws.solve(wg, precision=4, tol=args.conv_tol, init_u=u, init_rho=rho, nu=nu, fz=fz)
         # ablation: the MRT rest state without the predicted velocity
         b32, _, setb = ws.solve(wg, precision=1, tol=args.conv_tol, rest_base=True, nu=nu, fz=fz)
         k0 = nu * float(np.mean(u[2])) / fz
@@ -370,6 +373,9 @@ def warmstart_study(args):
                      "k_err_fp64_warm": abs(w64.k - ref.k) / ref.k,
                      "steps_fp32_warm": w32.steps, "s_fp32_warm": w32.seconds + infer + set32,
                      "k_err_fp32_warm": abs(w32.k - ref.k) / ref.k,
+                     "steps_ff_rest": rff.steps, "s_ff_rest": rff.seconds, "k_err_ff_rest": abs(rff.k - ref.k) / ref.k,
+                     "steps_ff_warm": wff.steps, "s_ff_warm": wff.seconds + infer + setff,
+                     "k_err_ff_warm": abs(wff.k - ref.k) / ref.k,
                      "steps_fp32_mrt_rest": b32.steps, "s_fp32_mrt_rest": b32.seconds + setb,
                      "k_err_fp32_mrt_rest": abs(b32.k - ref.k) / ref.k,
                      "k_err_prediction_only": abs(k0 - ref.k) / ref.k, "inference_s": infer})
@@ -390,6 +396,8 @@ def warmstart_study(args):
                        "steps_ratio_fp32_mrt_rest_over_fp32_warm": agg("steps_fp32_mrt_rest") / agg("steps_fp32_warm"),
                        "time_ratio_fp64_rest_over_fp64_warm": agg("s_fp64_rest") / agg("s_fp64_warm"),
                        "time_ratio_fp64_rest_over_fp32_rest": agg("s_fp64_rest") / agg("s_fp32_rest"),
+                       "time_ratio_fp64_rest_over_ff_warm": agg("s_fp64_rest") / agg("s_ff_warm"),
+                       "max_k_err_ff_warm": agg("k_err_ff_warm", np.max),
                        "samples": rows}}
     print(json.dumps(line), flush=True)
     return 0

@@ -31,6 +31,8 @@ LIB = os.path.join(OUT_DIR, "libmflbm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr"]
+# extra nvcc flags for tuning builds (e.g. MFLBM_NVCC_FLAGS="-DMFLBM_FF_MIN_BLOCKS=5")
+EXTRA = os.environ.get("MFLBM_NVCC_FLAGS", "").split()
 UNITS = {
     "api.o": ("api.cu", []),
     "kernels_fast.o": ("kernels_fast.cu", []),
@@ -70,7 +72,7 @@ def build(force=False, verbose=False):
     exe = nvcc()
     procs = []
     for obj, (src, extra) in UNITS.items():
-        cmd = [exe, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", os.path.join(BUILD_DIR, obj)]
+        cmd = [exe, *ARCH, *COMMON, *extra, *EXTRA, "-c", os.path.join(CSRC, src), "-o", os.path.join(BUILD_DIR, obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         procs.append((subprocess.Popen(cmd), obj))

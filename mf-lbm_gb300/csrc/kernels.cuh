@@ -160,6 +160,19 @@ template <> struct Store<ffs> {
     __device__ __forceinline__ static void st64(ffs *p, int64_t o, double v, double, float) { st(p, o, v, 0.0, 0.0); }
 };
 
+// Resident 128-thread blocks per SM that the sweep kernels ask the register allocator
+// for.  The double-word storage sweep issues about 1,500 instructions per node and waits
+// on memory between them: its natural 96 registers leave 5 blocks per SM; a cap of 72
+// registers gives 7 at about 70 bytes of spill, measured 7 % faster on GB300 (5 / 6 / 7
+// blocks: 14.0 / 14.5 / 15.0 GLUPS on a 256^3 packing).  The FP64-storage double-word
+// sweep is issue-bound (conversions) and gained nothing; the other forms keep the
+// allocator's choice.
+#ifndef MFLBM_FF_MIN_BLOCKS
+#define MFLBM_FF_MIN_BLOCKS 7
+#endif
+template <class S> struct SweepOcc { static constexpr int kMinBlocks = 1; };
+template <> struct SweepOcc<ffs> { static constexpr int kMinBlocks = MFLBM_FF_MIN_BLOCKS; };
+
 // load/store of the collision sweep: deviations for the deviation forms, values else
 template <class S>
 __device__ __forceinline__ typename Store<S>::RS ld_sweep(const S *p, int64_t o, int q, typename Store<S>::RS inv) {
@@ -555,7 +568,7 @@ __device__ __forceinline__ void mrt_collide_ff(ff (&ft)[19], const MrtFold<ff> &
 // even: ft_q <- f_opp(q)(x)  ... f_q(x) <- ft_q
 // ---------------------------------------------------------------------------------
 template <class S, bool ODD, bool UNIT>
-__global__ void __launch_bounds__(128) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
+__global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__restrict__ f, const int32_t *__restrict__ cells, const int ncell,
                                                  const Layout L, const StepParams P,
                                                  const MrtFold<typename Store<S>::RS> cf, const float scale) {
     using St = Store<S>;
@@ -1605,7 +1618,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
 }
 
 template <class S, bool ODD, bool UNIT>
-__global__ void __launch_bounds__(128) k_sp_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
+__global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                                  const int nf, const StepParams P,
                                                  const MrtFold<typename Store<S>::RS> cf, const float scale) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
