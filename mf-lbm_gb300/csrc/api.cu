@@ -33,6 +33,8 @@ struct mflbm_ctx {
     bool have_geometry = false;
     bool open_z = false;
     int64_t cells_cap = 0;
+    int64_t gn_cap = 0, gc_cap = 0, sbc_cap = 0;  // capacities of the colour-gradient lists
+    SolidBndC *sbc_buf = nullptr;
     void *pdf = nullptr;          // PDF storage (dense planes or fluid-list arrays)
     size_t pdf_bytes = 0;
     std::vector<void *> list_bufs;  // neighbour table, cell map, link table, slice starts
@@ -429,6 +431,8 @@ void mflbm_destroy(mflbm_ctx *c) {
     delete c;
 }
 
+static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid);
+
 int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid,
                            const mflbm_fluid_bnd *fluid, int32_t n_fluid, const double *w_in) {
     if (!c) return MFLBM_EINVAL;
@@ -547,8 +551,83 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     if (n_fluid) CK(c, cudaMemcpy((void *)c->st.fb, fb.data(), sizeof(FluidBnd) * n_fluid, cudaMemcpyHostToDevice));
     c->st.ns = n_solid;
     c->st.nf = n_fluid;
+    if (p.multiphase) {
+        int r = gradient_lists(c, walls, solid, n_solid);
+        if (r) return r;
+    }
     CK(c, cudaDeviceSynchronize());
     c->have_geometry = true;
+    return MFLBM_OK;
+}
+
+// Device lists of the colour-gradient step (multiphase): the fluid cells that need normals
+// ([-1, n+2]^3, walls != 1) and curvature ([1, n]^3, walls == 0), packed, for the
+// fluid-cell kernels of the default build; and the compact solid-boundary records when every
+// neighbour list is ascending (the order of the sums is then the set-bit order).  The
+// gradient fields are zeroed: cells the lists skip keep those zeros, as the full-box
+// kernels would write them.
+static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid) {
+    const mflbm_params &p = c->p;
+    const Layout &L = c->st.L;
+    const size_t fe = (size_t)c->st.felt;
+    CK(c, cudaMemsetAsync(c->st.cnx, 0, fe * n2(p), c->stream));
+    CK(c, cudaMemsetAsync(c->st.cny, 0, fe * n2(p), c->stream));
+    CK(c, cudaMemsetAsync(c->st.cnz, 0, fe * n2(p), c->stream));
+    CK(c, cudaMemsetAsync(c->st.cnorm, 0, fe * n2(p), c->stream));
+    CK(c, cudaMemsetAsync(c->st.curv, 0, fe * n1(p), c->stream));
+    c->st.glist = 0;
+    c->st.n_gcell_n = 0;
+    c->st.n_gcell_c = 0;
+    c->st.sbc = nullptr;
+    if (!cell_packable(p.nx, p.ny, p.nz)) return MFLBM_OK;  // the full-box kernels serve
+    std::vector<uint32_t> gn, gc;
+    for (int k = -1; k <= p.nz + 2; ++k)
+        for (int j = -1; j <= p.ny + 2; ++j)
+            for (int i = -1; i <= p.nx + 2; ++i) {
+                const int8_t w = walls[L.i2(i, j, k)];
+                if (w != 1) gn.push_back(pack_cell(i, j, k));
+                if (w == 0 && i >= 1 && i <= p.nx && j >= 1 && j <= p.ny && k >= 1 && k <= p.nz)
+                    gc.push_back(pack_cell(i, j, k));
+            }
+    auto put = [&](const std::vector<uint32_t> &v, const uint32_t **dst, int64_t &cap) -> int {
+        if (v.empty()) return MFLBM_OK;
+        if ((int64_t)v.size() > cap) {
+            uint32_t *d = nullptr;
+            int r = dalloc(c, &d, (int64_t)v.size());
+            if (r) return r;
+            *dst = d;
+            cap = (int64_t)v.size();
+        }
+        CK(c, cudaMemcpy((void *)*dst, v.data(), sizeof(uint32_t) * v.size(), cudaMemcpyHostToDevice));
+        return MFLBM_OK;
+    };
+    int r;
+    if ((r = put(gn, &c->st.gcell_n, c->gn_cap))) return r;
+    if ((r = put(gc, &c->st.gcell_c, c->gc_cap))) return r;
+    c->st.n_gcell_n = (int)gn.size();
+    c->st.n_gcell_c = (int)gc.size();
+    c->st.glist = 1;
+    std::vector<SolidBndC> sc((size_t)n_solid);
+    for (int32_t t = 0; t < n_solid; ++t) {
+        const mflbm_solid_bnd &s = solid[t];
+        uint32_t m = 0;
+        int prev = 0;
+        for (int n = 0; n < s.i_fluid_num; ++n) {
+            const int d = s.neighbor_list[n];
+            if (d <= prev) return MFLBM_OK;  // not ascending: keep the record kernels
+            prev = d;
+            m |= 1u << (d - 1);
+        }
+        sc[t] = SolidBndC{pack_cell(s.ix, s.iy, s.iz), m, s.la_weight};
+    }
+    if (n_solid > 0) {
+        if (n_solid > c->sbc_cap) {
+            if ((r = dalloc(c, &c->sbc_buf, n_solid))) return r;
+            c->sbc_cap = n_solid;
+        }
+        CK(c, cudaMemcpy(c->sbc_buf, sc.data(), sizeof(SolidBndC) * n_solid, cudaMemcpyHostToDevice));
+        c->st.sbc = c->sbc_buf;
+    }
     return MFLBM_OK;
 }
 

@@ -86,6 +86,28 @@ struct SolidBnd {  // identical to mflbm_solid_bnd (96 bytes)
     double la_weight;
 };
 
+// A cell of the halo-2 neighbourhood [-2, 2045] x [-2, 2045] x [-2, 1021] packed in 32 bits
+// (device lists of the multiphase colour-gradient kernels)
+__host__ __device__ constexpr uint32_t pack_cell(int i, int j, int k) {
+    return (uint32_t)(i + 2) | ((uint32_t)(j + 2) << 11) | ((uint32_t)(k + 2) << 22);
+}
+__host__ __device__ __forceinline__ void unpack_cell(uint32_t c, int &i, int &j, int &k) {
+    i = (int)(c & 0x7ffu) - 2;
+    j = (int)((c >> 11) & 0x7ffu) - 2;
+    k = (int)(c >> 22) - 2;
+}
+__host__ __device__ constexpr bool cell_packable(int nx, int ny, int nz) {
+    return nx + 5 <= 2047 && ny + 5 <= 2047 && nz + 5 <= 1023;
+}
+
+// compact solid-boundary record: packed cell, bit (d-1) set for every fluid-neighbour
+// direction d, and the record's la_weight (16 bytes)
+struct SolidBndC {
+    uint32_t ijk;
+    uint32_t mask;
+    double la_weight;
+};
+
 // Folded MRT coefficients (see mrt_collide_pairs in kernels.cuh): every post-collision
 // moment, already divided by its back-transform norm, is a linear combination of the
 // pre-collision moment, its equilibrium term and its forcing term.

@@ -1210,20 +1210,57 @@ __global__ void k_extrap_phi(T *__restrict__ phi, const SolidBnd *__restrict__ s
     phi[L.i4(s.ix, s.iy, s.iz)] = acc / T(s.la_weight);
 }
 
-// ISO4 gradient and unit normal over [1-2, n+2]^3 (:33-79)
+// The same two extrapolations over the compact solid-boundary records (SolidBndC: packed
+// cell, bit mask of the fluid-neighbour directions, la_weight): 16 bytes read per node
+// instead of 96.  The set bits are visited in ascending direction order, which is the order
+// of the neighbour list whenever the context builds these records, so the sums are the
+// same operations in the same order.
 template <class T>
-__global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, const int8_t *__restrict__ walls,
-                                                 T *__restrict__ cnx, T *__restrict__ cny,
-                                                 T *__restrict__ cnz, T *__restrict__ cnorm, const Layout L) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
-    const int k = blockIdx.z - 1;
-    if (i > L.nx + 2 || j > L.ny + 2) return;
-    const int64_t id = L.i2(i, j, k);
-    if (walls[id] == 1) {  // the reference zeroes normals at wall nodes (Phase_gradient.F90:65-69)
-        cnx[id] = T(0.0); cny[id] = T(0.0); cnz[id] = T(0.0); cnorm[id] = T(0.0);
-        return;
+__global__ void k_extrap_phi_c(T *__restrict__ phi, const SolidBndC *__restrict__ sb, int ns, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    const SolidBndC s = sb[t];
+    int ix, iy, iz;
+    unpack_cell(s.ijk, ix, iy, iz);
+    T acc = T(0.0);
+    for (uint32_t m = s.mask; m; m &= m - 1u) {
+        const int ie = __ffs((int)m);
+        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
+        acc = acc + phi[L.i4(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie])] * w;
     }
+    phi[L.i4(ix, iy, iz)] = acc / T(s.la_weight);
+}
+
+template <class T>
+__global__ void k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+                                   const SolidBndC *__restrict__ sb, int ns, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    const SolidBndC s = sb[t];
+    int ix, iy, iz;
+    unpack_cell(s.ijk, ix, iy, iz);
+    if (!(ix >= 0 && ix <= L.nx + 1 && iy >= 0 && iy <= L.ny + 1 && iz >= 0 && iz <= L.nz + 1)) return;
+    T ax = T(0.0), ay = T(0.0), az = T(0.0);
+    for (uint32_t m = s.mask; m; m &= m - 1u) {
+        const int ie = __ffs((int)m);
+        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
+        const int64_t nb = L.i2(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie]);
+        ax = ax + cnx[nb] * w;
+        ay = ay + cny[nb] * w;
+        az = az + cnz[nb] * w;
+    }
+    const int64_t id = L.i2(ix, iy, iz);
+    const T lw = T(s.la_weight);
+    cnx[id] = ax / lw;
+    cny[id] = ay / lw;
+    cnz[id] = az / lw;
+}
+
+// ISO4 gradient and unit normal of one cell (:33-79)
+template <class T>
+__device__ __forceinline__ void normals_at(const T *__restrict__ phi, int i, int j, int k, int64_t id,
+                                           T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+                                           T *__restrict__ cnorm, const Layout &L) {
     auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
     const T c1 = T(ISO4_1), c2 = T(ISO4_2);
     T gx = c1 * (P(1, 0, 0) - P(-1, 0, 0)) +
@@ -1244,6 +1281,41 @@ __global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, cons
 #endif
     }
     cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
+}
+
+// over [1-2, n+2]^3, every cell
+template <class T>
+__global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, const int8_t *__restrict__ walls,
+                                                 T *__restrict__ cnx, T *__restrict__ cny,
+                                                 T *__restrict__ cnz, T *__restrict__ cnorm, const Layout L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > L.nx + 2 || j > L.ny + 2) return;
+    const int64_t id = L.i2(i, j, k);
+    if (walls[id] == 1) {  // the reference zeroes normals at wall nodes (Phase_gradient.F90:65-69)
+        cnx[id] = T(0.0); cny[id] = T(0.0); cnz[id] = T(0.0); cnorm[id] = T(0.0);
+        return;
+    }
+    normals_at<T>(phi, i, j, k, id, cnx, cny, cnz, cnorm, L);
+}
+
+// Fluid-cell forms of k_normals / k_curvature (default build): one thread per entry of a
+// list of the cells that need the value, packed as (i+2) | (j+2) << 11 | (k+2) << 22 in
+// ascending cell order (pack_cell in common.cuh).  Wall cells are never visited: they keep the zeros the context
+// wrote when the geometry was set (the full-box kernels write the same zeros each call),
+// and solid-boundary cells receive their extrapolated normals as before.  At porosity 0.22
+// this skips about two thirds of the cells, and every lane of a warp does work.
+
+template <class T>
+__global__ void __launch_bounds__(256) k_normals_list(const T *__restrict__ phi, const uint32_t *__restrict__ cl, int n,
+                                                      T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+                                                      T *__restrict__ cnorm, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_cell(cl[t], i, j, k);
+    normals_at<T>(phi, i, j, k, L.i2(i, j, k), cnx, cny, cnz, cnorm, L);
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
@@ -1308,23 +1380,11 @@ __global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__
     cnz[id] = az / lw;
 }
 
-// curvature over [1, n]^3 (:113-201)
+// curvature of one cell (:113-201)
 template <class T>
-__global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                                   const T *__restrict__ cnz, T *__restrict__ curv,
-                                                   const int8_t *__restrict__ walls, const Layout L) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > L.nx || j > L.ny) return;
-#ifndef MFLBM_STRICT
-    // curv is read only at fluid nodes (collision, compute_macro_vars masks walls); the
-    // default build leaves 0 at wall nodes instead of the reference's unused value
-    if (walls[L.i2(i, j, k)] != 0) {
-        curv[L.i1(i, j, k)] = T(0.0);
-        return;
-    }
-#endif
+__device__ __forceinline__ void curvature_at(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                             const T *__restrict__ cnz, T *__restrict__ curv, int i, int j, int k,
+                                             const Layout &L) {
     const T c1 = T(ISO4_1), c2 = T(ISO4_2);
     auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
     auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
@@ -1350,6 +1410,37 @@ __global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, co
     const T cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
     curv[L.i1(i, j, k)] = (cx * cx - T(1.0)) * kxx + (cy * cy - T(1.0)) * kyy + (cz * cz - T(1.0)) * kzz + cx * cy * (kxy + kyx) +
                           cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz);
+}
+
+// over [1, n]^3, every cell
+template <class T>
+__global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                                   const T *__restrict__ cnz, T *__restrict__ curv,
+                                                   const int8_t *__restrict__ walls, const Layout L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > L.nx || j > L.ny) return;
+#ifndef MFLBM_STRICT
+    // curv is read only at fluid nodes (collision, compute_macro_vars masks walls); the
+    // default build leaves 0 at wall nodes instead of the reference's unused value
+    if (walls[L.i2(i, j, k)] != 0) {
+        curv[L.i1(i, j, k)] = T(0.0);
+        return;
+    }
+#endif
+    curvature_at<T>(cnx, cny, cnz, curv, i, j, k, L);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_curvature_list(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                                        const T *__restrict__ cnz, T *__restrict__ curv,
+                                                        const uint32_t *__restrict__ cl, int n, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_cell(cl[t], i, j, k);
+    curvature_at<T>(cnx, cny, cnz, curv, i, j, k, L);
 }
 
 // ---------------------------------------------------------------------------------

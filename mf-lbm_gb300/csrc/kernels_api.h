@@ -29,6 +29,12 @@ struct DevState {
     double *w_in;          // (nx+2)(ny+2)
     double *fconv, *gconv, *phiconv;
     const SolidBnd *sb;
+    const SolidBndC *sbc;     // compact form of sb (nullptr: a neighbour list is not ascending)
+    int glist;                // 1: the packed fluid-cell lists below are valid
+    const uint32_t *gcell_n;  // fluid cells of [-1, n+2]^3 (walls != 1), packed: normals
+    int n_gcell_n;
+    const uint32_t *gcell_c;  // fluid cells of [1, n]^3 (walls == 0), packed: curvature
+    int n_gcell_c;
     int ns;
     const FluidBnd *fb;
     int nf;

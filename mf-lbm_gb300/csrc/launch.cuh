@@ -192,7 +192,17 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
     T *phi = fld<T>(st.phi), *cnx = fld<T>(st.cnx), *cny = fld<T>(st.cny), *cnz = fld<T>(st.cnz);
     T *cnorm = fld<T>(st.cnorm), *curv = fld<T>(st.curv);
     int n_launch = 2 + (st.ns > 0 ? 2 : 0) + (st.nf > 0 ? 1 : 0);
-    if (st.ns > 0) k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
+    if (st.ns > 0) {
+        if (st.sbc) k_extrap_phi_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sbc, st.ns, L);
+        else k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
+    }
+#ifndef MFLBM_STRICT
+    if (st.glist) {
+        if (st.n_gcell_n > 0)
+            k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny, cnz,
+                                                                        cnorm, L);
+    } else
+#endif
     {
         const int nxh = L.nx + 4;
         const int bx = nxh >= 128 ? 128 : ((nxh + 31) / 32) * 32;
@@ -201,7 +211,17 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
     }
     if (st.nf > 0) k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L);
-    if (st.ns > 0) k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
+    if (st.ns > 0) {
+        if (st.sbc) k_extrap_normals_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sbc, st.ns, L);
+        else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
+    }
+#ifndef MFLBM_STRICT
+    if (st.glist) {
+        if (st.n_gcell_c > 0)
+            k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
+                                                                           st.n_gcell_c, L);
+    } else
+#endif
     {
         const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
         const dim3 b(bx, 256 / bx);
