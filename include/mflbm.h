@@ -70,8 +70,9 @@ extern "C" {
 #define MFLBM_FP64 0   /* plain drop-in: FP64 storage, FP64 collision               */
 #define MFLBM_FP32 1   /* FP32 storage, FP32 collision                              */
 #define MFLBM_FP16 2   /* FP16 storage of scaled deviations from the rest state, FP32 collision */
-#define MFLBM_FP64FF 3 /* singlephase: FP64 storage, collision in double-word (two-FP32, about
-                          48-bit) arithmetic on the FP32 pipe; every other kernel as MFLBM_FP64 */
+#define MFLBM_FP64FF 3 /* FP64 storage, collision in double-word (two-FP32, about 48-bit)
+                          arithmetic on the FP32 pipe; every other kernel as MFLBM_FP64
+                          (singlephase and multiphase) */
 #define MFLBM_FF 4     /* singlephase: double-word storage (hi + lo FP32 pair per population,
                           8 bytes, about 48 bits) and the double-word collision */
 

@@ -109,8 +109,8 @@ int validate(const mflbm_params *p, std::string &err) {
             err = "multiphase supports MFLBM_FP64 and MFLBM_FP32 storage (FP16 deviations cannot hold a vanishing species)";
             return MFLBM_EINVAL;
         }
-        if (p->precision == MFLBM_FP64FF || p->precision == MFLBM_FF) {
-            err = "MFLBM_FP64FF and MFLBM_FF (double-word collision) are singlephase";
+        if (p->precision == MFLBM_FF) {
+            err = "MFLBM_FF (double-word storage) is singlephase; multiphase takes MFLBM_FP64FF";
             return MFLBM_EINVAL;
         }
         if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
@@ -373,6 +373,8 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     c->st.ref = 1.0f;
     c->st.scale = 4096.0f;
     c->st.rk_weight2 = 1.0 / std::sqrt(2.0) / 36.0;
+    c->st.mpff = MpConstFF{ff(0.5 * p.gamma), ff(p.force_z), ff(P.la_nui1), ff(P.la_nui2), ff(p.beta),
+                           ff(1.0 / 18.0), ff(c->st.rk_weight2)};
 
     // device arrays (MemAllocate_multi, Init_multiphase.F90:583-828)
     const int nsp = p.multiphase ? 2 : 1;

@@ -100,6 +100,16 @@ __host__ __device__ constexpr bool cell_packable(int nx, int ny, int nz) {
     return nx + 5 <= 2047 && ny + 5 <= 2047 && nz + 5 <= 1023;
 }
 
+// run constants of the double-word multiphase collision, split once on the host
+struct MpConstFF {
+    ff half_gamma;   // 0.5 * gamma
+    ff force_z;
+    ff nui1, nui2;   // 1 / la_nu1, 1 / la_nu2
+    ff beta;
+    ff w1_tmp_scale; // w_equ_1 (the recolouring weight of the axis directions)
+    ff rkw2;         // 1 / sqrt(2) / 36 (the diagonal directions)
+};
+
 // compact solid-boundary record: packed cell, bit (d-1) set for every fluid-neighbour
 // direction d, and the record's la_weight (16 bytes)
 struct SolidBndC {

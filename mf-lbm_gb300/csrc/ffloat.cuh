@@ -82,6 +82,21 @@ __device__ __forceinline__ ff ff_mulf(ff x, float k) {
 // x * 2^n: exact
 __device__ __forceinline__ ff ff_pow2(ff x, float p2) { return ff{__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)}; }
 
+// x / y: the long-division form of the double-word quotient (Joldes, Muller and Popescu
+// 2017, DWDivDW1): q1 = x.hi / y.hi, the remainder r = x - q1 y in double-word arithmetic
+// (exact TwoProd of q1 y.hi), q2 = r.hi / y.hi; relative error about 2^-45.  The FP32
+// divisions are IEEE round-to-nearest (__fdiv_rn).
+__device__ __forceinline__ ff operator/(ff x, ff y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    const float p = __fmul_rn(q1, y.hi);
+    const float pe = __fmaf_rn(q1, y.hi, -p);          // q1 * y.hi = p + pe exactly
+    const ff d = ff_two_sum(x.hi, -p);
+    // remainder x - q1 y = (x.hi - p) - pe + x.lo - q1 y.lo
+    const float r = __fadd_rn(d.hi, __fadd_rn(__fadd_rn(d.lo, -pe), __fmaf_rn(-q1, y.lo, x.lo)));
+    const float q2 = __fdiv_rn(r, y.hi);
+    return ff_fast2sum(q1, q2);
+}
+
 // FP64 -> double word on the integer pipe only (selects, no FP64 instruction: GB300
 // executes FP64 conversions on its narrow FP64 pipe, and a predicated fallback would still
 // issue them).  hi is the FP64 significand truncated to 24 bits (the exponent rebased from

@@ -735,6 +735,90 @@ __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restric
     }
 }
 
+// The multiphase collision of the double-word form (MFLBM_FP64FF): FP64 storage of f, g,
+// phi and the gradient fields, arithmetic in FP32 pairs (ffloat.cuh).  The operations are
+// k_mp_step's default build, term for term: phi and the recolouring weights from one
+// reciprocal of the density, the CSF force, the per-node viscosity and MRT rates folded by
+// fold_rates_dev, the pair-form MRT collision with a general force, the recolouring.  Each
+// FP64 value is split on load and joined on store (one FP64 add), so the FP64 pipe carries
+// 39 adds per node instead of the whole collision.
+template <bool ODD>
+__global__ void __launch_bounds__(128) k_mp_step_ff(double *__restrict__ f, double *__restrict__ g,
+                                                    double *__restrict__ phi, const double *__restrict__ cnx,
+                                                    const double *__restrict__ cny, const double *__restrict__ cnz,
+                                                    const double *__restrict__ cnorm, const double *__restrict__ curv,
+                                                    const int32_t *__restrict__ cells, const int ncell, const Layout L,
+                                                    const MpConstFF K, const int mrt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    const int64_t c = cells[t];
+    const int k = (int)(c / L.pz);
+    const int64_t r = c - (int64_t)k * L.pz;
+    const int j = (int)(r / L.pitch);
+    const int i = (int)(r - (int64_t)j * L.pitch) - L.xo;
+    const int64_t w2 = L.i2(i, j, k);
+    ff ft[19];
+    ff rho1, rho2;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const ff a = ff_from_f64(ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c]);
+        ft[q] = a;
+        rho1 = q == 0 ? a : rho1 + a;
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const ff b = ff_from_f64(ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c]);
+        ft[q] = ft[q] + b;
+        rho2 = q == 0 ? b : rho2 + b;
+    }
+    const ff den = rho1 + rho2;
+    const ff inv_den = ff(1.0f) / den;
+    const ff ph = (rho1 - rho2) * inv_den;
+    phi[L.i4(i, j, k)] = f64_of_ff(ph);
+    const ff cx = ff_from_f64(cnx[w2]), cy = ff_from_f64(cny[w2]), cz = ff_from_f64(cnz[w2]);
+    const ff tmpf = K.half_gamma * ff_from_f64(curv[L.i1(i, j, k)]) * ff_from_f64(cnorm[w2]);
+    const ff fx = tmpf * cx, fy = tmpf * cy, fz = tmpf * cz + K.force_z;
+    const ff visc = (ff(1.0f) + ph) * K.nui1 + (ff(1.0f) - ph) * K.nui2;
+    const ff omega = visc / (ff(6.0f) + ff_pow2(visc, 0.5f));
+    MrtFold<ff> cf;
+    if (mrt == 1) {
+        const ff sq = ff_mulf(ff(2.0f) - omega, 8.0f) / (ff(8.0f) - omega);
+        cf = fold_rates_dev<ff>(omega, omega, sq, omega, omega, sq);
+    } else if (mrt == 3) {
+        cf = fold_rates_dev<ff>(omega, omega, omega, omega, omega, omega);
+    } else if (mrt == 4) {
+        const ff sq = (ff(6.0f) - ff_mulf(omega, 3.0f)) / (ff(3.0f) - omega);
+        cf = fold_rates_dev<ff>(omega, omega, sq, omega, omega, omega);
+    } else {
+        cf = fold_rates_dev<ff>(ff(1.19), ff(1.4), ff(1.2), omega, ff(1.4), ff(1.98));
+    }
+    mrt_collide_pairs<ff, true, false>(ft, den, fx, fy, fz, cf);
+    // recolouring (Kernel_multiphase.F90:272-315)
+    const ff tmp1 = rho1 * inv_den;
+    const ff tmp = rho1 * rho2 * K.beta * inv_den;
+    f[c] = f64_of_ff(tmp1 * ft[0]);
+    g[c] = f64_of_ff(ft[0] * (ff(1.0f) - tmp1));
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        const ff sx = EX(q) > 0 ? cx : -cx, sy = EY(q) > 0 ? cy : -cy, sz = EZ(q) > 0 ? cz : -cz;
+        ff proj;
+        if (q <= 6)
+            proj = EX(q) != 0 ? sx : (EY(q) != 0 ? sy : sz);
+        else if (EZ(q) == 0)
+            proj = sx + sy;
+        else if (EY(q) == 0)
+            proj = sx + sz;
+        else
+            proj = sy + sz;
+        const ff wt = q <= 6 ? K.w1_tmp_scale * tmp : K.rkw2 * tmp;
+        const ff a = tmp1 * ft[q] + wt * proj;
+        const ff b = ft[q] - a;
+        const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
+        f[o] = f64_of_ff(a);
+        g[o] = f64_of_ff(b);
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // Periodic halo exchange (single-device form of Mpi.F90:101-598).  Faces copy the five
 // PDFs that cross the face over the interior tangential range; the edge kernel then

@@ -55,6 +55,7 @@ struct DevState {
     MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
     MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
     MrtFold<ff> foldff;      // the same as double words (MFLBM_FP64FF collision)
+    MpConstFF mpff;          // multiphase run constants as double words (MFLBM_FP64FF)
     int unit;                // 1: fold_is_unit(fold), the collision skips the zero terms
 };
 

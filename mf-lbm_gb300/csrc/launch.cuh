@@ -70,8 +70,26 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
     return 1;
 }
 
+int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
+    if (st.ncell == 0) return 0;
+    const unsigned nb = (unsigned)((st.ncell + 127) / 128);
+    double *f = fs<double>(st), *gg = gs<double>(st);
+    if (odd)
+        k_mp_step_ff<true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
+                                             fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
+                                             st.ncell, st.L, st.mpff, st.P.mrt);
+    else
+        k_mp_step_ff<false><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
+                                              fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
+                                              st.ncell, st.L, st.mpff, st.P.mrt);
+    return 1;
+}
+
 int collide(const DevState &st, bool odd, cudaStream_t s) {
-    if (st.multiphase) return mp_fp32(st) ? collide_mp<float>(st, odd, s) : collide_mp<double>(st, odd, s);
+    if (st.multiphase) {
+        if (st.prec == MFLBM_FP64FF) return collide_mp_ff(st, odd, s);
+        return mp_fp32(st) ? collide_mp<float>(st, odd, s) : collide_mp<double>(st, odd, s);
+    }
     switch (st.prec) {
         case MFLBM_FP32: return collide_t<dfloat>(st, odd, s);
         case MFLBM_FP16: return collide_t<__half>(st, odd, s);

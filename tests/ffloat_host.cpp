@@ -14,6 +14,7 @@
 static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }
 static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
 static inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b, c); }
 static inline double __dadd_rn(double a, double b) { return a + b; }
 static inline float __double2float_rn(double d) { return (float)d; }
@@ -61,7 +62,7 @@ void ffh_to_f64(const float *hi, const float *lo, double *d, int n) {
 void ffh_f32_to_f64(const float *x, double *d, int n) {
     for (int i = 0; i < n; ++i) d[i] = mflbm::f64_of_f32(x[i]);
 }
-// op 0: x + y, 1: x - y, 2: x * y, 3: x * y.hi (FP32 factor), 4: x * 0.5
+// op 0: x + y, 1: x - y, 2: x * y, 3: x * y.hi (FP32 factor), 4: x * 0.5, 5: x / y
 void ffh_op(int op, const float *xh, const float *xl, const float *yh, const float *yl, float *zh, float *zl, int n) {
     for (int i = 0; i < n; ++i) {
         const ff x{xh[i], xl[i]}, y{yh[i], yl[i]};
@@ -71,7 +72,9 @@ void ffh_op(int op, const float *xh, const float *xl, const float *yh, const flo
             case 1: z = x - y; break;
             case 2: z = x * y; break;
             case 3: z = mflbm::ff_mulf(x, y.hi); break;
-            default: z = mflbm::ff_pow2(x, 0.5f); break;
+            case 5: z = x / y; break;
+            case 4: z = mflbm::ff_pow2(x, 0.5f); break;
+            default: z = x; break;
         }
         zh[i] = z.hi;
         zl[i] = z.lo;

@@ -6,7 +6,8 @@ mapped onto IEEE operations, against exact rational arithmetic:
     signed zero, infinities and NaN kept
   - (hi, lo) -> FP64: hi + lo rounded once
   - sum, difference: absolute error <= 2^-46 (|x| + |y|), also for unnormalised inputs
-  - products: relative error <= 2^-45; power-of-two scaling exact
+  - products and quotients: relative error <= 2^-45 (2^-44 for quotients); power-of-two
+    scaling exact
 """
 import ctypes as C
 import os
@@ -152,3 +153,14 @@ def test_products(lib):
     z = op(lib, 4, x, y)
     for u, w in zip(exact(*x), exact(*z)):
         assert w == u / 2
+
+
+def test_quotients(lib):
+    rng = np.random.default_rng(7)
+    n = 3000
+    x = split(lib, rand_doubles(rng, n, -8, 3))
+    # divisors of the collision: densities near 1, viscosity terms, la_weight sums
+    y = split(lib, np.concatenate([1.0 + 1e-3 * rng.normal(size=n // 2), rand_doubles(rng, n // 2, -3, 2)]))
+    z = op(lib, 5, x, y)
+    for u, v, w in zip(exact(*x), exact(*y), exact(*z)):
+        assert abs(w - u / v) <= Fraction(2) ** -44 * abs(u / v)

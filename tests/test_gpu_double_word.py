@@ -98,3 +98,41 @@ def test_double_word_storage_round_trip():
     b = _inner(case["f"])
     fl = _fluid(case)
     assert np.all(np.abs(a[:, fl] - b[:, fl]) <= 2.0 ** -46 * np.abs(b[:, fl]))
+
+
+MP_CASES = {
+    "mp_periodic_yz": dict(per=(0, 1, 1)),
+    "mp_velocity_inlet_convective": dict(per=(0, 0, 0), inlet=1, outlet=1, theta_deg=30.0),
+    "mp_pressure_bcs": dict(per=(0, 0, 0), inlet=2, outlet=2, sa_inject=0.0),
+    "mp_viscosity_ratio_mrt1": dict(per=(0, 1, 1), nu1=0.02, nu2=0.2, mrt=1),
+    "mp_mrt2_fixed_rates": dict(per=(0, 1, 1), mrt=2),
+    "mp_mrt3": dict(per=(0, 1, 1), mrt=3, theta_deg=120.0),
+    "mp_mrt4": dict(per=(0, 1, 1), mrt=4, beta=0.7),
+    "mp_body_force": dict(per=(0, 0, 1), force=1e-5),
+}
+
+
+@pytest.mark.parametrize("name", list(MP_CASES))
+@pytest.mark.parametrize("steps", [1, 9, 40])
+def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
+    """Multiphase, FP64 storage with the double-word collision, against the FP64 oracle:
+    |df|, |dg| <= 1e-12 (n+1), |dphi| <= 1e-10 (n+1) after n steps (populations of order
+    0.1; a wrong term shows at 1e-6 and above)."""
+    from cases import mp_case
+    case = mp_case(strict=0, precision=MFLBM_FP64FF, **MP_CASES[name])
+    with Solver(case["params"]) as gpu:
+        load_case(gpu, case)
+        for n in range(1, steps + 1):
+            gpu.step(n)
+        a = gpu.download_state()
+    orc = Oracle(case["params"])
+    load_case(orc, case)
+    for n in range(1, steps + 1):
+        orc.step(n)
+    b = orc.download_state()
+    orc.close()
+    df = max(np.abs(a[k] - b[k]).max() for k in ("f", "g"))
+    dphi = np.abs(a["phi"] - b["phi"]).max()
+    print(f"{name} steps {steps}: max |df| {df:.3e} max |dphi| {dphi:.3e}")
+    assert df <= 1e-12 * (steps + 1)
+    assert dphi <= 1e-10 * (steps + 1)
