@@ -36,7 +36,8 @@ import numpy as np  # noqa: E402
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
 BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1, 4: 19 * 8 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
-BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1}
+BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1,
+                   3: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1}
 # 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe;
 # 4: double-word storage (hi + lo FP32 pair, 8 bytes) and the double-word collision
 DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff", 4: "ff"}
