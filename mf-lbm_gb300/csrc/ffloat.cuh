@@ -97,6 +97,24 @@ __device__ __forceinline__ ff operator/(ff x, ff y) {
     return ff_fast2sum(q1, q2);
 }
 
+// sqrt(x) for x >= 0: s = sqrt(x.hi) (IEEE round to nearest), then one correction with
+// the exact residual x - s^2 (TwoProd of s, s): s + (x - s^2) / (2 s) (Karp and Markstein,
+// 1997); relative error about 2^-46.  x = 0 gives 0.
+__device__ __forceinline__ ff ff_sqrt(ff x) {
+    const float s = __fsqrt_rn(x.hi);
+    if (s == 0.0f) return ff{0.0f, 0.0f};
+    const float p = __fmul_rn(s, s);
+    const float pe = __fmaf_rn(s, s, -p);                 // s^2 = p + pe exactly
+    const float r = __fadd_rn(__fadd_rn(__fsub_rn(x.hi, p), -pe), x.lo);
+    return ff_fast2sum(s, __fdiv_rn(r, __fadd_rn(s, s)));
+}
+
+// x < y, decided on the double-word value
+__device__ __forceinline__ bool ff_less(ff x, ff y) {
+    const ff d = x - y;
+    return d.hi < 0.0f || (d.hi == 0.0f && d.lo < 0.0f);
+}
+
 // FP64 -> double word on the integer pipe only (selects, no FP64 instruction: GB300
 // executes FP64 conversions on its narrow FP64 pipe, and a predicated fallback would still
 // issue them).  hi is the FP64 significand truncated to 24 bits (the exponent rebased from

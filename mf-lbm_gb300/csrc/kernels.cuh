@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restric
 // FP64 value is split on load and joined on store (one FP64 add), so the FP64 pipe carries
 // 39 adds per node instead of the whole collision.
 template <bool ODD>
-__global__ void __launch_bounds__(128) k_mp_step_ff(double *__restrict__ f, double *__restrict__ g,
+__global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, double *__restrict__ g,
                                                     double *__restrict__ phi, const double *__restrict__ cnx,
                                                     const double *__restrict__ cny, const double *__restrict__ cnz,
                                                     const double *__restrict__ cnorm, const double *__restrict__ curv,
@@ -1400,6 +1400,75 @@ __global__ void __launch_bounds__(256) k_normals_list(const T *__restrict__ phi,
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
     normals_at<T>(phi, i, j, k, L.i2(i, j, k), cnx, cny, cnz, cnorm, L);
+}
+
+// The two stencils of the double-word form (MFLBM_FP64FF, multiphase): FP64 fields split on
+// load, the default build's operations in FP32 pairs (ISO4 sums, norm, reciprocal), FP64
+// results.  Fluid-cell lists only; without them the form uses the FP64 kernels.
+template <int DUMMY = 0>
+__global__ void __launch_bounds__(256) k_normals_list_ff(const double *__restrict__ phi, const uint32_t *__restrict__ cl,
+                                                         int n, double *__restrict__ cnx, double *__restrict__ cny,
+                                                         double *__restrict__ cnz, double *__restrict__ cnorm,
+                                                         const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_cell(cl[t], i, j, k);
+    const int64_t id = L.i2(i, j, k);
+    auto P = [&](int a, int b, int c) { return ff_from_f64(phi[L.i4(i + a, j + b, k + c)]); };
+    constexpr ff c1 = ff_const(ISO4_1), c2 = ff_const(ISO4_2);
+    ff gx = c1 * (P(1, 0, 0) - P(-1, 0, 0)) +
+            c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
+    ff gy = c1 * (P(0, 1, 0) - P(0, -1, 0)) +
+            c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
+    ff gz = c1 * (P(0, 0, 1) - P(0, 0, -1)) +
+            c2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
+    ff cn = ff_sqrt(gx * gx + gy * gy + gz * gz);
+    if (ff_less(cn, ff_const(1e-6))) {
+        cnx[id] = 0.0; cny[id] = 0.0; cnz[id] = 0.0; cnorm[id] = 0.0;
+        return;
+    }
+    const ff inv = ff(1.0f) / cn;
+    cnx[id] = f64_of_ff(gx * inv);
+    cny[id] = f64_of_ff(gy * inv);
+    cnz[id] = f64_of_ff(gz * inv);
+    cnorm[id] = f64_of_ff(cn);
+}
+
+template <int DUMMY = 0>
+__global__ void __launch_bounds__(256) k_curvature_list_ff(const double *__restrict__ cnx, const double *__restrict__ cny,
+                                                           const double *__restrict__ cnz, double *__restrict__ curv,
+                                                           const uint32_t *__restrict__ cl, int n, const Layout L) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i, j, k;
+    unpack_cell(cl[t], i, j, k);
+    constexpr ff c1 = ff_const(ISO4_1), c2 = ff_const(ISO4_2);
+    auto X = [&](int a, int b, int c) { return ff_from_f64(cnx[L.i2(i + a, j + b, k + c)]); };
+    auto Y = [&](int a, int b, int c) { return ff_from_f64(cny[L.i2(i + a, j + b, k + c)]); };
+    auto Z = [&](int a, int b, int c) { return ff_from_f64(cnz[L.i2(i + a, j + b, k + c)]); };
+    const ff kxx = c1 * (X(1, 0, 0) - X(-1, 0, 0)) +
+                   c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
+    const ff kyy = c1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
+                   c2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(-1, 1, 0) - Y(1, -1, 0) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, 1, -1) - Y(0, -1, 1));
+    const ff kzz = c1 * (Z(0, 0, 1) - Z(0, 0, -1)) +
+                   c2 * (Z(1, 0, 1) - Z(-1, 0, -1) + Z(-1, 0, 1) - Z(1, 0, -1) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, -1, 1) - Z(0, 1, -1));
+    const ff kxy = c1 * (X(0, 1, 0) - X(0, -1, 0)) +
+                   c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(-1, 1, 0) - X(1, -1, 0) + X(0, 1, 1) - X(0, -1, -1) + X(0, 1, -1) - X(0, -1, 1));
+    const ff kxz = c1 * (X(0, 0, 1) - X(0, 0, -1)) +
+                   c2 * (X(1, 0, 1) - X(-1, 0, -1) + X(-1, 0, 1) - X(1, 0, -1) + X(0, 1, 1) - X(0, -1, -1) + X(0, -1, 1) - X(0, 1, -1));
+    const ff kyx = c1 * (Y(1, 0, 0) - Y(-1, 0, 0)) +
+                   c2 * (Y(1, 1, 0) - Y(-1, -1, 0) + Y(1, -1, 0) - Y(-1, 1, 0) + Y(1, 0, 1) - Y(-1, 0, -1) + Y(1, 0, -1) - Y(-1, 0, 1));
+    const ff kyz = c1 * (Y(0, 0, 1) - Y(0, 0, -1)) +
+                   c2 * (Y(1, 0, 1) - Y(-1, 0, -1) + Y(-1, 0, 1) - Y(1, 0, -1) + Y(0, 1, 1) - Y(0, -1, -1) + Y(0, -1, 1) - Y(0, 1, -1));
+    const ff kzx = c1 * (Z(1, 0, 0) - Z(-1, 0, 0)) +
+                   c2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(1, -1, 0) - Z(-1, 1, 0) + Z(1, 0, 1) - Z(-1, 0, -1) + Z(1, 0, -1) - Z(-1, 0, 1));
+    const ff kzy = c1 * (Z(0, 1, 0) - Z(0, -1, 0)) +
+                   c2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(-1, 1, 0) - Z(1, -1, 0) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, 1, -1) - Z(0, -1, 1));
+    const ff cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
+    const ff one(1.0f);
+    curv[L.i1(i, j, k)] = f64_of_ff((cx * cx - one) * kxx + (cy * cy - one) * kyy + (cz * cz - one) * kzz +
+                                    cx * cy * (kxy + kyx) + cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz));
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)

@@ -216,9 +216,19 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
     }
 #ifndef MFLBM_STRICT
     if (st.glist) {
-        if (st.n_gcell_n > 0)
-            k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny, cnz,
-                                                                        cnorm, L);
+        if (st.n_gcell_n > 0) {
+            bool done = false;
+            if constexpr (std::is_same<T, double>::value) {
+                if (st.prec == MFLBM_FP64FF) {
+                    k_normals_list_ff<<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny,
+                                                                                cnz, cnorm, L);
+                    done = true;
+                }
+            }
+            if (!done)
+                k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny,
+                                                                            cnz, cnorm, L);
+        }
     } else
 #endif
     {
@@ -235,9 +245,19 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
     }
 #ifndef MFLBM_STRICT
     if (st.glist) {
-        if (st.n_gcell_c > 0)
-            k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
-                                                                           st.n_gcell_c, L);
+        if (st.n_gcell_c > 0) {
+            bool done = false;
+            if constexpr (std::is_same<T, double>::value) {
+                if (st.prec == MFLBM_FP64FF) {
+                    k_curvature_list_ff<<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
+                                                                                  st.n_gcell_c, L);
+                    done = true;
+                }
+            }
+            if (!done)
+                k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
+                                                                               st.n_gcell_c, L);
+        }
     } else
 #endif
     {

@@ -15,6 +15,7 @@ static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }
 static inline float __fmul_rn(float a, float b) { return a * b; }
 static inline float __fdiv_rn(float a, float b) { return a / b; }
+static inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 static inline float __fmaf_rn(float a, float b, float c) { return std::fmaf(a, b, c); }
 static inline double __dadd_rn(double a, double b) { return a + b; }
 static inline float __double2float_rn(double d) { return (float)d; }
@@ -73,6 +74,7 @@ void ffh_op(int op, const float *xh, const float *xl, const float *yh, const flo
             case 2: z = x * y; break;
             case 3: z = mflbm::ff_mulf(x, y.hi); break;
             case 5: z = x / y; break;
+            case 6: z = mflbm::ff_sqrt(x); break;
             case 4: z = mflbm::ff_pow2(x, 0.5f); break;
             default: z = x; break;
         }

@@ -164,3 +164,16 @@ def test_quotients(lib):
     z = op(lib, 5, x, y)
     for u, v, w in zip(exact(*x), exact(*y), exact(*z)):
         assert abs(w - u / v) <= Fraction(2) ** -44 * abs(u / v)
+
+
+def test_square_roots(lib):
+    rng = np.random.default_rng(8)
+    n = 3000
+    v = np.abs(rand_doubles(rng, n, -20, 6))
+    x = split(lib, v)
+    z = op(lib, 6, x, x)
+    for u, w in zip(exact(*x), exact(*z)):
+        # |w - sqrt(u)| <= 2^-45 sqrt(u)  <=>  |w^2 - u| <= ~2^-44 u
+        assert abs(w * w - u) <= Fraction(2) ** -44 * u
+    z0 = op(lib, 6, split(lib, np.zeros(4)), split(lib, np.zeros(4)))
+    assert np.all(z0[0] == 0) and np.all(z0[1] == 0)

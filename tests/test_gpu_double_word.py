@@ -115,9 +115,10 @@ MP_CASES = {
 @pytest.mark.parametrize("name", list(MP_CASES))
 @pytest.mark.parametrize("steps", [1, 9, 40])
 def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
-    """Multiphase, FP64 storage with the double-word collision, against the FP64 oracle:
-    |df|, |dg| <= 1e-12 (n+1), |dphi| <= 1e-10 (n+1) after n steps (populations of order
-    0.1; a wrong term shows at 1e-6 and above)."""
+    """Multiphase, FP64 storage with the double-word collision and colour-gradient stencils,
+    against the FP64 oracle: |df|, |dg| <= 1e-12 (n+1), |dphi| <= 1e-10 (n+1) after n steps
+    (populations of order 0.1; a wrong term shows at 1e-6 and above); normals within 1e-9
+    and curvature at fluid nodes within 1e-7."""
     from cases import mp_case
     case = mp_case(strict=0, precision=MFLBM_FP64FF, **MP_CASES[name])
     with Solver(case["params"]) as gpu:
@@ -125,14 +126,23 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
         for n in range(1, steps + 1):
             gpu.step(n)
         a = gpu.download_state()
+        ga = gpu.get_gradient()
     orc = Oracle(case["params"])
     load_case(orc, case)
     for n in range(1, steps + 1):
         orc.step(n)
     b = orc.download_state()
+    gb = orc.get_gradient()
     orc.close()
     df = max(np.abs(a[k] - b[k]).max() for k in ("f", "g"))
     dphi = np.abs(a["phi"] - b["phi"]).max()
-    print(f"{name} steps {steps}: max |df| {df:.3e} max |dphi| {dphi:.3e}")
+    dcn = max(np.abs(ga[k] - gb[k]).max() for k in ("cn_x", "cn_y", "cn_z", "c_norm"))
+    fl = case["walls"][2:-2, 2:-2, 2:-2] == 0
+    dcurv = np.abs(ga["curv"][1:-1, 1:-1, 1:-1][fl] - gb["curv"][1:-1, 1:-1, 1:-1][fl]).max()
+    print(f"{name} steps {steps}: max |df| {df:.3e} |dphi| {dphi:.3e} |dcn| {dcn:.3e} |dcurv| {dcurv:.3e}")
     assert df <= 1e-12 * (steps + 1)
     assert dphi <= 1e-10 * (steps + 1)
+    # normals and curvature (double-word stencils on fluid-cell lists): the default build's
+    # gates against the oracle
+    assert dcn <= 1e-9
+    assert dcurv <= 1e-7
