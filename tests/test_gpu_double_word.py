@@ -117,8 +117,9 @@ MP_CASES = {
 def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     """Multiphase, FP64 storage with the double-word collision and colour-gradient stencils,
     against the FP64 oracle: |df|, |dg| <= 1e-12 (n+1), |dphi| <= 1e-10 (n+1) after n steps
-    (populations of order 0.1; a wrong term shows at 1e-6 and above); normals within 1e-9
-    and curvature at fluid nodes within 1e-7."""
+    (populations of order 0.1; a wrong term shows at 1e-6 and above); the gradient
+    n |grad phi| and |grad phi| within 1e-12 (n+1), kappa |grad phi| at fluid nodes within
+    1e-10 (n+1)."""
     from cases import mp_case
     case = mp_case(strict=0, precision=MFLBM_FP64FF, **MP_CASES[name])
     with Solver(case["params"]) as gpu:
@@ -136,13 +137,20 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     orc.close()
     df = max(np.abs(a[k] - b[k]).max() for k in ("f", "g"))
     dphi = np.abs(a["phi"] - b["phi"]).max()
-    dcn = max(np.abs(ga[k] - gb[k]).max() for k in ("cn_x", "cn_y", "cn_z", "c_norm"))
+    # the gradient enters the collision as n |grad phi| and kappa |grad phi| (CSF force,
+    # recolouring); the unit normal alone amplifies the ~1e-14 gradient error by 1/|grad phi|
+    # where the gradient is just above the 1e-6 cut-off, so the products are the gates
+    dgrad = max(np.abs(ga[k] * ga["c_norm"] - gb[k] * gb["c_norm"]).max() for k in ("cn_x", "cn_y", "cn_z"))
+    dnorm = np.abs(ga["c_norm"] - gb["c_norm"]).max()
     fl = case["walls"][2:-2, 2:-2, 2:-2] == 0
-    dcurv = np.abs(ga["curv"][1:-1, 1:-1, 1:-1][fl] - gb["curv"][1:-1, 1:-1, 1:-1][fl]).max()
-    print(f"{name} steps {steps}: max |df| {df:.3e} |dphi| {dphi:.3e} |dcn| {dcn:.3e} |dcurv| {dcurv:.3e}")
+    ka = (ga["curv"] * ga["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
+    kb = (gb["curv"] * gb["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
+    dforce = np.abs(ka - kb).max()
+    dcn = max(np.abs(ga[k] - gb[k]).max() for k in ("cn_x", "cn_y", "cn_z"))
+    print(f"{name} steps {steps}: max |df| {df:.3e} |dphi| {dphi:.3e} |d(n|g|)| {dgrad:.3e} |d|g|| {dnorm:.3e} "
+          f"|d(kappa|g|)| {dforce:.3e} (|dn| {dcn:.3e})")
     assert df <= 1e-12 * (steps + 1)
     assert dphi <= 1e-10 * (steps + 1)
-    # normals and curvature (double-word stencils on fluid-cell lists): the default build's
-    # gates against the oracle
-    assert dcn <= 1e-9
-    assert dcurv <= 1e-7
+    assert dgrad <= 1e-12 * (steps + 1)
+    assert dnorm <= 1e-12 * (steps + 1)
+    assert dforce <= 1e-10 * (steps + 1)
