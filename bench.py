@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--c3-fp64-steps", type=int, default=0,
                     help="c3 study: steps of the FP64 run (0: --c3-steps); the phi L1 error is taken there")
     ap.add_argument("--c4-fp64", action="store_true", help="c4: also run the FP64 ensemble for per-sample k errors")
+    ap.add_argument("--c4-ff", action="store_true",
+                    help="c4: also run the double-word storage ensemble (FP64-grade k) on every sample")
     ap.add_argument("--c4-fp64-samples", type=int, default=0,
                     help="c4: run the FP64 reference on the first K samples only (0: all)")
     ap.add_argument("--n", type=int, default=256, help="lattice edge (c2) / cross-section (c3)")
@@ -259,7 +261,9 @@ def ensemble_study(args):
     """c4: every sample of the ensemble from rest to |du|/u < tol (checks every 100
     steps), converged samples leaving the sweep; value = fluid-node updates per second,
     samples/s in config.  With --c4-fp64 the FP64 ensemble of the same seeds gives the
-    per-sample permeability error of the storage form."""
+    per-sample permeability error of the storage form; with --c4-ff the double-word storage
+    ensemble (k within ~1e-10 of FP64 at 4-5x its rate) gives it for every sample, and its own
+    error against FP64 on the FP64 subset."""
     from mflbm import workloads
     world, rank, local = dist_env()
     prec = args.precision if args.precision else 1
@@ -272,9 +276,9 @@ def ensemble_study(args):
     torch.cuda.set_device(local)
     res = {}
     k64 = args.c4_fp64_samples if args.c4_fp64_samples > 0 else args.samples
-    for pr in ([prec, 0] if args.c4_fp64 else [prec]):
+    for pr in [prec] + ([4] if args.c4_ff else []) + ([0] if args.c4_fp64 else []):
         case["params"].precision = pr
-        samples, nf = (case["samples"], case["nf"]) if pr == prec else (case["samples"][:k64], case["nf"][:k64])
+        samples, nf = (case["samples"][:k64], case["nf"][:k64]) if pr == 0 else (case["samples"], case["nf"])
         with Ensemble(case["params"], samples) as ens:
             tune = tune_cached(ens, None, steps=6)
             ens.init()
@@ -301,6 +305,8 @@ def ensemble_study(args):
                "k": float(r.k[i])}
         if args.c4_fp64 and i < k64:
             row.update(steps_fp64=int(res[0][0].steps[i]), k_fp64=float(res[0][0].k[i]))
+        if args.c4_ff:
+            row.update(steps_ff=int(res[4][0].steps[i]), k_ff=float(res[4][0].k[i]))
         per.append(row)
     line["config"]["per_sample"] = per
     if args.c4_fp64:
@@ -310,6 +316,19 @@ def ensemble_study(args):
                                                "samples_compared": int(k64)}
         line["config"]["fp64_wall_s"] = r64.seconds
         line["config"]["fp64_samples_per_s"] = k64 / r64.seconds
+    if args.c4_ff:
+        rff = res[4][0]
+        err = np.abs(r.k - rff.k) / np.abs(rff.k)
+        line["config"]["k_rel_err_vs_ff"] = {"max": float(err.max()), "median": float(np.median(err)),
+                                             "p99": float(np.quantile(err, 0.99)),
+                                             "above_1e-3": int((err > 1e-3).sum()), "samples_compared": args.samples}
+        line["config"]["ff_wall_s"] = rff.seconds
+        line["config"]["ff_samples_per_s"] = args.samples / rff.seconds
+        line["config"]["ff_converged"] = int(rff.converged.sum())
+        line["config"]["ff_launch"] = res[4][1].get("chosen")
+        if args.c4_fp64:
+            e2 = np.abs(rff.k[:k64] - res[0][0].k) / np.abs(res[0][0].k)
+            line["config"]["ff_k_rel_err_vs_fp64"] = {"max": float(e2.max()), "samples_compared": int(k64)}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -4,7 +4,9 @@ runs of the same geometry.
 Same arithmetic as the single-sample fluid-list sweep, so the per-sample flow sums agree
 to summation order (rtol 1e-12); persistent and per-step launch shapes agree exactly;
 inactive samples stay frozen; steady-state permeability per sample equals the
-single-sample result (rtol 1e-9, FP64) and the FP32 ensemble is within 1e-3 of FP64.
+single-sample result (rtol 1e-9, FP64), the double-word ensembles (FP64 storage, and
+double-word storage) within 1e-8 of FP64 at the same step counts, and the FP32 ensemble
+within 1e-3 of FP64.
 """
 import numpy as np
 import pytest
@@ -45,7 +47,7 @@ def test_flux_matches_single_sample_runs():
         np.testing.assert_allclose(w[s], _single_flux(case, s, 24), rtol=1e-12)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 3, 4])
 def test_persistent_equals_per_step_and_inactive_frozen(precision):
     case = _ens(precision)
     out = []
@@ -96,6 +98,15 @@ def test_steady_permeability_per_sample():
             r = single_steady(sim, p, check_every=100, tol=1e-7, max_steps=40000)
         assert r.steps == r64.steps[s]
         np.testing.assert_allclose(r64.k[s], r.k, rtol=1e-9)
+    for prec in (3, 4):
+        cdw = _ens(prec, n=3, seed=5)
+        with Ensemble(cdw["params"], cdw["samples"]) as ens:
+            ens.init()
+            rdw = run_to_steady(ens, cdw["nf"], check_every=100, tol=1e-7, max_steps=40000)
+        print("precision", prec, "k", rdw.k, "rel", np.abs(rdw.k - r64.k) / np.abs(r64.k))
+        assert rdw.converged.all()
+        assert np.array_equal(rdw.steps, r64.steps)
+        assert (np.abs(rdw.k - r64.k) / np.abs(r64.k)).max() <= 1e-8
     case32 = _ens(1, n=3, seed=5)
     with Ensemble(case32["params"], case32["samples"]) as ens:
         ens.init()
