@@ -667,8 +667,8 @@ def main():
     if os.path.exists(tf):
         try:
             t = json.load(open(tf))
-            # the double-word form moves the FP64 form's bytes
-            key = f"{DTYPE[0 if args.precision in (3, 4) else args.precision]}_{layout}"
+            # FP64 storage with the double-word collision moves the FP64 form's bytes
+            key = f"{DTYPE[0 if args.precision == 3 else args.precision]}_{layout}"
             traffic = t[key] * pore if (key in t and not p.multiphase) else None
         except Exception:
             traffic = None
