@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--c3-study", action="store_true",
                     help="c3: FP64 and FP32 forms over --c3-steps steps, saturation every 500 steps, phi L1 error")
     ap.add_argument("--c3-steps", type=int, default=20000)
+    ap.add_argument("--c3-ff", action="store_true", help="c3 study: also the double-word form (FP64 storage)")
     ap.add_argument("--c3-fp64-steps", type=int, default=0,
                     help="c3 study: steps of the FP64 run (0: --c3-steps); the phi L1 error is taken there")
     ap.add_argument("--c4-fp64", action="store_true", help="c4: also run the FP64 ensemble for per-sample k errors")
@@ -509,9 +510,10 @@ def network_step_bench(args):
 
 
 def drainage_study(args):
-    """c3 at scale: the FP64 form and the FP32 mixed form of the same drainage from the
-    same initial state; saturation (FP64 device sums) every 500 steps and, at the end,
-    the phi-field L1 error of the mixed form against FP64 over the interior nodes."""
+    """c3 at scale: the FP64 form, the FP32 mixed form and (--c3-ff) the FP64-grade
+    double-word form of the same drainage from the same initial state; saturation (FP64
+    device sums) every 500 steps and, at the end, the phi-field L1 error of each form against
+    FP64 over the interior nodes."""
     import copy
     import torch
     from mflbm import Solver, workloads
@@ -522,10 +524,10 @@ def drainage_study(args):
     res = {}
     every = 500
     n64 = args.c3_fp64_steps if args.c3_fp64_steps > 0 else args.c3_steps
-    for prec in (0, 1):
+    for prec in (0, 1) + ((3,) if args.c3_ff else ()):
         p = copy.copy(case["params"])
         p.precision = prec
-        nsteps = n64 if prec == 0 else args.c3_steps
+        nsteps = n64 if prec in (0, 3) else args.c3_steps
         with Solver(p) as sim:
             setup(sim, case)
             sim.run(1, 2)
@@ -568,6 +570,14 @@ def drainage_study(args):
                        "max_abs_saturation_diff": float(np.abs(s64[:m] - s32[:m]).max()),
                        "phi_L1_fp32_vs_fp64": float(dphi.mean()), "phi_max_abs_diff": float(dphi.max()),
                        "timed": "host clock around graph-replayed runs of 500 steps, saturation sums outside"}}
+    if 3 in res:
+        dff = np.abs(res[3][1] - res[0][1])[fluid]
+        sff = np.array([x[1] for x in res[3][0]])
+        line["config"]["double_word"] = {
+            "mlups": pore * res[3][3] / res[3][2] / 1e6, "wall_s": res[3][2], "steps": res[3][3],
+            "saturation_every_500": sff.tolist(),
+            "max_abs_saturation_diff": float(np.abs(s64[:len(sff)] - sff).max()),
+            "phi_L1_vs_fp64": float(dff.mean()), "phi_max_abs_diff": float(dff.max())}
     print(json.dumps(line), flush=True)
     return 0
 
