@@ -1472,9 +1472,14 @@ __global__ void __launch_bounds__(256) k_curvature_list_ff(const double *__restr
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
+// min_one_m bounds 1 - (nw.n)^2 below in the forms whose unit normals carry more than FP64
+// rounding (FP32: 1e-6; the double-word form: 1e-12, its normals being unit vectors to
+// ~1e-14); 0 keeps the reference's formula as is (the FP64 drop-in).  Where the bound
+// applies, |n - (nw.n) nw| <= sqrt(bound), so the corrected normal stays O(1).
 template <class T>
 __global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                          const T *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L) {
+                          const T *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L,
+                          const T min_one_m) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
     const FluidBnd b = fb[t];
@@ -1484,10 +1489,10 @@ __global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restric
         const T nwx = T(b.nwx), nwy = T(b.nwy), nwz = T(b.nwz), sin_t = T(b.sin_t);
         const T tmpCos = T(b.cos_t);
         const T tmp1 = nwx * cnx0 + nwy * cny0 + nwz * cnz0;
-        // FP32 form: unit vectors normalised in FP32 can give |nw.n| a few ulp above 1, where
-        // the reference's 1/sqrt(1 - (nw.n)^2) has no value; FP64 keeps the formula as is
+        // unit vectors normalised with fewer than 53 bits can give |nw.n| a few ulp above 1,
+        // where the reference's 1/sqrt(1 - (nw.n)^2) has no value
         T one_m = T(1.0) - tmp1 * tmp1;
-        if (sizeof(T) == 4 && one_m < T(1e-6)) one_m = T(1e-6);
+        if (min_one_m > T(0.0) && one_m < min_one_m) one_m = min_one_m;
         const T tmp2 = T(1.0) / sqrt(one_m);
         const T coe1 = sin_t * tmp1 * tmp2;
         const T coe2 = sin_t * tmp2;

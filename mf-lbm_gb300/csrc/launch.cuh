@@ -238,7 +238,10 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         const dim3 g((nxh + b.x - 1) / b.x, (L.ny + 4 + b.y - 1) / b.y, L.nz + 4);
         k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
     }
-    if (st.nf > 0) k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L);
+    if (st.nf > 0) {
+        const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (st.prec == MFLBM_FP64FF ? T(1e-12) : T(0.0));
+        k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L, min_one_m);
+    }
     if (st.ns > 0) {
         if (st.sbc) k_extrap_normals_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sbc, st.ns, L);
         else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);

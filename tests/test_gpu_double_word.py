@@ -162,3 +162,30 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     assert dgrad <= 1e-10
     assert dgrad_wet <= 1e-8
     assert dforce <= 1e-8
+
+
+@pytest.mark.parametrize("precision", [1, MFLBM_FP64FF])
+def test_wetting_with_wall_parallel_phase_normals_stays_finite(precision):
+    """A flat phase slab across a channel walled in x (uniform in y and z, exact rest states):
+    every phase normal is parallel to the wall normal, where the reference's wetting factor
+    1/sqrt(1 - (nw.n)^2) has no value once rounding puts |nw.n| at or above 1.  The FP32 and
+    double-word forms bound 1 - (nw.n)^2 below (1e-6, 1e-12) and stay finite over 200 steps;
+    the FP64 drop-in keeps the reference's formula."""
+    from cases import W, mp_case
+    case = mp_case(nx=12, ny=6, nz=8, per=(0, 1, 1), spheres=0, strict=0, precision=precision, theta_deg=30.0)
+    p = case["params"]
+    nx, ny, nz = p.nx, p.ny, p.nz
+    x = np.arange(-3, nx + 5, dtype=np.float64)
+    phi = np.broadcast_to(np.tanh((x - 0.5 * nx) / 1.5), (nz + 8, ny + 8, nx + 8)).copy()
+    ph1 = phi[3:nz + 5, 3:ny + 5, 3:nx + 5]
+    case["phi"] = phi
+    case["f"] = W[:, None, None, None] * (0.5 * (1.0 + ph1))[None]
+    case["g"] = W[:, None, None, None] * (0.5 * (1.0 - ph1))[None]
+    with Solver(p) as gpu:
+        load_case(gpu, case)
+        gpu.run(1, 200)
+        st = gpu.download_state()
+        grad = gpu.get_gradient()
+        v1, v2 = gpu.saturation()
+    assert np.isfinite(st["f"]).all() and np.isfinite(st["g"]).all() and np.isfinite(st["phi"]).all()
+    assert np.isfinite(grad["cn_x"]).all() and np.isfinite(v1) and np.isfinite(v2)
