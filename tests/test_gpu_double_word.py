@@ -147,10 +147,19 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     wet = np.zeros(case["walls"].shape, dtype=bool)
     fb = case["fluid"]
     wet[fb["iz"] + 1, fb["iy"] + 1, fb["ix"] + 1] = True
+    # cells within rounding of the reference's |grad phi| < 1e-6 cut-off may fall on either
+    # side in the two forms (the product n |grad phi| then jumps by ~1e-6): left out, with
+    # the curvature stencil's neighbours
+    band = ((ga["c_norm"] > 5e-7) & (ga["c_norm"] < 2e-6)) | ((gb["c_norm"] > 5e-7) & (gb["c_norm"] < 2e-6))
+    near = np.zeros_like(band)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                near |= np.roll(band, (dz, dy, dx), axis=(0, 1, 2))
     dg = np.max([np.abs(ga[k] * ga["c_norm"] - gb[k] * gb["c_norm"]) for k in ("cn_x", "cn_y", "cn_z")], axis=0)
-    dgrad, dgrad_wet = dg[~wet].max(), dg[wet].max()
+    dgrad, dgrad_wet = dg[~wet & ~band].max(), dg[wet & ~band].max()
     dnorm = np.abs(ga["c_norm"] - gb["c_norm"]).max()
-    fl = case["walls"][2:-2, 2:-2, 2:-2] == 0
+    fl = (case["walls"][2:-2, 2:-2, 2:-2] == 0) & ~near[2:-2, 2:-2, 2:-2]
     ka = (ga["curv"] * ga["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
     kb = (gb["curv"] * gb["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
     dforce = np.abs(ka - kb).max()
