@@ -22,13 +22,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
-def lib(tmp_path_factory):
+def lib():
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("g++ not available")
-    out = str(tmp_path_factory.mktemp("ffloat") / "libffloat_host.so")
+    build = os.path.join(HERE, "_build")
+    os.makedirs(build, exist_ok=True)
+    out = os.path.join(build, "libffloat_host.so")
+    tmp = out + f".{os.getpid()}"
     subprocess.run([gxx, "-O2", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC", "-std=c++17",
-                    os.path.join(HERE, "ffloat_host.cpp"), "-o", out], check=True)
+                    os.path.join(HERE, "ffloat_host.cpp"), "-o", tmp], check=True)
+    os.replace(tmp, out)
     L = C.CDLL(out)
     P = np.ctypeslib.ndpointer
     L.ffh_from_f64.argtypes = [P(np.float64), P(np.float32), P(np.float32), C.c_int]
