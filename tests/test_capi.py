@@ -75,3 +75,16 @@ def test_null_context_calls_fail_cleanly():
     assert lib.mflbm_step(None, 0) == _capi.MFLBM_EINVAL
     assert lib.mflbm_synchronize(None) == _capi.MFLBM_EINVAL
     lib.mflbm_destroy(None)
+
+
+def test_header_constants_match_the_binding():
+    """Every integer #define MFLBM_* of include/mflbm.h has the same value in the Python
+    binding (the layout constants are bound as LAYOUT_*)."""
+    import re
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "mflbm.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define (MFLBM_[A-Z0-9_]+)\s+(-?\d+)\b", hdr, re.M)}
+    assert "MFLBM_FP64FF" in defs and "MFLBM_FF" in defs
+    for name, value in defs.items():
+        py = name.replace("MFLBM_LAYOUT_", "LAYOUT_")
+        assert hasattr(_capi, py), name
+        assert getattr(_capi, py) == value, name
