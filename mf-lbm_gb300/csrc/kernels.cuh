@@ -1225,15 +1225,8 @@ __global__ void __launch_bounds__(256) k_curvature_list_ff(const double *__restr
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
-// The reference writes the two candidates as (cos - s t/sqrt(1-t^2)) nw + (s/sqrt(1-t^2)) n
-// with t = nw.n, i.e. cos nw +- s (n - t nw)/sqrt(1 - t^2): for a unit n, sqrt(1 - t^2) is the
-// length of the perpendicular part n - t nw.  Where the phase normal is nearly parallel to
-// the wall normal, that length is tiny and the formula divides any departure of |n| from 1
-// by it: FP64-normalised normals rarely meet it, but FP32 or double-word normals (unit to
-// 1e-7 / 1e-14) gave |n| of 1.01-1.05 at such nodes, which grew into NaN on large packings.
-// With min_one_m > 0 (FP32: 1e-6, double-word form: 1e-12) the perpendicular part is
-// normalised by its own length (bounded below by sqrt(min_one_m)), the same formula for a
-// unit n with a unit result; min_one_m = 0 keeps the reference's expression (FP64 drop-in).
+#include "wetting.cuh"
+
 template <class T>
 __global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
                           const T *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L,
@@ -1243,37 +1236,9 @@ __global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restric
     const FluidBnd b = fb[t];
     const int64_t id = L.i2(b.ix, b.iy, b.iz);
     if (cnorm[id] > T(1e-6)) {
-        const T cnx0 = cnx[id], cny0 = cny[id], cnz0 = cnz[id];
-        const T nwx = T(b.nwx), nwy = T(b.nwy), nwz = T(b.nwz), sin_t = T(b.sin_t);
-        const T tmpCos = T(b.cos_t);
-        const T tmp1 = nwx * cnx0 + nwy * cny0 + nwz * cnz0;
-        T cnxp, cnyp, cnzp, cnxm, cnym, cnzm;
-        if (min_one_m > T(0.0)) {
-            // cos nw +- sin (n - t nw) / |n - t nw|
-            const T px = cnx0 - tmp1 * nwx, py = cny0 - tmp1 * nwy, pz = cnz0 - tmp1 * nwz;
-            T pp = px * px + py * py + pz * pz;
-            if (pp < min_one_m) pp = min_one_m;
-            const T coe2 = sin_t / sqrt(pp);
-            cnxp = tmpCos * nwx + coe2 * px; cnyp = tmpCos * nwy + coe2 * py; cnzp = tmpCos * nwz + coe2 * pz;
-            cnxm = tmpCos * nwx - coe2 * px; cnym = tmpCos * nwy - coe2 * py; cnzm = tmpCos * nwz - coe2 * pz;
-        } else {
-            const T tmp2 = T(1.0) / sqrt(T(1.0) - tmp1 * tmp1);
-            const T coe1 = sin_t * tmp1 * tmp2;
-            const T coe2 = sin_t * tmp2;
-            cnxp = (tmpCos - coe1) * nwx + coe2 * cnx0;
-            cnyp = (tmpCos - coe1) * nwy + coe2 * cny0;
-            cnzp = (tmpCos - coe1) * nwz + coe2 * cnz0;
-            cnxm = (tmpCos + coe1) * nwx - coe2 * cnx0;
-            cnym = (tmpCos + coe1) * nwy - coe2 * cny0;
-            cnzm = (tmpCos + coe1) * nwz - coe2 * cnz0;
-        }
-        const T distP = (cnxp - cnx0) * (cnxp - cnx0) + (cnyp - cny0) * (cnyp - cny0) + (cnzp - cnz0) * (cnzp - cnz0);
-        const T distM = (cnxm - cnx0) * (cnxm - cnx0) + (cnym - cny0) * (cnym - cny0) + (cnzm - cnz0) * (cnzm - cnz0);
-        if (distP <= distM) {
-            cnx[id] = cnxp; cny[id] = cnyp; cnz[id] = cnzp;
-        } else {
-            cnx[id] = cnxm; cny[id] = cnym; cnz[id] = cnzm;
-        }
+        T n[3] = {cnx[id], cny[id], cnz[id]};
+        wetting_normal<T>(n, T(b.nwx), T(b.nwy), T(b.nwz), T(b.cos_t), T(b.sin_t), min_one_m);
+        cnx[id] = n[0]; cny[id] = n[1]; cnz[id] = n[2];
     }
 }
 
