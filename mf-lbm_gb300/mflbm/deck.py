@@ -86,7 +86,8 @@ def _get(d, key, default):
 
 
 def make_run(deck, multiphase=True, device=0, precision=0, strict_fp=0):
-    """mflbm_params from a parsed deck, with the reference's host-side derivations."""
+    """mflbm_params from a parsed deck, with the reference's host-side derivations; precision
+    selects the storage form (see solver.make_params), which the deck itself does not name."""
     nx, ny, nz = _get(deck, "lattice_dimensions", [40, 40, 60])
     wx = _get(deck, "domain_wall_status_x", [1, 1])
     wy = _get(deck, "domain_wall_status_y", [1, 1])

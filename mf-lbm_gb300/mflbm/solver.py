@@ -18,7 +18,11 @@ from ._capi import MFLBM_ABI_VERSION, Params
 
 
 def make_params(**kw):
-    """mflbm_params with the reference's template defaults, overridden by kw."""
+    """mflbm_params with the reference's template defaults, overridden by kw.
+
+    precision: MFLBM_FP64 (0, the drop-in), MFLBM_FP32 (1), MFLBM_FP16 (2, singlephase),
+    MFLBM_FP64FF (3, FP64 storage with the double-word collision), MFLBM_FF (4, singlephase
+    double-word storage); layout: 0 auto, 1 dense, 2 fluid list (singlephase)."""
     p = Params()
     p.abi_version = MFLBM_ABI_VERSION
     defaults = dict(multiphase=0, nx=16, ny=16, nz=16, iper=0, jper=0, kper=0, wall_x_min=1, wall_x_max=1,
