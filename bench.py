@@ -17,6 +17,11 @@ Workload (one bench "step" = one LBM time step over the whole lattice):
           restatement, all host threads) on the same workload, bounded sample.
 Under torchrun (N>1) every rank runs an independent replica (the lattice is not
 sharded); value = total fluid-node updates of all ranks / max time over ranks.
+
+Other forms and workloads: --precision 0-4 (FP64, FP32, FP16 deviations, FP64 storage with
+the double-word collision, double-word storage), --workload c1 (tube drainage), c3
+(packing drainage; --c3-study for saturation and phi error against FP64), c4 (ensemble to
+steady state), c5 (learned warm start), c5net (one training step of its network).
 """
 import argparse
 import json
