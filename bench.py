@@ -84,6 +84,9 @@ def parse():
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
     ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="c2: skip the per-form measurement (FP64 storage + double-word collision, double-word "
+                         "storage, FP32 and FP16 deviations) that the default line carries under `forms`")
     ap.add_argument("--no-convergence", action="store_true",
                     help="skip the time-to-steady permeability study (singlephase workload only)")
     ap.add_argument("--conv-tol", type=float, default=1e-7)
@@ -117,6 +120,17 @@ def workload(args, device=0):
                 "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, F_z=1e-6, tau=1, "
                 "MRT preset 1")
     return case, desc
+
+
+def config_of(args, case, desc):
+    """The workload description both arms print (the same dict for --impl ours and
+    --impl reference): what was run, not what was measured."""
+    p = case["params"]
+    elt = 8 if args.precision in (0, 3, 4) else (4 if args.precision == 1 else 2)
+    state_bytes = (2 if p.multiphase else 1) * 19 * elt * case["pore"]
+    return {"workload": desc, "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": case["pore"],
+            "l2": f"PDF state of the fluid nodes {state_bytes / 1e9:.2f} GB vs 129 MB L2"
+                  + (": no flush needed" if state_bytes > 4 * 129e6 else ": inputs smaller than L2")}
 
 
 def setup(sim, case):
@@ -199,6 +213,69 @@ def cpu_baseline(case, steps):
                       f"C++ restatement -O3, OpenMP {threads} threads, {dt:.2f} s"}
 
 
+def hbm_peak():
+    """Measured copy bandwidth of the GB300s, else the stated fallback."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(peaks["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+
+
+def stored_traffic(prec, layout, multiphase, pore):
+    """DRAM bytes per launch of the collision sweep from the committed ncu capture
+    (profiles/sp_collide_traffic.json: bytes per fluid node x the fluid nodes here)."""
+    tf = os.path.join(ROOT, "profiles", "sp_collide_traffic.json")
+    if multiphase or not os.path.exists(tf):
+        return None
+    try:
+        t = json.load(open(tf))
+    except Exception:
+        return None
+    # FP64 storage with the double-word collision moves the FP64 form's bytes
+    key = f"{DTYPE[0 if prec == 3 else prec]}_{layout}"
+    return t[key] * pore if key in t else None
+
+
+def roofline_of(prof, pore, prec, multiphase, layout, hbm, peak_src):
+    """Roofline of the collision sweep: algorithmic bytes per launch / the average
+    event-timed launch duration, against the measured copy peak."""
+    avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
+    bpl = BYTES_PER_LU_MP[prec] if multiphase else BYTES_PER_LU[prec]
+    achieved = pore * bpl / avg_s / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": stored_traffic(prec, layout, multiphase, pore), "traffic_source": "ncu capture "
+            "(profiles/sp_collide_traffic.json, bytes per fluid node x fluid nodes)", "bytes_per_lu": bpl,
+            "peak_source": peak_src, "avg_launch_ms": avg_s * 1e3, "launches_timed": prof["collide_launches"]}
+
+
+def measure_form(args, case, prec, hbm, peak_src):
+    """One storage form of the singlephase workload on the same geometry, timed exactly
+    like the headline: per-step launches with events around every collision sweep,
+    --steps steps after --warmup, then graph replay of the same number of steps."""
+    import copy
+    from mflbm import Solver
+    p = copy.copy(case["params"])
+    p.precision = prec
+    pore = case["pore"]
+    with Solver(p) as sim:
+        setup(sim, case)
+        sim.run(1, max(args.warmup, 3))
+        sim.synchronize()
+        sim.set_profiling(True)
+        sim.run(args.warmup + 1, args.steps)
+        prof = sim.get_profile()
+        sim.set_profiling(False)
+        sim.run(args.warmup + 1 + args.steps, args.steps)
+        gprof = sim.get_profile()
+        layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
+    total_s = prof["region_ms"] / 1e3
+    roof = roofline_of(prof, pore, prec, False, layout, hbm, peak_src)
+    return {"value": pore * args.steps / total_s / 1e6, "unit": "MLUPS", "ms_per_step": 1e3 * total_s / args.steps,
+            "graph_replay_mlups": pore * args.steps / (gprof["region_ms"] / 1e3) / 1e6, "layout": layout,
+            "gpu_launches": prof["kernel_launches"], "roofline": roof}
+
+
 def convergence_study(args, case, device):
     """Time-to-steady permeability of each storage form on the same geometry.
 
@@ -241,23 +318,26 @@ def run_reference(args):
     args.precision = 0
     case, desc = workload(args)
     p, pore = case["params"], case["pore"]
-    steps = max(1, min(args.steps, args.cpu_sample_steps))
+    steps = max(1, args.steps)
     import pyoracle
     threads = os.cpu_count() or 1
     o = pyoracle.Oracle(p, variant="fast", threads=threads)
     setup(o, case)
-    o.run(1, 2)
+    o.run(1, max(1, args.warmup))
     t0 = time.perf_counter()
-    o.run(3, steps)
+    o.run(1 + max(1, args.warmup), steps)
     dt = time.perf_counter() - t0
+    o.close()
     v = pore * steps / dt / 1e6
     line = {"metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": desc, "fluid_nodes": pore},
+            "config": config_of(args, case, desc),
             "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
-                             "sample": f"{steps} steps of the full workload; the Fortran reference cannot be built "
-                                       "(no Fortran compiler or MPI), so its C++ restatement runs instead"},
+                             "sample": f"{steps} steps of the full workload after {max(1, args.warmup)} warm-up "
+                                       f"steps, {dt:.2f} s; the Fortran reference cannot be built (no Fortran "
+                                       "compiler or MPI), so its C++ restatement runs instead, OpenMP "
+                                       f"{threads} threads"},
             "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -610,6 +690,7 @@ def main():
     from mflbm import Solver
     case, desc = workload(args, device=local)
     p, pore = case["params"], case["pore"]
+    hbm, peak_src = hbm_peak()
     sim = Solver(p)
     setup(sim, case)
     # warm-up (graph capture, first touch)
@@ -622,12 +703,13 @@ def main():
         torch.cuda.synchronize()
 
     # ---- device-resident timed region: per-step launches with CUDA events around every
-    # collision sweep (profiling mode), the region bracketed by events on the same stream
+    # collision sweep (profiling mode), the region bracketed by events on the same stream.
+    # The clock sampler runs from here to the end of the per-form measurements below.
     barrier()
+    clk = ClockSampler(local).__enter__()
     sim.set_profiling(True)
-    with ClockSampler(local) as clk:
-        sim.run(args.warmup + 1, args.steps)
-        prof = sim.get_profile()   # synchronises the context stream
+    sim.run(args.warmup + 1, args.steps)
+    prof = sim.get_profile()   # synchronises the context stream
     total_s = prof["region_ms"] / 1e3
     if dist:
         t = torch.tensor([total_s], device="cuda")
@@ -666,27 +748,22 @@ def main():
         e2e = {"value": None, "unit": "MLUPS", "error": str(exc)[:200]}
 
     layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
-    collide_avg_s = prof["collide_ms"] / max(1, prof["collide_launches"]) / 1e3
-    elt = 8 if args.precision in (0, 3, 4) else (4 if args.precision == 1 else 2)
-    state_bytes = (2 if p.multiphase else 1) * 19 * elt * (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
-    bpl = BYTES_PER_LU_MP[args.precision] if p.multiphase else BYTES_PER_LU[args.precision]
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    achieved = pore * bpl / collide_avg_s / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "sp_collide_traffic.json")
-    if os.path.exists(tf):
-        try:
-            t = json.load(open(tf))
-            # FP64 storage with the double-word collision moves the FP64 form's bytes
-            key = f"{DTYPE[0 if args.precision == 3 else args.precision]}_{layout}"
-            traffic = t[key] * pore if (key in t and not p.multiphase) else None
-        except Exception:
-            traffic = None
+    sim.close()
+    roof = roofline_of(prof, pore, args.precision, bool(p.multiphase), layout, hbm, peak_src)
+    roof["kernel"] = "k_mp_step" if p.multiphase else ("k_sp_list" if layout == "list" else "k_sp_step")
+
+    # ---- every other storage form of the singlephase workload, measured the same way
+    forms = None
+    if rank == 0 and args.workload == "c2" and not args.no_forms:
+        forms = {}
+        for prec in (0, 3, 4, 1, 2):
+            if prec == args.precision:
+                continue
+            try:
+                forms[DTYPE[prec]] = measure_form(args, case, prec, hbm, peak_src)
+            except Exception as exc:
+                forms[DTYPE[prec]] = {"error": str(exc)[:200]}
+    clk.__exit__(None, None, None)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -701,22 +778,18 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
             "data": "synthetic",
-            "config": {"workload": desc, "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": pore, "replicas": world,
-                       "layout": layout,
-                       "l2": f"state {state_bytes / 1e9:.2f} GB vs 129 MB L2"
-                             + (": no flush needed" if state_bytes > 4 * 129e6 else ": inputs smaller than L2"),
+            "config": config_of(args, case, desc),
+            "detail": {"replicas": world, "layout": layout,
                        "timed_path": "per-step launches with events around each collision sweep",
                        "graph_replay_mlups": graph_mlups},
             "e2e": e2e,
             "gpu_launches": prof["kernel_launches"],
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic, "bytes_per_lu": bpl, "peak_source": "measured (MEASURED_PEAKS.json)",
-                         "kernel": "k_mp_step" if p.multiphase else ("k_sp_list" if layout == "list" else "k_sp_step"),
-                         "avg_launch_ms": collide_avg_s * 1e3},
+            "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
-    sim.close()
+        if forms is not None:
+            line["forms"] = forms
     if rank == 0 and args.workload == "c2" and not args.no_convergence:
         try:
             line["convergence"] = convergence_study(args, case, local)

@@ -269,8 +269,11 @@ int32_t mflbm_get_profile(mflbm_ctx *ctx, double *region_ms, double *collide_ms,
  *   stream  cudaStream_t to launch on (NULL: legacy default stream); asynchronous
  * Scratch is a fixed __device__ array shared by every call; overlapping calls race.
  * The first call on a device looks up the scratch address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  nz > MFLBM_NOALLOC_MAX_NZ returns
- * MFLBM_ERANGE.  Errors are reported through mflbm_last_error(NULL). */
+ * make that first call before any stream capture.  The address is kept for the life of
+ * the process: after cudaDeviceReset on a device, do not call this on that device again.
+ * nz > MFLBM_NOALLOC_MAX_NZ returns MFLBM_ERANGE.  A CUDA error already pending from
+ * earlier work is reported (MFLBM_ECUDA) and not cleared.  Errors are reported through
+ * mflbm_last_error(NULL). */
 int32_t mflbm_saturation_noalloc(const double *phi, const int8_t *walls, int32_t nx, int32_t ny, int32_t nz,
                                  double *vol, void *stream);
 
@@ -298,8 +301,9 @@ int32_t mflbm_ensemble_set_active(mflbm_ensemble *ens, const int32_t *active);
 int32_t mflbm_ensemble_run(mflbm_ensemble *ens, int32_t ntime0, int32_t nsteps);
 /* Per-sample sum of w over the fluid nodes and max |u|^2 (valid after even steps);
  * *status = MFLBM_FAILED on NaN or |u| > 0.5 in an active sample.  Returns
- * MFLBM_ETIMEOUT when a grid barrier of the persistent kernel gave up (the ensemble
- * must then be destroyed).  Synchronises. */
+ * MFLBM_ETIMEOUT when a grid barrier of the persistent kernel gave up; the PDF state is
+ * then undefined, and mflbm_ensemble_init (or mflbm_ensemble_configure) clears the
+ * barrier's error word before the next run.  Synchronises. */
 int32_t mflbm_ensemble_flux(mflbm_ensemble *ens, double *w_sum, double *umax2, int32_t *status);
 /* Launch shape: threads per block (64..1024, multiple of 32) and persistent = 1 for one
  * cooperative launch per run (grid barrier between steps) or 0 for one launch per step. */
@@ -308,6 +312,12 @@ int32_t mflbm_ensemble_configure(mflbm_ensemble *ens, int32_t block, int32_t per
  * fastest; `report` (may be NULL) receives the timings as JSON.  Changes the PDF
  * state: call mflbm_ensemble_init afterwards. */
 int32_t mflbm_ensemble_tune(mflbm_ensemble *ens, int32_t steps, char *report, int32_t report_len);
+/* Diagnostics of the persistent kernel's failure path (no counterpart in the reference):
+ * spin_limit = polls per grid-barrier wait (<= 0: the default, several seconds), and
+ * unreachable = 1 makes every barrier wait for one block more than the grid holds, so
+ * each wait runs out and the kernel returns early (mflbm_ensemble_flux then reports
+ * MFLBM_ETIMEOUT).  Clears the barrier state and drops captured graphs.  Synchronises. */
+int32_t mflbm_ensemble_set_wait(mflbm_ensemble *ens, int64_t spin_limit, int32_t unreachable);
 /* Fluid nodes of the active samples and the launch shape in use. */
 int32_t mflbm_ensemble_info(const mflbm_ensemble *ens, int64_t *active_nodes, int32_t *block,
                             int32_t *persistent, int32_t *grid);
@@ -327,6 +337,12 @@ int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B, int32_t ld
 int32_t mflbm_nn_gemm_bf16_splitk(const void *A, int32_t lda, const void *B, int32_t ldb, float *C, int32_t ldc,
                                   int32_t M, int32_t N, int32_t K, int32_t accumulate, int32_t ksplit, float *work,
                                   int32_t *err, void *stream);
+
+/* Diagnostics of the GEMM's failure path (no counterpart in the reference): wait_limit =
+ * probes per mbarrier wait of later GEMMs (<= 0: the default), skip_commit = 1 makes the
+ * MMA thread issue no tensor-core work and no commit, so every wait runs out: the GEMM
+ * returns MFLBM_OK, sets *err and leaves its output tiles undefined.  Process-wide. */
+int32_t mflbm_nn_set_wait(int64_t wait_limit, int32_t skip_commit);
 
 /* Channels-last activations [D][H][W][C] (bf16 unless stated), 3x3x3 periodic stencil.
  * col[v][tap*Cin + c] = X[v + d_tap][c], zero for k in [27*Cin, Kp). */

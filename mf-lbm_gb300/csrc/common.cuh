@@ -246,7 +246,13 @@ struct EnsArgs {
     unsigned int *bar;       // [2] arrival count, generation
     int32_t *err;            // set when a barrier wait gives up
     int32_t unit;            // 1: the unit-rate collision (tau = 1, MRT preset 1) applies
+    long long spin_limit;    // polls of one grid-barrier wait before it gives up
+    uint32_t bar_extra;      // arrivals a barrier waits for beyond the grid (0; >0 only in
+                             // the timeout test: the barrier can then never open)
 };
+// default poll limit of the persistent ensemble kernel's grid barrier (100 ns sleeps:
+// several seconds, far beyond any step)
+constexpr long long kBarrierSpinsDefault = 1ll << 26;
 
 // FP16 deviation storage: value = w_q * ref + half_value * scale, ref = the rest
 // density of the species.

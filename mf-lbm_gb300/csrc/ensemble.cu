@@ -114,6 +114,15 @@ int grid_for(mflbm_ensemble *e, int block, int persistent) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(all, std::max(maxg, 1) * 4));
 }
 
+// Arrival count, generation and error word of the grid barrier back to zero.  A barrier
+// that timed out leaves a partial count and a set error word, which would make every
+// later persistent run leave at its first barrier.
+int clear_barrier(mflbm_ensemble *e) {
+    EK(e, cudaMemsetAsync(e->a.bar, 0, 2 * sizeof(unsigned int), e->stream));
+    EK(e, cudaMemsetAsync(e->a.err, 0, sizeof(int32_t), e->stream));
+    return MFLBM_OK;
+}
+
 int launch(mflbm_ensemble *e, int32_t ntime0, int32_t nsteps) {
     e->a.ntime0 = ntime0;
     e->a.nsteps = nsteps;
@@ -271,6 +280,8 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
         a.fold32.fz = (float)P.force_z;
         a.foldff = fold_to_ff(a.fold);
         a.unit = fold_is_unit(a.fold) ? 1 : 0;
+        a.spin_limit = kBarrierSpinsDefault;
+        a.bar_extra = 0;
     }
     e->block = 128;
     e->persistent = 0;
@@ -289,6 +300,8 @@ fail:
 int32_t mflbm_ensemble_init(mflbm_ensemble *e) {
     if (!e) return MFLBM_EINVAL;
     EK(e, cudaSetDevice(e->dev));
+    int r = clear_barrier(e);
+    if (r) return r;
     e->kt->ens_init(e->a, e->p.precision, e->stream);
     EK(e, cudaPeekAtLastError());
     EK(e, cudaStreamSynchronize(e->stream));
@@ -378,7 +391,27 @@ int32_t mflbm_ensemble_configure(mflbm_ensemble *e, int32_t block, int32_t persi
     e->persistent = persistent ? 1 : 0;
     e->grid = g;
     drop_graphs(e);
+    int r = clear_barrier(e);
+    if (r) return r;
     return rebuild_tiles(e);
+}
+
+// Diagnostics for the failure path of the persistent kernel's grid barrier (no
+// counterpart in the reference): spin_limit polls per wait (<= 0: the default), and
+// unreachable = 1 makes every barrier wait for one block more than the grid holds, so
+// that each wait runs out, the kernel returns early and mflbm_ensemble_flux reports
+// MFLBM_ETIMEOUT.  Clears the barrier state; captured graphs are dropped.
+int32_t mflbm_ensemble_set_wait(mflbm_ensemble *e, int64_t spin_limit, int32_t unreachable) {
+    if (!e) return MFLBM_EINVAL;
+    EK(e, cudaSetDevice(e->dev));
+    EK(e, cudaStreamSynchronize(e->stream));
+    e->a.spin_limit = spin_limit > 0 ? (long long)spin_limit : kBarrierSpinsDefault;
+    e->a.bar_extra = unreachable ? 1u : 0u;
+    drop_graphs(e);
+    int r = clear_barrier(e);
+    if (r) return r;
+    EK(e, cudaStreamSynchronize(e->stream));
+    return MFLBM_OK;
 }
 
 // In-project autotuner: times every candidate launch shape over `steps` steps (after

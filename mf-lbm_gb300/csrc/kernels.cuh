@@ -1634,11 +1634,10 @@ __global__ void k_ens_step(const EnsArgs a) {
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  Sense by
-// generation counter; the wait is bounded: after kBarrierSpins polls the block sets
-// *err and every block leaves at its next barrier.
-constexpr long long kBarrierSpins = 1ll << 26;
-
-__device__ __forceinline__ bool grid_barrier(unsigned int *bar, int32_t *err) {
+// generation counter; the wait is bounded: after `limit` polls the block sets *err and
+// every other block leaves at its next poll.  The last of gridDim.x + extra arrivals
+// opens the barrier; extra is 0 except in the timeout test, where nobody can open it.
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, int32_t *err, long long limit, unsigned int extra) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1647,14 +1646,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *bar, int32_t *err) {
         const unsigned int gen = *vgen;
         __threadfence();
         const unsigned int arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == gridDim.x - 1 + extra) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
             long long it = 0;
             while (*vgen == gen) {
-                if (++it > kBarrierSpins || *(volatile int32_t *)err) {
+                if (++it > limit || *(volatile int32_t *)err) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;
@@ -1674,7 +1673,7 @@ __global__ void k_ens_persistent(const EnsArgs a) {
     for (int s = 0; s < a.nsteps; ++s) {
         if (((a.ntime0 + s) & 1) != 0) ens_sweep<S, true, UNIT>(a);
         else ens_sweep<S, false, UNIT>(a);
-        if (s + 1 < a.nsteps && !grid_barrier(a.bar, a.err)) return;
+        if (s + 1 < a.nsteps && !grid_barrier(a.bar, a.err, a.spin_limit, a.bar_extra)) return;
     }
 }
 

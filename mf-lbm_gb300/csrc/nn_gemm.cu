@@ -11,9 +11,15 @@
 // chunks placed at their 128B-swizzled positions); one thread issues four
 // tcgen05.mma (K = 16 each) per stage and commits them to the stage's mbarrier, which
 // gates the refill.  The epilogue reads the accumulator rows of each warp's 32 TMEM
-// lanes with tcgen05.ld.  Every mbarrier wait is bounded; a timeout sets *err.
+// lanes with tcgen05.ld.  Every mbarrier wait is bounded.  A wait that runs out makes
+// the whole block give up together (the decision is taken with __syncthreads_and, so no
+// warp runs a collective tcgen05 instruction alone): it sets *err, waits (bounded again)
+// for the MMAs it issued, frees its TMEM and returns without writing its tile; that
+// tile of C is then undefined and the host reports MFLBM_ETIMEOUT from *err.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -24,7 +30,13 @@ namespace mflbm {
 namespace nn {
 
 constexpr int kStages = 3;
-constexpr long long kWaitLimit = 1ll << 22;
+constexpr long long kWaitLimit = 1ll << 22;   // probes of one mbarrier wait (default)
+
+// Diagnostics of the timeout path (mflbm_nn_set_wait): the probe limit of every wait,
+// and whether the MMA thread skips its tensor-core work and commits, so that no
+// mbarrier phase ever completes and every wait runs out.
+std::atomic<long long> g_wait_limit{kWaitLimit};
+std::atomic<int> g_skip_commit{0};
 
 template <int BN>
 struct GemmSmem {
@@ -37,7 +49,8 @@ struct GemmSmem {
 template <int BN>
 __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restrict__ A, int lda,
                                                    const __nv_bfloat16 *__restrict__ B, int ldb, float *__restrict__ C,
-                                                   int ldc, int M, int N, int K, int accumulate, int *__restrict__ err) {
+                                                   int ldc, int M, int N, int K, int accumulate, int *__restrict__ err,
+                                                   long long wait_limit, int skip_commit) {
     using namespace umma;
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t bars[kStages];
@@ -94,7 +107,8 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
         }
     };
 
-    bool ok = true;
+    bool ok = true;   // block-uniform: every change goes through __syncthreads_and
+    int last_commit = -1;   // k-tile of the last commit of thread 0
     for (int s = 0; s < kStages - 1; ++s) {
         if (s < KT) load_stage(s, s);
         cp_async_commit();
@@ -105,7 +119,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
         cp_async_wait<kStages - 2>();
         fence_async_smem();
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !skip_commit) {
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + s * GemmSmem<BN>::kStage);
             const uint32_t sb = sa + GemmSmem<BN>::kA;
@@ -113,26 +127,39 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
             for (int j = 0; j < 4; ++j)
                 mma_bf16(tmem, desc_sw128(sa + j * 32), desc_sw128(sb + j * 32), idesc, (kt > 0 || j > 0) ? 1u : 0u);
             mma_commit(&bars[s]);
+            last_commit = kt;
         }
-        // refill the stage that MMA kt-1 read once it has completed
+        // refill the stage that MMA kt-1 read once it has completed (nk < KT is the same
+        // for every thread, so all of them reach the vote)
         const int nk = kt + kStages - 1;
         if (nk < KT) {
+            bool w = true;
             if (kt >= 1) {
                 const int ps = (kt - 1) % kStages;
-                if (!mbar_wait(&bars[ps], (uint32_t)(((kt - 1) / kStages) & 1), kWaitLimit)) ok = false;
+                w = mbar_wait(&bars[ps], (uint32_t)(((kt - 1) / kStages) & 1), wait_limit);
             }
+            ok = __syncthreads_and(w) != 0;
             if (ok) load_stage(nk % kStages, nk);
         }
         cp_async_commit();
     }
     cp_async_wait<0>();
     // all MMAs issued so far complete when the last commit arrives
+    bool fin = ok;
     if (ok && KT > 0) {
         const int ls = (KT - 1) % kStages;
-        if (!mbar_wait(&bars[ls], (uint32_t)(((KT - 1) / kStages) & 1), kWaitLimit)) ok = false;
+        fin = mbar_wait(&bars[ls], (uint32_t)(((KT - 1) / kStages) & 1), wait_limit);
     }
-    if (!ok && lane == 0) atomicExch(err, 1);
-    __syncthreads();
+    ok = __syncthreads_and(fin) != 0;
+    if (!ok) {
+        if (tid == 0) {
+            atomicExch(err, 1);
+            // the MMAs this block issued must be done before their TMEM is freed
+            if (last_commit >= 0)
+                (void)mbar_wait(&bars[last_commit % kStages], (uint32_t)((last_commit / kStages) & 1), wait_limit);
+        }
+        __syncthreads();
+    }
     tc_fence_after();
     if (ok) {
         const int row = m0 + warp * 32 + lane;
@@ -158,18 +185,31 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16 *__restri
     if (warp == 0) tmem_dealloc(tmem, kCols);
 }
 
+// The dynamic shared-memory opt-in of cudaFuncSetAttribute applies to the current
+// device only: it is made once per device and tile width, under a lock.
+constexpr int kMaxDevices = 64;
+std::mutex g_attr_mu;
+bool g_attr_done[kMaxDevices][4] = {};
+
+template <int BN> constexpr int bn_slot() { return BN == 128 ? 0 : (BN == 64 ? 1 : (BN == 32 ? 2 : 3)); }
+
 template <int BN>
 int launch_gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N, int K,
                 int accumulate, int ksplit, int *err, cudaStream_t s) {
     const int bytes = GemmSmem<BN>::kBytes;
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
-            return MFLBM_ECUDA;
-        configured = true;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MFLBM_ENODEV;
+    {
+        std::lock_guard<std::mutex> lock(g_attr_mu);
+        if (!g_attr_done[dev][bn_slot<BN>()]) {
+            if (cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+                return MFLBM_ECUDA;
+            g_attr_done[dev][bn_slot<BN>()] = true;
+        }
     }
     dim3 grid((M + 127) / 128, (N + BN - 1) / BN, ksplit);
-    k_gemm_bf16<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, M, N, K, accumulate, err);
+    k_gemm_bf16<BN><<<grid, 128, bytes, s>>>(A, lda, B, ldb, C, ldc, M, N, K, accumulate, err, g_wait_limit.load(),
+                                             g_skip_commit.load());
     return cudaPeekAtLastError() == cudaSuccess ? MFLBM_OK : MFLBM_ECUDA;
 }
 
@@ -206,6 +246,16 @@ extern "C" int32_t mflbm_nn_gemm_bf16(const void *A, int32_t lda, const void *B,
     if (M == 0 || N == 0) return MFLBM_OK;
     return nn::gemm_dispatch((const __nv_bfloat16 *)A, lda, (const __nv_bfloat16 *)B, ldb, C, ldc, M, N, K, accumulate, 1,
                              err, (cudaStream_t)stream);
+}
+
+// Diagnostics of the GEMM's timeout path (no counterpart in the reference): the probe
+// limit of every mbarrier wait of later GEMMs (<= 0: the default) and skip_commit = 1,
+// which makes the MMA thread issue no tensor-core work and no commit, so that every wait
+// runs out and *err is set.  Process-wide; not for concurrent use with real GEMMs.
+extern "C" int32_t mflbm_nn_set_wait(int64_t wait_limit, int32_t skip_commit) {
+    nn::g_wait_limit.store(wait_limit > 0 ? (long long)wait_limit : nn::kWaitLimit);
+    nn::g_skip_commit.store(skip_commit ? 1 : 0);
+    return MFLBM_OK;
 }
 
 // Split-K form for long reductions (weight gradients reduce over every voxel): ksplit

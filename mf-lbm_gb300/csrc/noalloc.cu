@@ -16,6 +16,12 @@
 // array and it keeps the last call's contents; each call writes all 2*nz slots it later
 // reads, so no clearing is needed.  Calls that overlap on the GPU (two streams, or two
 // host threads) race on the array and must be serialised by the caller.
+//
+// The array's device address is looked up once per device (cudaGetSymbolAddress, with
+// that device current) and kept for the life of the process.  cudaDeviceReset releases
+// the array together with every other allocation of that device, and the kept address
+// then points at nothing: a process that resets a device must not call this entry point
+// on that device afterwards.
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -117,10 +123,22 @@ extern "C" int32_t mflbm_saturation_noalloc(const double *phi, const int8_t *wal
         }
         scratch = g_addr[dev];
     }
+    // an error left by earlier work of the caller is reported as such and left in place
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return fail(MFLBM_ECUDA, std::string("a CUDA error from earlier work is pending: ") + cudaGetErrorString(e));
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     k_sat_slices<<<nz, kThreads, 0, s>>>(phi, walls, nx, ny, nz, static_cast<double *>(scratch));
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // this call's own launch error
+        return fail(MFLBM_ECUDA, std::string("k_sat_slices launch: ") + cudaGetErrorString(e));
+    }
     k_sat_finish<<<1, 1, 0, s>>>(static_cast<const double *>(scratch), nz, vol);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(MFLBM_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MFLBM_ECUDA, std::string("k_sat_finish launch: ") + cudaGetErrorString(e));
+    }
     return MFLBM_OK;
 }

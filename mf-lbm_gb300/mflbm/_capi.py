@@ -114,6 +114,8 @@ SIGNATURES = {
     "mflbm_ensemble_configure": (C.c_int32, [P, C.c_int32, C.c_int32]),
     "mflbm_ensemble_tune": (C.c_int32, [P, C.c_int32, P, C.c_int32]),
     "mflbm_ensemble_info": (C.c_int32, [P, P, P, P, P]),
+    "mflbm_ensemble_set_wait": (C.c_int32, [P, C.c_int64, C.c_int32]),
+    "mflbm_nn_set_wait": (C.c_int32, [C.c_int64, C.c_int32]),
     "mflbm_layout": (C.c_int32, [P]),
     "mflbm_init_velocity": (C.c_int32, [P, P, P, P, P, C.c_int32]),
     "mflbm_steady_monitor": (C.c_int32, [P, C.c_int32, P]),

@@ -61,6 +61,11 @@ class Ensemble:
     def configure(self, block, persistent):
         self._check(self.lib.mflbm_ensemble_configure(self.h, block, int(bool(persistent))))
 
+    def set_wait(self, spin_limit=0, unreachable=False):
+        """Grid-barrier poll limit (0: default) and the unreachable-barrier hook of the
+        timeout test; clears the barrier state."""
+        self._check(self.lib.mflbm_ensemble_set_wait(self.h, int(spin_limit), int(bool(unreachable))))
+
     def tune(self, steps=10):
         buf = C.create_string_buffer(8192)
         self._check(self.lib.mflbm_ensemble_tune(self.h, steps, buf, len(buf)))
