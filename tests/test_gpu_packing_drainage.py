@@ -1,0 +1,106 @@
+"""The packing-drainage configuration (sphere packing, porosity 0.22, inlet and outlet
+buffers, theta = 30, velocity inlet 5e-5, convective outlet) on a 64^2 x 64 crop with
+8-layer buffers, against the oracle.
+
+This is the configuration whose boundary-node lists come from the GPU preprocessing
+(mflbm_preprocess_geometry) and whose default build uses the compact solid records and
+fluid-cell gradient lists; the same lists go to the oracle.
+
+strict build: bit-identical f, g, phi and convective memory after 1, 2, 3 and 200 steps.
+default (FMA) build after 200 steps: max|dphi| <= 1e-6, max|du| <= 1e-10, |dS|/S <= 1e-10
+(the gates of the tube drainage); FP32 form: phi L1 <= 1e-3, |dS|/S <= 1e-3.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from mflbm import Solver
+from mflbm.workloads import packing_drainage
+from pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+STEPS = (1, 2, 3, 200)
+
+
+def _setup(sim, case):
+    sim.set_geometry(case["walls"], case["solid"], case["fluid"], case["w_in"])
+    sim.init_equilibrium(case["phi"])
+    sim.color_gradient()
+
+
+@pytest.fixture(scope="module")
+def crop():
+    case = packing_drainage(nxy=64, nzp=64, buffer=8, strict_fp=1, gpu_preprocess=True)
+    assert len(case["solid"]) > 1000 and len(case["fluid"]) > 1000
+    return case
+
+
+@pytest.fixture(scope="module")
+def oracle_states(crop):
+    orc = Oracle(crop["params"])
+    _setup(orc, crop)
+    out, done = {}, 0
+    for n in STEPS:
+        orc.run(1 + done, n - done)
+        done = n
+        out[n] = orc.download_state()
+    out["sat"] = orc.saturation()
+    out["macro"] = orc.macro()
+    orc.close()
+    return out
+
+
+def test_strict_bit_identical(crop, oracle_states):
+    gpu = Solver(crop["params"])
+    _setup(gpu, crop)
+    done = 0
+    for n in STEPS:
+        gpu.run(1 + done, n - done)
+        done = n
+        a, b = gpu.download_state(), oracle_states[n]
+        for k in ("f", "g", "phi", "f_convec", "g_convec", "phi_convec"):
+            assert np.array_equal(a[k], b[k]), (n, k, np.abs(a[k] - b[k]).max())
+    np.testing.assert_allclose(gpu.saturation(), oracle_states["sat"], rtol=1e-11)
+    gpu.close()
+
+
+def test_fma_build_after_200_steps(crop, oracle_states):
+    p = copy.copy(crop["params"])
+    p.strict_fp = 0
+    gpu = Solver(p)
+    _setup(gpu, crop)
+    gpu.run(1, 200)
+    a, b = gpu.download_state(), oracle_states[200]
+    inner = (slice(4, -4),) * 3
+    dphi = np.abs(a["phi"][inner] - b["phi"][inner]).max()
+    m, mo = gpu.macro(), oracle_states["macro"]
+    du = max(np.abs(m[k][1:-1, 1:-1, 1:-1] - mo[k][1:-1, 1:-1, 1:-1]).max() for k in ("u", "v", "w"))
+    v1, v2 = gpu.saturation()
+    o1, o2 = oracle_states["sat"]
+    ds = abs(v1 / (v1 + v2) - o1 / (o1 + o2)) / (o1 / (o1 + o2))
+    print(f"packing drainage, FMA build, 200 steps: max|dphi|={dphi:.3e} max|du|={du:.3e} dS/S={ds:.3e}")
+    assert dphi <= 1e-6
+    assert du <= 1e-10
+    assert ds <= 1e-10
+    gpu.close()
+
+
+def test_fp32_form_after_200_steps(crop, oracle_states):
+    p = copy.copy(crop["params"])
+    p.strict_fp = 0
+    p.precision = 1
+    gpu = Solver(p)
+    _setup(gpu, crop)
+    gpu.run(1, 200)
+    a, b = gpu.download_state(), oracle_states[200]
+    fluid = crop["walls"][2:-2, 2:-2, 2:-2] == 0
+    dphi = np.abs(a["phi"][4:-4, 4:-4, 4:-4] - b["phi"][4:-4, 4:-4, 4:-4])[fluid]
+    v1, v2 = gpu.saturation()
+    o1, o2 = oracle_states["sat"]
+    ds = abs(v1 / (v1 + v2) - o1 / (o1 + o2)) / (o1 / (o1 + o2))
+    print(f"packing drainage, FP32 form, 200 steps: phi L1={dphi.mean():.3e} max|dphi|={dphi.max():.3e} dS/S={ds:.3e}")
+    assert dphi.mean() <= 1e-3
+    assert ds <= 1e-3
+    gpu.close()
