@@ -197,6 +197,13 @@ int32_t mflbm_download_state(mflbm_ctx *ctx, double *const *f, double *const *g,
  * phi (halo 4) is required for multiphase and ignored for singlephase. */
 int32_t mflbm_init_equilibrium(mflbm_ctx *ctx, const double *phi);
 
+/* change_inlet_fluid_phase (multiphase_3D/0.src/Misc.F90:507-621), which the reference
+ * calls once after initialisation or restart when change_inlet_fluid_phase_cmd /= 0
+ * (Main_multiphase.F90:96-99): in every slot of the halo-1 box with z <= interface_z0,
+ * cmd 1 moves all of g into f (f <- f + g, g <- 0), cmd 2 all of f into g; cmd 0 does
+ * nothing.  phi is left as it is (the next collision recomputes it).  Synchronises. */
+int32_t mflbm_change_inlet_fluid_phase(mflbm_ctx *ctx, int32_t cmd, double interface_z0);
+
 /* One main_iteration_kernel for time step ntime (asynchronous). */
 int32_t mflbm_step(mflbm_ctx *ctx, int32_t ntime);
 

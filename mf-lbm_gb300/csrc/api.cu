@@ -828,6 +828,22 @@ int32_t mflbm_steady_monitor(mflbm_ctx *c, int32_t kind, double *out) {
     return MFLBM_OK;
 }
 
+int32_t mflbm_change_inlet_fluid_phase(mflbm_ctx *c, int32_t cmd, double interface_z0) {
+    int r = ready(c);
+    if (r) return r;
+    const mflbm_params &p = c->p;
+    if (!p.multiphase) return fail(c, MFLBM_EINVAL, "change_inlet_fluid_phase is multiphase only");
+    if (cmd < 0 || cmd > 2) return fail(c, MFLBM_EINVAL, "change_inlet_fluid_phase_cmd must be 0, 1 or 2");
+    if (cmd == 0 || !(interface_z0 >= 0.0)) return MFLBM_OK;
+    CK(c, cudaSetDevice(c->dev));
+    // k runs over the halo-1 box 0..nz+1; z = k on one rank, and z <= interface_z0
+    const int kmax = (int)std::min<double>(std::floor(interface_z0), (double)(p.nz + 1));
+    c->kt->change_inlet_phase(c->st, cmd, kmax, c->stream);
+    CK(c, cudaPeekAtLastError());
+    CK(c, cudaStreamSynchronize(c->stream));
+    return MFLBM_OK;
+}
+
 int32_t mflbm_step(mflbm_ctx *c, int32_t ntime) {
     int r = ready(c);
     if (r) return r;

@@ -1951,6 +1951,31 @@ __global__ void __launch_bounds__(MON_THREADS) k_steady(const T *__restrict__ ph
     }
 }
 
+// change_inlet_fluid_phase (multiphase_3D/0.src/Misc.F90:507-621): in every slot of the
+// halo-1 box with k <= kmax (z <= interface_z0 on one rank) one species takes the sum of
+// both populations and the other is emptied; to_f = 1 (cmd 1): f <- f + g, g <- 0;
+// to_f = 0 (cmd 2): g <- f + g, f <- 0.  One thread per (q, cell).
+template <class T>
+__global__ void k_change_inlet_phase(T *__restrict__ f, T *__restrict__ g, const Layout L, int kmax, int to_f) {
+    const int64_t nrow = L.nx + 2, nplane = nrow * (L.ny + 2), ncell = nplane * (kmax + 1);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 19 * ncell) return;
+    const int q = (int)(t / ncell);
+    const int64_t r = t - q * ncell;
+    const int k = (int)(r / nplane);
+    const int64_t r2 = r - k * nplane;
+    const int j = (int)(r2 / nrow), i = (int)(r2 - j * nrow);
+    const int64_t id = (int64_t)q * L.qs + L.cell(i, j, k);
+    const T a = f[id], b = g[id];
+    if (to_f) {
+        f[id] = a + b;
+        g[id] = T(0);
+    } else {
+        g[id] = a + b;
+        f[id] = T(0);
+    }
+}
+
 // FP64 host image <-> field array of type T (phi, gradient fields of the mixed form)
 template <class T>
 __global__ void k_field_in(T *__restrict__ dst, const double *__restrict__ src, int64_t n) {

@@ -97,6 +97,8 @@ struct KernelTable {
     int (*init_velocity)(const DevState &, const double *rho, int rest_base, cudaStream_t);
     // steady-state / breakthrough partials into out[7 * nz] (phi_old nullable)
     int (*steady)(const DevState &, void *phi_old, double *out, int obs_z, int copy_old, cudaStream_t);
+    // change_inlet_fluid_phase over the halo-1 planes k = 0..kmax (cmd 1: into f, 2: into g)
+    int (*change_inlet_phase)(const DevState &, int cmd, int kmax, cudaStream_t);
 };
 
 const KernelTable *kernels_fast();

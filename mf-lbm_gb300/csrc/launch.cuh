@@ -531,10 +531,20 @@ int steady(const DevState &st, void *phi_old, double *out, int obs_z, int copy_o
     return 1;
 }
 
+int change_inlet_phase(const DevState &st, int cmd, int kmax, cudaStream_t s) {
+    if (kmax < 0 || (cmd != 1 && cmd != 2)) return 0;
+    const Layout &L = st.L;
+    const int64_t n = (int64_t)19 * (L.nx + 2) * (L.ny + 2) * (kmax + 1);
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (mp_fp32(st)) k_change_inlet_phase<float><<<nb, 256, 0, s>>>(fs<float>(st), gs<float>(st), L, kmax, cmd == 1);
+    else k_change_inlet_phase<double><<<nb, 256, 0, s>>>(fs<double>(st), gs<double>(st), L, kmax, cmd == 1);
+    return 1;
+}
+
 const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,
                            init_equilibrium, convert_in,  convert_out, field_in,      field_out,
                            ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity,
-                           steady};
+                           steady,           change_inlet_phase};
 
 }  // namespace MFLBM_NS
 }  // namespace mflbm

@@ -127,6 +127,7 @@ SIGNATURES = {
     "mflbm_download_state": (C.c_int32, [P, P, P, P, P, P, P]),
     "mflbm_init_equilibrium": (C.c_int32, [P, P]),
     "mflbm_step": (C.c_int32, [P, C.c_int32]),
+    "mflbm_change_inlet_fluid_phase": (C.c_int32, [P, C.c_int32, C.c_double]),
     "mflbm_run": (C.c_int32, [P, C.c_int32, C.c_int32]),
     "mflbm_color_gradient": (C.c_int32, [P]),
     "mflbm_get_gradient": (C.c_int32, [P, P, P, P, P, P]),

@@ -74,6 +74,7 @@ class Run:
     n_exclude_outlet: int = 0
     convergence_criteria: float = 1e-6
     steady_state_option: int = 0
+    change_inlet_fluid_phase_cmd: int = 0
     flowrate: float = 0.0
     a_xy: float = 0.0
 
@@ -134,6 +135,9 @@ def make_run(deck, multiphase=True, device=0, precision=0, strict_fp=0):
         run.interface_z0 = _get(deck, "initial_interface_position", 0.0)
         run.initial_option = _get(deck, "initial_fluid_distribution_option", 1)
         run.sa_target = _get(deck, "target_fluid1_saturation", 0.0)
+        # applied once after initialisation or restart (Main_multiphase.F90:96-99) through
+        # Solver.change_inlet_fluid_phase(cmd, interface_z0)
+        run.change_inlet_fluid_phase_cmd = _get(deck, "change_inlet_fluid_phase_cmd", 0)
         if open_z:
             if p.inlet_bc == 1:
                 p.force_z = 0.0

@@ -183,6 +183,11 @@ class Solver:
         self._check(self.lib.mflbm_steady_monitor(self.ctx, kind, _ptr(out)))
         return out[:{0: 0, 1: 6, 2: 2, 3: 1}[kind]]
 
+    def change_inlet_fluid_phase(self, cmd, interface_z0):
+        """change_inlet_fluid_phase: cmd 1 moves species 2 into species 1 for z <= interface_z0,
+        cmd 2 the reverse (0 does nothing)."""
+        self._check(self.lib.mflbm_change_inlet_fluid_phase(self.ctx, int(cmd), float(interface_z0)))
+
     def saturation(self):
         a, b = C.c_double(), C.c_double()
         self._check(self.lib.mflbm_saturation(self.ctx, C.byref(a), C.byref(b)))

@@ -74,6 +74,7 @@ struct Orc {
     bool mp = false;
     std::vector<double> f[19], g[19];
     std::vector<double> phi, cnx, cny, cnz, cnorm, curv, u, v, w, rho;
+    std::vector<double> phi_old;   // steady_state_option 2 (Monitor.F90:287-365)
     std::vector<int8_t> walls;
     std::vector<double> w_in, fconv, gconv, phiconv;
     std::vector<mflbm_solid_bnd> sb;
@@ -1277,6 +1278,99 @@ int32_t orc_monitor(void *h, double *prof, double *scal, int32_t *status) {
     scal[0] = umax; scal[1] = usq1; scal[2] = usq2;
     if (std::isnan(umax) || std::sqrt(umax) > 0.5) bad = true;
     if (status) *status = bad ? MFLBM_FAILED : MFLBM_RUNNING;
+    return MFLBM_OK;
+}
+
+// The other monitors of the multiphase loop (Main_multiphase.F90:184-195), one kind per
+// call, with the outputs of mflbm_steady_monitor:
+//   kind 0: phi_old <- phi (the set-up of steady_state_option 2, Init_multiphase.F90:340-351)
+//   kind 1: monitor_multiphase_steady_capillarypressure (Monitor.F90:370-462):
+//           out = pc, pre_w, pre_nw, umax, i_w, i_nw
+//   kind 2: monitor_multiphase_steady_phasefield (Monitor.F90:287-365): out = max |phi -
+//           phi_old| over the fluid nodes, umax; then phi_old <- phi
+//   kind 3: monitor_breakthrough (Monitor.F90:472-507): out = fluid nodes with phi > 0 in
+//           the plane obs_z = nz - 1
+// umax is the square root of the largest |u|^2 over the fluid nodes.  The sums run in the
+// reference's loop order (k, then j, then i).
+int32_t orc_steady_monitor(void *h, int32_t kind, double *out) {
+    Orc *o = (Orc *)h;
+    if (!o->mp) { o->err = "steady-state monitors are multiphase"; return MFLBM_EINVAL; }
+    if (kind < 0 || kind > 3 || (kind > 0 && !out)) { o->err = "kind must be 0..3 and out non-NULL"; return MFLBM_EINVAL; }
+    const int nx = o->nx, ny = o->ny, nz = o->nz;
+    static const double eps = 1.110223025e-16;   // Misc_module eps (Module.F90:8)
+    if (kind == 0 || o->phi_old.empty()) {
+        o->phi_old = o->phi;
+        if (kind == 0) return MFLBM_OK;
+    }
+    if (kind == 3) {
+        const int obs_z = nz - 1;
+        int itemp = 0;
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (o->WALL(i, j, obs_z) == 0 && o->PHI(i, j, obs_z) > 0.0) itemp = itemp + 1;
+        out[0] = (double)itemp;
+        return MFLBM_OK;
+    }
+    macro_vars(*o);
+    double umax = 0.0, d_phi_max = 0.0;
+    double pre_w = 0.0, pre_nw = 0.0;
+    int i_w = 0, i_nw = 0;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                const int64_t id = o->I1(i, j, k), i4 = o->I4(i, j, k);
+                const int wi = o->WALL(i, j, k);
+                const double tmp1 = (o->u[id] * o->u[id] + o->v[id] * o->v[id] + o->w[id] * o->w[id]) * (double)(1 - wi);
+                if (umax < tmp1) umax = tmp1;
+                if (kind == 2) {
+                    const double tmp2 = std::fabs(o->phi[i4] - o->phi_old[i4]) * (double)(1 - wi);
+                    if (d_phi_max < tmp2) d_phi_max = tmp2;
+                } else if (wi == 0) {
+                    if (o->phi[i4] < -0.99) { pre_w = pre_w + o->rho[id]; i_w = i_w + 1; }
+                    if (o->phi[i4] > 0.99) { pre_nw = pre_nw + o->rho[id]; i_nw = i_nw + 1; }
+                }
+            }
+    if (kind == 2) {
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) o->phi_old[o->I4(i, j, k)] = o->PHI(i, j, k);
+        out[0] = d_phi_max;
+        out[1] = std::sqrt(umax);
+        return MFLBM_OK;
+    }
+    const double pw = pre_w / ((double)i_w + eps), pnw = pre_nw / ((double)i_nw + eps);
+    out[0] = (pnw - pw) / 3.0;
+    out[1] = pw;
+    out[2] = pnw;
+    out[3] = std::sqrt(umax);
+    out[4] = (double)i_w;
+    out[5] = (double)i_nw;
+    return MFLBM_OK;
+}
+
+// change_inlet_fluid_phase (multiphase_3D/0.src/Misc.F90:507-621) for one rank: every
+// slot of the halo-1 box (k = 1-overlap .. nz+overlap, overlap = 1) with z = k <=
+// interface_z0; cmd 1: f = f + g, g = 0; cmd 2: g = f + g, f = 0.
+int32_t orc_change_inlet_fluid_phase(void *h, int32_t cmd, double interface_z0) {
+    Orc *o = (Orc *)h;
+    if (!o->mp) { o->err = "change_inlet_fluid_phase is multiphase only"; return MFLBM_EINVAL; }
+    if (cmd < 0 || cmd > 2) { o->err = "change_inlet_fluid_phase_cmd must be 0, 1 or 2"; return MFLBM_EINVAL; }
+    for (int k = 0; k <= o->nz + 1; ++k)
+        for (int j = 0; j <= o->ny + 1; ++j)
+            for (int i = 0; i <= o->nx + 1; ++i) {
+                const int z = k;
+                if (!((double)z <= interface_z0)) continue;
+                const int64_t id = o->I1(i, j, k);
+                for (int q = 0; q < 19; ++q) {
+                    if (cmd == 1) {
+                        o->f[q][id] = o->f[q][id] + o->g[q][id];
+                        o->g[q][id] = 0.0;
+                    } else if (cmd == 2) {
+                        o->g[q][id] = o->f[q][id] + o->g[q][id];
+                        o->f[q][id] = 0.0;
+                    }
+                }
+            }
     return MFLBM_OK;
 }
 

@@ -50,6 +50,8 @@ def load(variant="strict"):
         "orc_macro": (C.c_int32, [P, P, P, P, P, P]),
         "orc_monitor": (C.c_int32, [P, P, P, P]),
         "orc_saturation": (C.c_int32, [P, P, P]),
+        "orc_steady_monitor": (C.c_int32, [P, C.c_int32, P]),
+        "orc_change_inlet_fluid_phase": (C.c_int32, [P, C.c_int32, C.c_double]),
         "orc_set_threads": (C.c_int32, [C.c_int32]),
         "orc_set_walls": (C.c_int64, [P, P, P]),
         "orc_geometry_preprocess": (C.c_int32, [P, P, C.c_double, P, P, P, P]),
@@ -182,6 +184,15 @@ class Oracle:
         a, b = C.c_double(), C.c_double()
         self._check(self.lib.orc_saturation(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def change_inlet_fluid_phase(self, cmd, interface_z0):
+        self._check(self.lib.orc_change_inlet_fluid_phase(self.h, int(cmd), float(interface_z0)))
+
+    def steady_monitor(self, kind):
+        n = {0: 0, 1: 6, 2: 2, 3: 1}[kind]
+        out = np.zeros(max(n, 1))
+        self._check(self.lib.orc_steady_monitor(self.h, kind, _ptr(out)))
+        return out[:n]
 
     def close(self):
         if getattr(self, "h", None):

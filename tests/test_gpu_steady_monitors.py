@@ -45,3 +45,27 @@ def test_capillary_pressure_phase_field_and_breakthrough(precision, tmp_path):
     assert (tmp_path / "out1.output" / "steady_monitor_capillary_pressure_error.dat").read_text().count("\n") == 1
     assert output.breakthrough(cnt) == (output.CONVERGED if cnt >= 1 else output.RUNNING)
     sim.close()
+
+
+def test_steady_monitors_match_the_oracle():
+    """The same monitors on the GPU (strict build) and on the oracle's restatement of
+    Monitor.F90:287-507 after the same steps: maxima and counts exact, sums to rtol 1e-12."""
+    from pyoracle import Oracle
+    case = mp_case(per=(0, 0, 0), inlet=1, outlet=1, strict=1)
+    sims = [Solver(case["params"]), Oracle(case["params"])]
+    res = []
+    for sim in sims:
+        load_case(sim, case)
+        sim.steady_monitor(0)
+        sim.run(1, 8)
+        r = {1: sim.steady_monitor(1), 2: sim.steady_monitor(2)}
+        sim.run(9, 4)
+        r["2b"] = sim.steady_monitor(2)
+        r[3] = sim.steady_monitor(3)
+        res.append(r)
+        sim.close()
+    g, o = res
+    np.testing.assert_allclose(g[1][:3], o[1][:3], rtol=1e-12)
+    assert g[1][3] == o[1][3] and g[1][4] == o[1][4] and g[1][5] == o[1][5]
+    assert np.array_equal(g[2], o[2]) and np.array_equal(g["2b"], o["2b"])
+    assert g[3][0] == o[3][0]
