@@ -10,6 +10,7 @@
 // mflbm_run replays the same launches from CUDA graphs captured once per context.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -271,6 +272,54 @@ int ready(mflbm_ctx *c) {
     return MFLBM_OK;
 }
 
+// The error word of the sweep kernels (set when a bounded wait gave up); read and cleared
+// at the calls that synchronise.  Synchronises the context stream.
+int check_device_err(mflbm_ctx *c) {
+    int32_t e = 0;
+    CK(c, cudaMemcpyAsync(&e, c->st.err, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (e) {
+        CK(c, cudaMemsetAsync(c->st.err, 0, sizeof(int32_t), c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        return fail(c, MFLBM_ETIMEOUT, "a bounded wait of the TMA list sweep gave up; the PDF state is undefined");
+    }
+    return MFLBM_OK;
+}
+
+// Tensor map of the fluid-list arrays for the TMA even step: dimension 0 the nfl fluid
+// nodes (contiguous), dimension 1 the 19 direction arrays (pitch lstride elements), box
+// 128 nodes x 19 directions, no swizzle, zero fill outside.  The driver's encoder is
+// reached through the runtime's entry-point query (no link against libcuda).  Returns
+// false when the encoder is unavailable or rejects the map (the plain sweep then runs).
+bool encode_list_map(mflbm_ctx *c) {
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return false;
+        }
+        encode = reinterpret_cast<Encode>(fn);
+    }
+    const DevState &st = c->st;
+    if (st.nfl <= 0) return false;
+    const CUtensorMapDataType dt = c->elt == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64
+                                 : (c->elt == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16);
+    const cuuint64_t dims[2] = {(cuuint64_t)st.nfl, 19};
+    const cuuint64_t strides[1] = {(cuuint64_t)st.lstride * c->elt};
+    const cuuint32_t box[2] = {128, 19};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(&c->st.tmap, dt, 2, c->pdf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
@@ -393,6 +442,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.w, n1(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.rho, n1(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.mon, (int64_t)kMonNQ * p.nz))) goto fail_create;
+    if ((r = dalloc(c, &c->st.err, 1))) goto fail_create;
     // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
     // phase field when that is larger
     if ((!f64_storage(p) || !p.multiphase) &&
@@ -518,6 +568,10 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             st.nfl = (int)ll.nf;
             st.lseg = seg;
             st.ncell = 0;
+            // the TMA even step, unless MFLBM_NO_TMA is set (a diagnostic switch that selects
+            // the plain even step, for comparisons)
+            const char *no_tma = std::getenv("MFLBM_NO_TMA");
+            st.tma = (!no_tma || !*no_tma || std::strcmp(no_tma, "0") == 0) && encode_list_map(c) ? 1 : 0;
             c->st.ns = 0;
             c->st.nf = 0;
             CK(c, cudaDeviceSynchronize());
@@ -737,7 +791,7 @@ int32_t mflbm_download_state(mflbm_ctx *c, double *const *f, double *const *g, d
     if (p.multiphase && phi_convec)
         CK(c, cudaMemcpyAsync(phi_convec, c->st.phiconv, sizeof(double) * nplane(p), cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    return MFLBM_OK;
+    return check_device_err(c);
 }
 
 int32_t mflbm_init_equilibrium(mflbm_ctx *c, const double *phi) {
@@ -925,6 +979,7 @@ int32_t mflbm_get_profile(mflbm_ctx *c, double *region_ms, double *collide_ms, i
     CK(c, cudaEventRecord(c->region1, c->stream));
     int r = drain_events(c);
     if (r) return r;
+    if ((r = check_device_err(c))) return r;
     CK(c, cudaEventSynchronize(c->region1));
     float rms = 0.f;
     CK(c, cudaEventElapsedTime(&rms, c->region0, c->region1));
@@ -990,6 +1045,7 @@ int32_t mflbm_monitor(mflbm_ctx *c, double *profiles, double *scalars, int32_t *
     CK(c, cudaPeekAtLastError());
     CK(c, cudaMemcpyAsync(c->h_mon.data(), c->st.mon, sizeof(double) * kMonNQ * p.nz, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    if ((r = check_device_err(c))) return r;
     const int nz = p.nz;
     const double *m = c->h_mon.data();
     bool bad = false;
@@ -1039,7 +1095,7 @@ int32_t mflbm_synchronize(mflbm_ctx *c) {
     if (!c) return MFLBM_EINVAL;
     CK(c, cudaSetDevice(c->dev));
     CK(c, cudaStreamSynchronize(c->stream));
-    return MFLBM_OK;
+    return check_device_err(c);
 }
 
 }  // extern "C"

@@ -9,6 +9,7 @@
 // The host layer picks the flavour per context (mflbm_params.strict_fp).
 #pragma once
 #include <type_traits>
+#include "bulk.cuh"
 #include "common.cuh"
 #include "kernels_api.h"
 
@@ -1554,6 +1555,26 @@ __global__ void k_convert_out(double *__restrict__ dst, const S *__restrict__ sr
 // nb[(d-1)*nf + x] is the slot of x + e_d (see listlayout.h).  The arithmetic is the
 // dense kernel's (k_sp_step), so the strict flavour stays bit-identical to the oracle.
 // ---------------------------------------------------------------------------------
+// the singlephase collision of one node in the sweep's arithmetic type (shared by the list
+// sweeps): the double-word form, the reference's order (strict build) or the pair form
+template <class S, bool UNIT>
+__device__ __forceinline__ void sp_collide(typename Store<S>::RS (&ft)[19], const StepParams &P,
+                                           const MrtFold<typename Store<S>::RS> &cf) {
+    using R = typename Store<S>::RS;
+    if constexpr (std::is_same<R, ff>::value) {
+        mrt_collide_ff<UNIT>(ft, cf);
+    } else {
+#ifdef MFLBM_STRICT
+        const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
+                      ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
+        mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi),
+                       R(P.s_t));
+#else
+        mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
+#endif
+    }
+}
+
 // one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
 template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
@@ -1573,18 +1594,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
 #pragma unroll
         for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
     }
-    if constexpr (std::is_same<R, ff>::value) {
-        mrt_collide_ff<UNIT>(ft, cf);
-    } else {
-#ifdef MFLBM_STRICT
-        const R den = ft[0] + ft[1] + ft[2] + ft[3] + ft[4] + ft[5] + ft[6] + ft[7] + ft[8] + ft[9] + ft[10] + ft[11] +
-                      ft[12] + ft[13] + ft[14] + ft[15] + ft[16] + ft[17] + ft[18];
-        mrt_collide<R>(ft, den, R(0.0), R(0.0), R(P.force_z), R(P.s_e), R(P.s_e2), R(P.s_q), R(P.s_nu), R(P.s_pi),
-                       R(P.s_t));
-#else
-        mrt_collide_pairs<R, false, true, UNIT>(ft, R(0.0), R(0.0), R(0.0), cf.fz, cf);
-#endif
-    }
+    sp_collide<S, UNIT>(ft, P, cf);
     const R sc = R(scale);
     if (ODD) {
         st_sweep<S>(A, t, 0, ft[0], sc);
@@ -1603,6 +1613,101 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
+}
+
+// ---------------------------------------------------------------------------------
+// The even step of the list sweep through the tensor memory accelerator (TMA).  The even
+// step reads A_opp(q)[x] and writes A_q[x] over a contiguous range of fluid nodes, so one
+// tiled load brings a 19 x 128 box (every direction array, 128 consecutive nodes) into
+// shared memory, the collision runs from there, and one tiled store writes the box back.
+// A persistent grid walks the tiles.  In each block one thread of warp 4 issues the copies
+// and warps 0-3 compute, one node per thread; two shared-memory stages let the load of the
+// next tile and the store of the last one overlap the arithmetic.  Stage hand-over uses
+// mbarriers: `full` completes with the load's byte count, `empty` when all 128 computing
+// threads have written their results (and fenced them for the async proxy).  The tensor's
+// extent is the nf fluid nodes: columns of the last tile past nf load as zeros and are
+// not stored, so the link slots after nf are untouched.  Every wait is bounded; a wait
+// that runs out sets *err, and the copy thread waits (bounded again) for the loads it
+// issued before the block exits.
+// ---------------------------------------------------------------------------------
+constexpr int kTmaNodes = 128;            // nodes per tile = computing threads per block
+constexpr int kTmaStages = 2;
+constexpr long long kTmaWait = 1ll << 26; // probes of one wait before it gives up
+
+template <class S> struct TmaTile { static constexpr int bytes = 19 * kTmaNodes * (int)sizeof(S); };
+
+template <class S, bool UNIT>
+__global__ void __launch_bounds__(kTmaNodes + 32, 4)
+    k_sp_list_even_tma(const __grid_constant__ CUtensorMap map, const int nf, const StepParams P,
+                       const MrtFold<typename Store<S>::RS> cf, const float scale, int32_t *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ uint64_t full[kTmaStages], empty[kTmaStages];
+    S *tiles = reinterpret_cast<S *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int tid = threadIdx.x;
+    const int ntiles = (nf + kTmaNodes - 1) / kTmaNodes;
+    const int m = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            bulk::mbar_init(&full[s], 1);
+            bulk::mbar_init(&empty[s], kTmaNodes);
+        }
+        bulk::fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid >= kTmaNodes) {
+        if (tid != kTmaNodes) return;
+        // copy thread: tile n goes to stage n % kTmaStages; before reloading a stage, the
+        // results of the tile it held are stored and the store has read them out
+        int last_load[kTmaStages];
+        for (int s = 0; s < kTmaStages; ++s) last_load[s] = -1;
+        bool ok = true;
+        for (int n = 0; n < m + kTmaStages; ++n) {
+            const int s = n % kTmaStages;
+            S *buf = tiles + s * 19 * kTmaNodes;
+            if (n >= kTmaStages) {
+                const int np = n - kTmaStages;
+                if (!bulk::mbar_wait(&empty[s], (uint32_t)((np / kTmaStages) & 1), kTmaWait)) {
+                    ok = false;
+                    break;
+                }
+                bulk::tma_store_2d(&map, ((int)blockIdx.x + np * (int)gridDim.x) * kTmaNodes, 0, buf);
+                bulk::bulk_commit();
+                bulk::bulk_wait_read0();
+            }
+            if (n < m) {
+                bulk::mbar_arrive_expect_tx(&full[s], (uint32_t)TmaTile<S>::bytes);
+                bulk::tma_load_2d(buf, &map, ((int)blockIdx.x + n * (int)gridDim.x) * kTmaNodes, 0, &full[s]);
+                last_load[s] = n;
+            }
+        }
+        bulk::bulk_wait0();
+        if (!ok) {
+            atomicExch(err, 1);
+            for (int s = 0; s < kTmaStages; ++s)
+                if (last_load[s] >= 0)
+                    (void)bulk::mbar_wait(&full[s], (uint32_t)((last_load[s] / kTmaStages) & 1), kTmaWait);
+        }
+        return;
+    }
+    using R = typename Store<S>::RS;
+    const R inv_scale = R(1.0f / scale);
+    const R sc = R(scale);
+    for (int n = 0; n < m; ++n) {
+        const int s = n % kTmaStages;
+        S *buf = tiles + s * 19 * kTmaNodes;
+        if (!bulk::mbar_wait(&full[s], (uint32_t)((n / kTmaStages) & 1), kTmaWait)) {
+            atomicExch(err, 1);
+            break;
+        }
+        R ft[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(buf, (int64_t)OPP(q) * kTmaNodes + tid, q, inv_scale);
+        sp_collide<S, UNIT>(ft, P, cf);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) st_sweep<S>(buf, (int64_t)q * kTmaNodes + tid, q, ft[q], sc);
+        bulk::fence_async_smem();
+        bulk::mbar_arrive(&empty[s]);
+    }
 }
 
 // ---------------------------------------------------------------------------------

@@ -3,6 +3,7 @@
 // KernelTable; the ordering of one time step lives only in api.cu.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include "common.cuh"
 
@@ -52,6 +53,11 @@ struct DevState {
     int64_t nlink;
     int nfl;
     const int32_t *lseg;   // [nz+1] first fluid index of every z slice
+    // tensor map of the list arrays for the TMA even step: a 2-D tensor of 19 rows (one per
+    // direction array, row pitch lstride elements) by nfl fluid nodes; tma = 1 when valid
+    CUtensorMap tmap;
+    int tma;
+    int32_t *err;          // device word set when a bounded wait of a sweep kernel gave up
     MrtFold<double> fold;    // singlephase MRT coefficients of the default build (FP64 collision)
     MrtFold<float> fold32;   // the same, converted once on the host for FP32 collision
     MrtFold<ff> foldff;      // the same as double words (MFLBM_FP64FF collision)

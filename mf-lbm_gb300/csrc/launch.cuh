@@ -24,8 +24,36 @@ template <> const MrtFold<double> &fold_of<double>(const DevState &st) { return 
 template <> const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
 template <> const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldff; }
 
+// The TMA even step: a persistent grid of as many blocks as fit on the device at once
+// (blocks per SM from the occupancy calculator, cached per device), at most one per tile.
+template <class S, bool UNIT>
+int even_tma(const DevState &st, cudaStream_t s) {
+    const int ntiles = (st.nfl + kTmaNodes - 1) / kTmaNodes;
+    if (ntiles == 0) return 0;
+    const int smem = kTmaStages * TmaTile<S>::bytes + 1024;
+    static int max_grid[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    if (max_grid[dev] == 0) {
+        int per = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sp_list_even_tma<S, UNIT>, kTmaNodes + 32, smem) !=
+                cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || per < 1)
+            return -1;
+        max_grid[dev] = per * sms;
+    }
+    const int grid = ntiles < max_grid[dev] ? ntiles : max_grid[dev];
+    k_sp_list_even_tma<S, UNIT><<<grid, kTmaNodes + 32, smem, s>>>(st.tmap, st.nfl, st.P,
+                                                                   fold_of<typename Store<S>::RS>(st), st.scale, st.err);
+    return 1;
+}
+
 template <class S>
 int collide_list(const DevState &st, bool odd, cudaStream_t s) {
+    if (!odd && st.tma) {
+        const int r = st.unit ? even_tma<S, true>(st, s) : even_tma<S, false>(st, s);
+        if (r >= 0) return r;
+    }
     const unsigned nb = (unsigned)((st.nfl + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::RS>(st);
     if (st.unit) {

@@ -2,7 +2,7 @@
 build), at sizes the CPU oracle cannot afford: the Laplace law over three drop radii
 and the static contact angle of an attached drop for three prescribed angles.
 
-Laplace (option 5, 64^3 box): dp R / (2 gamma) within 4 % at R = 10, 2 % at R = 14 and
+Laplace (option 5, 80^3 box): dp R / (2 gamma) within 4 % at R = 10, 2 % at R = 14 and
 R = 18, approaching 1 as R grows (the interface has a fixed width of a few nodes).
 Contact angle (option 3, 32 x 64 x 64, R0 = 16, 16000 steps): the drop's angle is
 180 - theta within 3 degrees at the plane of the wetting nodes (x = 2); the angles at the
@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 def test_laplace_law_three_radii():
     ratios = []
     for R0 in (10.0, 14.0, 18.0):
-        case = kat.drop_case(66, 64, 5, R0)
+        case = kat.drop_case(82, 80, 5, R0)
         with Solver(case["params"]) as sim:
             kat.start(sim, case)
             sim.run(1, 1000)
