@@ -635,6 +635,12 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     c->st.n_gcell_n = 0;
     c->st.n_gcell_c = 0;
     c->st.sbc = nullptr;
+    // the shared-memory stencils, unless MFLBM_GRADIENT_LISTS is set (a diagnostic switch
+    // that selects the fluid-cell list kernels, for comparisons)
+    {
+        const char *gl = std::getenv("MFLBM_GRADIENT_LISTS");
+        c->st.gtile = (!gl || !*gl || std::strcmp(gl, "0") == 0) ? 1 : 0;
+    }
     if (!cell_packable(p.nx, p.ny, p.nz)) return MFLBM_OK;  // the full-box kernels serve
     std::vector<uint32_t> gn, gc;
     for (int k = -1; k <= p.nz + 2; ++k)

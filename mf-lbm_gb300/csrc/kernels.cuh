@@ -1050,9 +1050,11 @@ __global__ void k_extrap_phi(T *__restrict__ phi, const SolidBnd *__restrict__ s
 
 // The same two extrapolations over the compact solid-boundary records (SolidBndC: packed
 // cell, bit mask of the fluid-neighbour directions, la_weight): 16 bytes read per node
-// instead of 96.  The set bits are visited in ascending direction order, which is the order
-// of the neighbour list whenever the context builds these records, so the sums are the
-// same operations in the same order.
+// instead of 96.  The 18 directions are visited in ascending order, which is the order of
+// the neighbour list whenever the context builds these records, so the sums are the same
+// operations in the same order.  The loop is unrolled with one predicated gather per
+// direction, so a node's loads are all in flight at once instead of one per iteration
+// of a data-dependent loop.
 template <class T>
 __global__ void k_extrap_phi_c(T *__restrict__ phi, const SolidBndC *__restrict__ sb, int ns, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1060,13 +1062,16 @@ __global__ void k_extrap_phi_c(T *__restrict__ phi, const SolidBndC *__restrict_
     const SolidBndC s = sb[t];
     int ix, iy, iz;
     unpack_cell(s.ijk, ix, iy, iz);
+    const int64_t c = L.i4(ix, iy, iz);
+    T v[18];
+#pragma unroll
+    for (int ie = 1; ie <= 18; ++ie)
+        v[ie - 1] = (s.mask >> (ie - 1)) & 1u ? phi[c + EX(ie) + L.h4x * EY(ie) + L.h4xy * EZ(ie)] : T(0.0);
     T acc = T(0.0);
-    for (uint32_t m = s.mask; m; m &= m - 1u) {
-        const int ie = __ffs((int)m);
-        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
-        acc = acc + phi[L.i4(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie])] * w;
-    }
-    phi[L.i4(ix, iy, iz)] = acc / T(s.la_weight);
+#pragma unroll
+    for (int ie = 1; ie <= 18; ++ie)
+        if ((s.mask >> (ie - 1)) & 1u) acc = acc + v[ie - 1] * (ie <= 6 ? T(w_equ_1) : T(w_equ_2));
+    phi[c] = acc / T(s.la_weight);
 }
 
 template <class T>
@@ -1078,36 +1083,44 @@ __global__ void k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *
     int ix, iy, iz;
     unpack_cell(s.ijk, ix, iy, iz);
     if (!(ix >= 0 && ix <= L.nx + 1 && iy >= 0 && iy <= L.ny + 1 && iz >= 0 && iz <= L.nz + 1)) return;
-    T ax = T(0.0), ay = T(0.0), az = T(0.0);
-    for (uint32_t m = s.mask; m; m &= m - 1u) {
-        const int ie = __ffs((int)m);
-        const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
-        const int64_t nb = L.i2(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie]);
-        ax = ax + cnx[nb] * w;
-        ay = ay + cny[nb] * w;
-        az = az + cnz[nb] * w;
-    }
     const int64_t id = L.i2(ix, iy, iz);
+    T vx[18], vy[18], vz[18];
+#pragma unroll
+    for (int ie = 1; ie <= 18; ++ie) {
+        const bool on = (s.mask >> (ie - 1)) & 1u;
+        const int64_t nb = id + EX(ie) + L.h2x * EY(ie) + L.h2xy * EZ(ie);
+        vx[ie - 1] = on ? cnx[nb] : T(0.0);
+        vy[ie - 1] = on ? cny[nb] : T(0.0);
+        vz[ie - 1] = on ? cnz[nb] : T(0.0);
+    }
+    T ax = T(0.0), ay = T(0.0), az = T(0.0);
+#pragma unroll
+    for (int ie = 1; ie <= 18; ++ie) {
+        if ((s.mask >> (ie - 1)) & 1u) {
+            const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
+            ax = ax + vx[ie - 1] * w;
+            ay = ay + vy[ie - 1] * w;
+            az = az + vz[ie - 1] * w;
+        }
+    }
     const T lw = T(s.la_weight);
     cnx[id] = ax / lw;
     cny[id] = ay / lw;
     cnz[id] = az / lw;
 }
 
-// ISO4 gradient and unit normal of one cell (:33-79)
-template <class T>
-__device__ __forceinline__ void normals_at(const T *__restrict__ phi, int i, int j, int k, int64_t id,
-                                           T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                                           T *__restrict__ cnorm, const Layout &L) {
-    auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
+// ISO4 gradient and unit normal from a phi accessor P(a, b, c) = phi at offset (a, b, c)
+// (:33-79); shared by the global-memory and shared-memory forms
+template <class T, class PA>
+__device__ __forceinline__ void normals_of(PA P, T &gx, T &gy, T &gz, T &cn) {
     const T c1 = T(ISO4_1), c2 = T(ISO4_2);
-    T gx = c1 * (P(1, 0, 0) - P(-1, 0, 0)) +
-           c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
-    T gy = c1 * (P(0, 1, 0) - P(0, -1, 0)) +
-           c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
-    T gz = c1 * (P(0, 0, 1) - P(0, 0, -1)) +
-           c2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
-    T cn = sqrt(gx * gx + gy * gy + gz * gz);
+    gx = c1 * (P(1, 0, 0) - P(-1, 0, 0)) +
+         c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(1, -1, 0) - P(-1, 1, 0) + P(1, 0, 1) - P(-1, 0, -1) + P(1, 0, -1) - P(-1, 0, 1));
+    gy = c1 * (P(0, 1, 0) - P(0, -1, 0)) +
+         c2 * (P(1, 1, 0) - P(-1, -1, 0) + P(-1, 1, 0) - P(1, -1, 0) + P(0, 1, 1) - P(0, -1, -1) + P(0, 1, -1) - P(0, -1, 1));
+    gz = c1 * (P(0, 0, 1) - P(0, 0, -1)) +
+         c2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
+    cn = sqrt(gx * gx + gy * gy + gz * gz);
     if (cn < T(1e-6)) {
         gx = T(0.0); gy = T(0.0); gz = T(0.0); cn = T(0.0);
     } else {
@@ -1118,6 +1131,16 @@ __device__ __forceinline__ void normals_at(const T *__restrict__ phi, int i, int
         gx = gx * inv; gy = gy * inv; gz = gz * inv;
 #endif
     }
+}
+
+// ISO4 gradient and unit normal of one cell from global memory
+template <class T>
+__device__ __forceinline__ void normals_at(const T *__restrict__ phi, int i, int j, int k, int64_t id,
+                                           T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+                                           T *__restrict__ cnorm, const Layout &L) {
+    auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
+    T gx, gy, gz, cn;
+    normals_of<T>(P, gx, gy, gz, cn);
     cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
 }
 
@@ -1270,14 +1293,10 @@ __global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__
 }
 
 // curvature of one cell (:113-201)
-template <class T>
-__device__ __forceinline__ void curvature_at(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                             const T *__restrict__ cnz, T *__restrict__ curv, int i, int j, int k,
-                                             const Layout &L) {
+// curvature from accessors X, Y, Z of cn_x, cn_y, cn_z at offset (a, b, c) (:113-201)
+template <class T, class FX, class FY, class FZ>
+__device__ __forceinline__ T curvature_of(FX X, FY Y, FZ Z) {
     const T c1 = T(ISO4_1), c2 = T(ISO4_2);
-    auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
-    auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
-    auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };
     const T kxx = c1 * (X(1, 0, 0) - X(-1, 0, 0)) +
                        c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
     const T kyy = c1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
@@ -1297,8 +1316,18 @@ __device__ __forceinline__ void curvature_at(const T *__restrict__ cnx, const T 
     const T kzy = c1 * (Z(0, 1, 0) - Z(0, -1, 0)) +
                        c2 * (Z(1, 1, 0) - Z(-1, -1, 0) + Z(-1, 1, 0) - Z(1, -1, 0) + Z(0, 1, 1) - Z(0, -1, -1) + Z(0, 1, -1) - Z(0, -1, 1));
     const T cx = X(0, 0, 0), cy = Y(0, 0, 0), cz = Z(0, 0, 0);
-    curv[L.i1(i, j, k)] = (cx * cx - T(1.0)) * kxx + (cy * cy - T(1.0)) * kyy + (cz * cz - T(1.0)) * kzz + cx * cy * (kxy + kyx) +
-                          cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz);
+    return (cx * cx - T(1.0)) * kxx + (cy * cy - T(1.0)) * kyy + (cz * cz - T(1.0)) * kzz + cx * cy * (kxy + kyx) +
+           cx * cz * (kxz + kzx) + cy * cz * (kzy + kyz);
+}
+
+template <class T>
+__device__ __forceinline__ void curvature_at(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                             const T *__restrict__ cnz, T *__restrict__ curv, int i, int j, int k,
+                                             const Layout &L) {
+    auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
+    auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
+    auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };
+    curv[L.i1(i, j, k)] = curvature_of<T>(X, Y, Z);
 }
 
 // over [1, n]^3, every cell
@@ -1330,6 +1359,126 @@ __global__ void __launch_bounds__(256) k_curvature_list(const T *__restrict__ cn
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
     curvature_at<T>(cnx, cny, cnz, curv, i, j, k, L);
+}
+
+// Shared-memory forms of the two stencils (default build): a block of 32 x 8 threads owns
+// a 32 x 8 column of cells and marches it up a chunk of GRAD_KCH planes.  The planes
+// k-1, k, k+1 of the input field(s), with a one-cell halo in i and j, sit in a ring of
+// three shared-memory planes; each step stores the plane that was prefetched into
+// registers during the previous step, then issues the loads of the next one before
+// computing, so global loads overlap the stencil arithmetic.  Every input value is read
+// from global memory once per column (plus the halo) instead of once per neighbour, with
+// coalesced rows.  Outputs go to the same cells as the fluid-cell lists (normals: walls != 1
+// in [-1, n+2]^3; curvature: walls == 0 in [1, n]^3) with the same expressions.
+constexpr int GRAD_TX = 32, GRAD_TY = 8, GRAD_KCH = 16;
+constexpr int GRAD_PW = GRAD_TX + 2, GRAD_PH = GRAD_TY + 2, GRAD_PN = GRAD_PW * GRAD_PH;
+constexpr int GRAD_LD = (GRAD_PN + GRAD_TX * GRAD_TY - 1) / (GRAD_TX * GRAD_TY);   // loads per thread per plane
+
+// NF input fields of halo h (stride hx, hxy in elements, origin offset o so that cell
+// (i, j, k) is at o + i + hx j + hxy k), valid for i in [-h+1, nx+h] etc.
+template <class T, int NF>
+struct GradPlanes {
+    const T *src[NF];
+    int64_t hx, hxy, o;
+    int imax, jmax, kmax;   // largest valid index per axis
+    __device__ __forceinline__ void fetch(T (&r)[NF][GRAD_LD], int i0, int j0, int k, int tid) const {
+#pragma unroll
+        for (int l = 0; l < GRAD_LD; ++l) {
+            const int idx = tid + l * GRAD_TX * GRAD_TY;
+            const int ii = idx % GRAD_PW, jj = idx / GRAD_PW;
+            const int i = i0 - 1 + ii, j = j0 - 1 + jj;
+            const bool ok = idx < GRAD_PN && i <= imax && j <= jmax && k <= kmax;
+            const int64_t a = o + i + hx * j + hxy * k;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) r[f][l] = ok ? src[f][a] : T(0.0);
+        }
+    }
+    __device__ __forceinline__ void put(T (*sm)[3][GRAD_PN], const T (&r)[NF][GRAD_LD], int slot, int tid) const {
+#pragma unroll
+        for (int l = 0; l < GRAD_LD; ++l) {
+            const int idx = tid + l * GRAD_TX * GRAD_TY;
+            if (idx < GRAD_PN) {
+#pragma unroll
+                for (int f = 0; f < NF; ++f) sm[f][slot][idx] = r[f][l];
+            }
+        }
+    }
+};
+
+template <class T>
+__global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_normals_tile(const T *__restrict__ phi,
+                                                                    const int8_t *__restrict__ walls,
+                                                                    T *__restrict__ cnx, T *__restrict__ cny,
+                                                                    T *__restrict__ cnz, T *__restrict__ cnorm,
+                                                                    const Layout L) {
+    __shared__ T sm[1][3][GRAD_PN];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + GRAD_TX * ty;
+    const int i0 = -1 + (int)blockIdx.x * GRAD_TX, j0 = -1 + (int)blockIdx.y * GRAD_TY;
+    const int kb = -1 + (int)blockIdx.z * GRAD_KCH;
+    const int ke = min(kb + GRAD_KCH - 1, L.nz + 2);
+    GradPlanes<T, 1> g;
+    g.src[0] = phi;
+    g.hx = L.h4x; g.hxy = L.h4xy; g.o = 3 + 3 * L.h4x + 3 * L.h4xy;
+    g.imax = L.nx + 4; g.jmax = L.ny + 4; g.kmax = L.nz + 4;
+    T r[1][GRAD_LD];
+    g.fetch(r, i0, j0, kb - 1, tid);
+    g.put(sm, r, (kb - 1 + 3) % 3, tid);
+    g.fetch(r, i0, j0, kb, tid);
+    g.put(sm, r, (kb + 3) % 3, tid);
+    g.fetch(r, i0, j0, kb + 1, tid);
+    const int i = i0 + tx, j = j0 + ty;
+    const bool in_ij = i <= L.nx + 2 && j <= L.ny + 2;
+    for (int k = kb; k <= ke; ++k) {
+        g.put(sm, r, (k + 1 + 3) % 3, tid);
+        __syncthreads();
+        if (k + 1 < ke + 1) g.fetch(r, i0, j0, k + 2, tid);
+        if (in_ij) {
+            const int64_t id = L.i2(i, j, k);
+            if (walls[id] != 1) {
+                auto P = [&](int a, int b, int c) { return sm[0][(k + c + 3) % 3][(tx + 1 + a) + GRAD_PW * (ty + 1 + b)]; };
+                T gx, gy, gz, cn;
+                normals_of<T>(P, gx, gy, gz, cn);
+                cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_curvature_tile(const T *__restrict__ cnx, const T *__restrict__ cny,
+                                                                      const T *__restrict__ cnz, T *__restrict__ curv,
+                                                                      const int8_t *__restrict__ walls, const Layout L) {
+    __shared__ T sm[3][3][GRAD_PN];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + GRAD_TX * ty;
+    const int i0 = 1 + (int)blockIdx.x * GRAD_TX, j0 = 1 + (int)blockIdx.y * GRAD_TY;
+    const int kb = 1 + (int)blockIdx.z * GRAD_KCH;
+    const int ke = min(kb + GRAD_KCH - 1, L.nz);
+    GradPlanes<T, 3> g;
+    g.src[0] = cnx; g.src[1] = cny; g.src[2] = cnz;
+    g.hx = L.h2x; g.hxy = L.h2xy; g.o = 1 + L.h2x + L.h2xy;
+    g.imax = L.nx + 2; g.jmax = L.ny + 2; g.kmax = L.nz + 2;
+    T r[3][GRAD_LD];
+    g.fetch(r, i0, j0, kb - 1, tid);
+    g.put(sm, r, (kb - 1) % 3, tid);
+    g.fetch(r, i0, j0, kb, tid);
+    g.put(sm, r, kb % 3, tid);
+    g.fetch(r, i0, j0, kb + 1, tid);
+    const int i = i0 + tx, j = j0 + ty;
+    const bool in_ij = i <= L.nx && j <= L.ny;
+    for (int k = kb; k <= ke; ++k) {
+        g.put(sm, r, (k + 1) % 3, tid);
+        __syncthreads();
+        if (k + 1 < ke + 1) g.fetch(r, i0, j0, k + 2, tid);
+        if (in_ij && walls[L.i2(i, j, k)] == 0) {
+            const int c0 = (tx + 1) + GRAD_PW * (ty + 1);
+            auto X = [&](int a, int b, int c) { return sm[0][(k + c) % 3][c0 + a + GRAD_PW * b]; };
+            auto Y = [&](int a, int b, int c) { return sm[1][(k + c) % 3][c0 + a + GRAD_PW * b]; };
+            auto Z = [&](int a, int b, int c) { return sm[2][(k + c) % 3][c0 + a + GRAD_PW * b]; };
+            curv[L.i1(i, j, k)] = curvature_of<T>(X, Y, Z);
+        }
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -1624,11 +1773,13 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
 // and warps 0-3 compute, one node per thread; two shared-memory stages let the load of the
 // next tile and the store of the last one overlap the arithmetic.  Stage hand-over uses
 // mbarriers: `full` completes with the load's byte count, `empty` when all 128 computing
-// threads have written their results (and fenced them for the async proxy).  The tensor's
-// extent is the nf fluid nodes: columns of the last tile past nf load as zeros and are
-// not stored, so the link slots after nf are untouched.  Every wait is bounded; a wait
-// that runs out sets *err, and the copy thread waits (bounded again) for the loads it
-// issued before the block exits.
+// threads have written their results (and fenced them for the async proxy).  Only whole
+// tiles go through the copies, so no box reaches past the nf fluid nodes into the link
+// slots that follow them (a store clipped at the tensor's extent is clipped at 16-byte
+// granularity, which would reach the first link slot when nf * element size is not a
+// multiple of 16); the last block updates the nf % 128 remaining nodes with plain loads
+// and stores.  Every wait is bounded; a wait that runs out sets *err, and the copy thread
+// waits (bounded again) for the loads it issued before the block exits.
 // ---------------------------------------------------------------------------------
 constexpr int kTmaNodes = 128;            // nodes per tile = computing threads per block
 constexpr int kTmaStages = 2;
@@ -1638,13 +1789,14 @@ template <class S> struct TmaTile { static constexpr int bytes = 19 * kTmaNodes 
 
 template <class S, bool UNIT>
 __global__ void __launch_bounds__(kTmaNodes + 32, 4)
-    k_sp_list_even_tma(const __grid_constant__ CUtensorMap map, const int nf, const StepParams P,
-                       const MrtFold<typename Store<S>::RS> cf, const float scale, int32_t *__restrict__ err) {
+    k_sp_list_even_tma(const __grid_constant__ CUtensorMap map, S *__restrict__ A, const int64_t stride, const int nf,
+                       const StepParams P, const MrtFold<typename Store<S>::RS> cf, const float scale,
+                       int32_t *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t full[kTmaStages], empty[kTmaStages];
     S *tiles = reinterpret_cast<S *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int tid = threadIdx.x;
-    const int ntiles = (nf + kTmaNodes - 1) / kTmaNodes;
+    const int ntiles = nf / kTmaNodes;   // whole tiles only
     const int m = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tid == 0) {
         for (int s = 0; s < kTmaStages; ++s) {
@@ -1707,6 +1859,11 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
         for (int q = 0; q < 19; ++q) st_sweep<S>(buf, (int64_t)q * kTmaNodes + tid, q, ft[q], sc);
         bulk::fence_async_smem();
         bulk::mbar_arrive(&empty[s]);
+    }
+    // the nodes after the last whole tile, by the last block, from global memory
+    if (blockIdx.x == gridDim.x - 1) {
+        const int t = ntiles * kTmaNodes + tid;
+        if (t < nf) sp_list_node<S, false, UNIT>(A, stride, nullptr, nf, t, P, cf, scale);
     }
 }
 

@@ -28,8 +28,9 @@ template <> const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldf
 // (blocks per SM from the occupancy calculator, cached per device), at most one per tile.
 template <class S, bool UNIT>
 int even_tma(const DevState &st, cudaStream_t s) {
-    const int ntiles = (st.nfl + kTmaNodes - 1) / kTmaNodes;
-    if (ntiles == 0) return 0;
+    // whole tiles through the copies; the last block also takes the nfl % 128 nodes after them
+    const int ntiles = st.nfl / kTmaNodes;
+    if (ntiles == 0) return -1;   // fewer than 128 fluid nodes: the plain sweep
     const int smem = kTmaStages * TmaTile<S>::bytes + 1024;
     static int max_grid[64] = {};
     int dev = 0;
@@ -43,7 +44,7 @@ int even_tma(const DevState &st, cudaStream_t s) {
         max_grid[dev] = per * sms;
     }
     const int grid = ntiles < max_grid[dev] ? ntiles : max_grid[dev];
-    k_sp_list_even_tma<S, UNIT><<<grid, kTmaNodes + 32, smem, s>>>(st.tmap, st.nfl, st.P,
+    k_sp_list_even_tma<S, UNIT><<<grid, kTmaNodes + 32, smem, s>>>(st.tmap, fs<S>(st), st.lstride, st.nfl, st.P,
                                                                    fold_of<typename Store<S>::RS>(st), st.scale, st.err);
     return 1;
 }
@@ -243,7 +244,12 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         else k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
     }
 #ifndef MFLBM_STRICT
-    if (st.glist) {
+    if (st.gtile && st.prec != MFLBM_FP64FF) {
+        const dim3 b(GRAD_TX, GRAD_TY);
+        const dim3 g((L.nx + 4 + GRAD_TX - 1) / GRAD_TX, (L.ny + 4 + GRAD_TY - 1) / GRAD_TY,
+                     (L.nz + 4 + GRAD_KCH - 1) / GRAD_KCH);
+        k_normals_tile<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
+    } else if (st.glist) {
         if (st.n_gcell_n > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {
@@ -275,7 +281,11 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
     }
 #ifndef MFLBM_STRICT
-    if (st.glist) {
+    if (st.gtile && st.prec != MFLBM_FP64FF) {
+        const dim3 b(GRAD_TX, GRAD_TY);
+        const dim3 g((L.nx + GRAD_TX - 1) / GRAD_TX, (L.ny + GRAD_TY - 1) / GRAD_TY, (L.nz + GRAD_KCH - 1) / GRAD_KCH);
+        k_curvature_tile<T><<<g, b, 0, s>>>(cnx, cny, cnz, curv, st.walls, L);
+    } else if (st.glist) {
         if (st.n_gcell_c > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {

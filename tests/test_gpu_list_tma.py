@@ -32,6 +32,29 @@ def _run(case, steps, plain):
 
 
 @pytest.mark.parametrize("precision", [0, 1, 2, 3, 4])
+def test_small_odd_node_count(precision):
+    """1,513 fluid nodes: eleven whole tiles plus 105 nodes for the plain tail, and nf * 8
+    bytes not a multiple of 16 (a box clipped at the tensor's extent would reach the first
+    link slot)."""
+    from cases import periodic_ghosts, sp_case
+    case = sp_case(per=(1, 1, 1), spheres=4, force=1e-5, rest="mrt", precision=precision, strict=0)
+    case["f"] = periodic_ghosts(case["f"], (1, 1, 1))
+    out = []
+    for plain in (False, True):
+        if plain:
+            os.environ["MFLBM_NO_TMA"] = "1"
+        try:
+            with Solver(case["params"]) as sim:
+                sim.set_geometry(case["walls"])
+                sim.upload_state(case["f"])
+                sim.run(1, 5)
+                out.append(sim.download_state()["f"])
+        finally:
+            os.environ.pop("MFLBM_NO_TMA", None)
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2, 3, 4])
 def test_tma_even_step_equals_plain_even_step(precision):
     case = workloads.packing_permeability(n=96, porosity=0.22, seed=17, precision=precision, force_z=1e-5)
     nf = case["pore"]
