@@ -58,6 +58,8 @@ struct mflbm_ctx {
 };
 
 static const int kEventRing = 512;
+// fluid fraction above which the colour-gradient stencils run as shared-memory tiles
+static const double kGradientTileFraction = 0.6;
 
 static thread_local std::string g_last_create_error;
 
@@ -205,6 +207,8 @@ int alloc_dense(mflbm_ctx *c) {
     c->st.f = c->pdf;
     c->st.g = c->p.multiphase ? (void *)((char *)c->pdf + plane) : nullptr;
     c->st.list = 0;
+    c->st.tma = 0;
+    c->st.c16 = 0;
     return MFLBM_OK;
 }
 
@@ -537,7 +541,7 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     if (!p.multiphase && p.layout != MFLBM_LAYOUT_DENSE && p.inlet_bc == 0 && p.outlet_bc == 0) {
         ListLayout ll;
         std::string why;
-        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why);
+        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why, true);
         for (void *b : c->list_bufs) dfree(c, b);
         c->list_bufs.clear();
         if (ok) {
@@ -556,7 +560,23 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             CK(c, cudaMemcpy(cell1, ll.cell1.data(), sizeof(int32_t) * ll.cell1.size(), cudaMemcpyHostToDevice));
             if (ll.nlink) CK(c, cudaMemcpy(link, ll.link.data(), sizeof(int32_t) * ll.link.size(), cudaMemcpyHostToDevice));
             CK(c, cudaMemcpy(seg, ll.slice.data(), sizeof(int32_t) * ll.slice.size(), cudaMemcpyHostToDevice));
+            // the compressed neighbour table of the odd step, unless MFLBM_NO_NB16 is set (a
+            // diagnostic switch that selects the 32-bit table, for comparisons)
+            int16_t *nb16 = nullptr;
+            int32_t *lbase = nullptr;
+            const char *no16 = std::getenv("MFLBM_NO_NB16");
+            if (ll.c16 && (!no16 || !*no16 || std::strcmp(no16, "0") == 0)) {
+                if ((r = dalloc(c, &nb16, 18 * ll.nf))) return r;
+                c->list_bufs.push_back(nb16);
+                if ((r = dalloc(c, &lbase, ll.nf))) return r;
+                c->list_bufs.push_back(lbase);
+                CK(c, cudaMemcpy(nb16, ll.nb16.data(), sizeof(int16_t) * ll.nb16.size(), cudaMemcpyHostToDevice));
+                CK(c, cudaMemcpy(lbase, ll.lbase.data(), sizeof(int32_t) * ll.lbase.size(), cudaMemcpyHostToDevice));
+            }
             DevState &st = c->st;
+            st.nb16 = nb16;
+            st.lbase = lbase;
+            st.c16 = nb16 ? 1 : 0;
             st.list = 1;
             st.f = c->pdf;
             st.g = nullptr;
@@ -635,11 +655,21 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     c->st.n_gcell_n = 0;
     c->st.n_gcell_c = 0;
     c->st.sbc = nullptr;
-    // the shared-memory stencils, unless MFLBM_GRADIENT_LISTS is set (a diagnostic switch
-    // that selects the fluid-cell list kernels, for comparisons)
+    // Normals and curvature: the shared-memory plane-marching kernels visit every cell of the
+    // box, the fluid-cell list kernels only the cells that need a value.  The tiles pay when
+    // most cells are fluid; on a porous medium (a third fluid) the lists are faster.  The
+    // choice follows the fluid fraction of the interior; MFLBM_GRADIENT=tile|list (a
+    // diagnostic switch) overrides it.
     {
-        const char *gl = std::getenv("MFLBM_GRADIENT_LISTS");
-        c->st.gtile = (!gl || !*gl || std::strcmp(gl, "0") == 0) ? 1 : 0;
+        int64_t nfluid = 0;
+        for (int k = 1; k <= p.nz; ++k)
+            for (int j = 1; j <= p.ny; ++j)
+                for (int i = 1; i <= p.nx; ++i) nfluid += walls[L.i2(i, j, k)] == 0;
+        const double frac = (double)nfluid / ((double)p.nx * p.ny * p.nz);
+        const char *gsel = std::getenv("MFLBM_GRADIENT");
+        if (gsel && std::strcmp(gsel, "tile") == 0) c->st.gtile = 1;
+        else if (gsel && std::strcmp(gsel, "list") == 0) c->st.gtile = 0;
+        else c->st.gtile = frac > kGradientTileFraction ? 1 : 0;
     }
     if (!cell_packable(p.nx, p.ny, p.nz)) return MFLBM_OK;  // the full-box kernels serve
     std::vector<uint32_t> gn, gc;

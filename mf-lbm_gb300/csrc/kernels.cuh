@@ -1725,17 +1725,30 @@ __device__ __forceinline__ void sp_collide(typename Store<S>::RS (&ft)[19], cons
 }
 
 // one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
-template <class S, bool ODD, bool UNIT>
+// C16 = true: the odd step reads the compressed table (16-bit deltas and link ranks plus a
+// per-node link base, 40 bytes per node instead of 72) instead of nb.
+template <class S, bool ODD, bool UNIT, bool C16 = false>
 __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
                                              const int64_t nf, const int64_t t, const StepParams &P,
-                                             const MrtFold<typename Store<S>::RS> &cf, const float scale) {
+                                             const MrtFold<typename Store<S>::RS> &cf, const float scale,
+                                             const int16_t *__restrict__ nb16 = nullptr,
+                                             const int32_t *__restrict__ lbase = nullptr) {
     using R = typename Store<S>::RS;
     const R inv_scale = R(1.0f / scale);
     R ft[19];
     int32_t nbr[18];
-    if (ODD) {
+    if constexpr (ODD && C16) {
+        const int32_t lb = (int32_t)nf + lbase[t] - (kNb16Link - 17);
+#pragma unroll
+        for (int d = 0; d < 18; ++d) {
+            const int v = nb16[(int64_t)d * nf + t];
+            nbr[d] = v > kNb16Link ? (int32_t)t + v : lb + v;
+        }
+    } else if constexpr (ODD) {
 #pragma unroll
         for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * nf + t];
+    }
+    if (ODD) {
         ft[0] = ld_sweep<S>(A, t, 0, inv_scale);
 #pragma unroll
         for (int q = 1; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)q * stride + nbr[OPP(q) - 1], q, inv_scale);
@@ -1764,6 +1777,17 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
 }
 
+// the odd step over the compressed neighbour table
+template <class S, bool UNIT>
+__global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks)
+    k_sp_list_odd16(S *__restrict__ A, const int64_t stride, const int16_t *__restrict__ nb16,
+                    const int32_t *__restrict__ lbase, const int nf, const StepParams P,
+                    const MrtFold<typename Store<S>::RS> cf, const float scale) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf) return;
+    sp_list_node<S, true, UNIT, true>(A, stride, nullptr, nf, t, P, cf, scale, nb16, lbase);
+}
+
 // ---------------------------------------------------------------------------------
 // The even step of the list sweep through the tensor memory accelerator (TMA).  The even
 // step reads A_opp(q)[x] and writes A_q[x] over a contiguous range of fluid nodes, so one
@@ -1782,24 +1806,30 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
 // waits (bounded again) for the loads it issued before the block exits.
 // ---------------------------------------------------------------------------------
 constexpr int kTmaNodes = 128;            // nodes per tile = computing threads per block
-constexpr int kTmaStages = 2;
 constexpr long long kTmaWait = 1ll << 26; // probes of one wait before it gives up
 
-template <class S> struct TmaTile { static constexpr int bytes = 19 * kTmaNodes * (int)sizeof(S); };
+// bytes of one tile and shared-memory stages per block: two for 8-byte populations (the
+// arithmetic is long, two tiles in flight cover the copies), four for 4- and 2-byte ones
+// (short arithmetic: more tiles in flight keep HBM busy)
+template <class S> struct TmaTile {
+    static constexpr int bytes = 19 * kTmaNodes * (int)sizeof(S);
+    static constexpr int stages = sizeof(S) >= 8 ? 2 : 4;
+};
 
 template <class S, bool UNIT>
 __global__ void __launch_bounds__(kTmaNodes + 32, 4)
     k_sp_list_even_tma(const __grid_constant__ CUtensorMap map, S *__restrict__ A, const int64_t stride, const int nf,
                        const StepParams P, const MrtFold<typename Store<S>::RS> cf, const float scale,
                        int32_t *__restrict__ err) {
+    constexpr int NS = TmaTile<S>::stages;
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t full[kTmaStages], empty[kTmaStages];
+    __shared__ uint64_t full[NS], empty[NS];
     S *tiles = reinterpret_cast<S *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int tid = threadIdx.x;
     const int ntiles = nf / kTmaNodes;   // whole tiles only
     const int m = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tid == 0) {
-        for (int s = 0; s < kTmaStages; ++s) {
+        for (int s = 0; s < NS; ++s) {
             bulk::mbar_init(&full[s], 1);
             bulk::mbar_init(&empty[s], kTmaNodes);
         }
@@ -1808,17 +1838,17 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
     __syncthreads();
     if (tid >= kTmaNodes) {
         if (tid != kTmaNodes) return;
-        // copy thread: tile n goes to stage n % kTmaStages; before reloading a stage, the
+        // copy thread: tile n goes to stage n % NS; before reloading a stage, the
         // results of the tile it held are stored and the store has read them out
-        int last_load[kTmaStages];
-        for (int s = 0; s < kTmaStages; ++s) last_load[s] = -1;
+        int last_load[NS];
+        for (int s = 0; s < NS; ++s) last_load[s] = -1;
         bool ok = true;
-        for (int n = 0; n < m + kTmaStages; ++n) {
-            const int s = n % kTmaStages;
+        for (int n = 0; n < m + NS; ++n) {
+            const int s = n % NS;
             S *buf = tiles + s * 19 * kTmaNodes;
-            if (n >= kTmaStages) {
-                const int np = n - kTmaStages;
-                if (!bulk::mbar_wait(&empty[s], (uint32_t)((np / kTmaStages) & 1), kTmaWait)) {
+            if (n >= NS) {
+                const int np = n - NS;
+                if (!bulk::mbar_wait(&empty[s], (uint32_t)((np / NS) & 1), kTmaWait)) {
                     ok = false;
                     break;
                 }
@@ -1835,9 +1865,9 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
         bulk::bulk_wait0();
         if (!ok) {
             atomicExch(err, 1);
-            for (int s = 0; s < kTmaStages; ++s)
+            for (int s = 0; s < NS; ++s)
                 if (last_load[s] >= 0)
-                    (void)bulk::mbar_wait(&full[s], (uint32_t)((last_load[s] / kTmaStages) & 1), kTmaWait);
+                    (void)bulk::mbar_wait(&full[s], (uint32_t)((last_load[s] / NS) & 1), kTmaWait);
         }
         return;
     }
@@ -1845,9 +1875,9 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
     const R inv_scale = R(1.0f / scale);
     const R sc = R(scale);
     for (int n = 0; n < m; ++n) {
-        const int s = n % kTmaStages;
+        const int s = n % NS;
         S *buf = tiles + s * 19 * kTmaNodes;
-        if (!bulk::mbar_wait(&full[s], (uint32_t)((n / kTmaStages) & 1), kTmaWait)) {
+        if (!bulk::mbar_wait(&full[s], (uint32_t)((n / NS) & 1), kTmaWait)) {
             atomicExch(err, 1);
             break;
         }

@@ -31,7 +31,7 @@ int even_tma(const DevState &st, cudaStream_t s) {
     // whole tiles through the copies; the last block also takes the nfl % 128 nodes after them
     const int ntiles = st.nfl / kTmaNodes;
     if (ntiles == 0) return -1;   // fewer than 128 fluid nodes: the plain sweep
-    const int smem = kTmaStages * TmaTile<S>::bytes + 1024;
+    const int smem = TmaTile<S>::stages * TmaTile<S>::bytes + 1024;
     static int max_grid[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
@@ -51,12 +51,24 @@ int even_tma(const DevState &st, cudaStream_t s) {
 
 template <class S>
 int collide_list(const DevState &st, bool odd, cudaStream_t s) {
-    if (!odd && st.tma) {
+    // the TMA even step for every form but FP64 storage with the double-word collision,
+    // whose conversions make it issue-bound: it runs faster with the plain sweep's
+    // occupancy (measured on the 256^3 packing)
+    if (!odd && st.tma && !std::is_same<S, f64ff>::value) {
         const int r = st.unit ? even_tma<S, true>(st, s) : even_tma<S, false>(st, s);
         if (r >= 0) return r;
     }
     const unsigned nb = (unsigned)((st.nfl + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::RS>(st);
+    if (odd && st.c16) {
+        if (st.unit)
+            k_sp_list_odd16<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb16, st.lbase, st.nfl, st.P, cf,
+                                                        st.scale);
+        else
+            k_sp_list_odd16<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb16, st.lbase, st.nfl, st.P, cf,
+                                                         st.scale);
+        return 1;
+    }
     if (st.unit) {
         if (odd) k_sp_list<S, true, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
         else k_sp_list<S, false, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.nfl, st.P, cf, st.scale);
