@@ -4,8 +4,9 @@ The translation units are compiled in parallel and linked into
 mf-lbm_gb300/mflbm/lib/libmflbm.so:
 
   csrc/api.cu             C ABI, context, step ordering, CUDA graphs
-  csrc/kernels_fast.cu    kernels with nvcc's default FMA contraction
-  csrc/kernels_strict.cu  the same kernels with --fmad=false (bit-identical to an IEEE
+  csrc/kernels_fast*.cu   kernels with nvcc's default FMA contraction, in three units
+                          (collision sweeps; ensembles; the rest and the launch table)
+  csrc/kernels_strict*.cu the same kernels with --fmad=false (bit-identical to an IEEE
                           restatement that keeps the reference's operation order)
   csrc/noalloc.cu         mflbm_saturation_noalloc (fixed device scratch, no allocation)
   csrc/listlayout.cpp     host construction of the fluid-list layout
@@ -35,7 +36,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = os.environ.get("MFLBM_NVCC_FLAGS", "").split()
 UNITS = {
     "api.o": ("api.cu", []),
+    "kernels_fast_sweep.o": ("kernels_fast_sweep.cu", []),
+    "kernels_fast_ens.o": ("kernels_fast_ens.cu", []),
     "kernels_fast.o": ("kernels_fast.cu", []),
+    "kernels_strict_sweep.o": ("kernels_strict_sweep.cu", ["--fmad=false"]),
+    "kernels_strict_ens.o": ("kernels_strict_ens.cu", ["--fmad=false"]),
     "kernels_strict.o": ("kernels_strict.cu", ["--fmad=false"]),
     "noalloc.o": ("noalloc.cu", []),
     "listlayout.o": ("listlayout.cpp", []),

@@ -208,7 +208,7 @@ int alloc_dense(mflbm_ctx *c) {
     c->st.g = c->p.multiphase ? (void *)((char *)c->pdf + plane) : nullptr;
     c->st.list = 0;
     c->st.tma = 0;
-    c->st.c16 = 0;
+    c->st.wt = 0;
     return MFLBM_OK;
 }
 
@@ -541,7 +541,7 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     if (!p.multiphase && p.layout != MFLBM_LAYOUT_DENSE && p.inlet_bc == 0 && p.outlet_bc == 0) {
         ListLayout ll;
         std::string why;
-        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why, true);
+        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why);
         for (void *b : c->list_bufs) dfree(c, b);
         c->list_bufs.clear();
         if (ok) {
@@ -560,23 +560,29 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             CK(c, cudaMemcpy(cell1, ll.cell1.data(), sizeof(int32_t) * ll.cell1.size(), cudaMemcpyHostToDevice));
             if (ll.nlink) CK(c, cudaMemcpy(link, ll.link.data(), sizeof(int32_t) * ll.link.size(), cudaMemcpyHostToDevice));
             CK(c, cudaMemcpy(seg, ll.slice.data(), sizeof(int32_t) * ll.slice.size(), cudaMemcpyHostToDevice));
-            // the compressed neighbour table of the odd step, unless MFLBM_NO_NB16 is set (a
-            // diagnostic switch that selects the 32-bit table, for comparisons)
-            int16_t *nb16 = nullptr;
-            int32_t *lbase = nullptr;
-            const char *no16 = std::getenv("MFLBM_NO_NB16");
-            if (ll.c16 && (!no16 || !*no16 || std::strcmp(no16, "0") == 0)) {
-                if ((r = dalloc(c, &nb16, 18 * ll.nf))) return r;
-                c->list_bufs.push_back(nb16);
-                if ((r = dalloc(c, &lbase, ll.nf))) return r;
-                c->list_bufs.push_back(lbase);
-                CK(c, cudaMemcpy(nb16, ll.nb16.data(), sizeof(int16_t) * ll.nb16.size(), cudaMemcpyHostToDevice));
-                CK(c, cudaMemcpy(lbase, ll.lbase.data(), sizeof(int32_t) * ll.lbase.size(), cudaMemcpyHostToDevice));
+            // the warp-compressed neighbour table of the odd step, unless MFLBM_NO_WARP_TABLE is
+            // set (a diagnostic switch that selects the 32-bit table, for comparisons)
+            uint8_t *off8 = nullptr;
+            int32_t *whdr = nullptr, *wside = nullptr;
+            const char *nowt = std::getenv("MFLBM_NO_WARP_TABLE");
+            if (!nowt || !*nowt || std::strcmp(nowt, "0") == 0) {
+                build_warp_table(ll);
+                if ((r = dalloc(c, &off8, (int64_t)ll.off8.size()))) return r;
+                c->list_bufs.push_back(off8);
+                if ((r = dalloc(c, &whdr, (int64_t)ll.hdr.size()))) return r;
+                c->list_bufs.push_back(whdr);
+                if ((r = dalloc(c, &wside, std::max<int64_t>(32, (int64_t)ll.side.size())))) return r;
+                c->list_bufs.push_back(wside);
+                CK(c, cudaMemcpy(off8, ll.off8.data(), ll.off8.size(), cudaMemcpyHostToDevice));
+                CK(c, cudaMemcpy(whdr, ll.hdr.data(), sizeof(int32_t) * ll.hdr.size(), cudaMemcpyHostToDevice));
+                if (!ll.side.empty())
+                    CK(c, cudaMemcpy(wside, ll.side.data(), sizeof(int32_t) * ll.side.size(), cudaMemcpyHostToDevice));
             }
             DevState &st = c->st;
-            st.nb16 = nb16;
-            st.lbase = lbase;
-            st.c16 = nb16 ? 1 : 0;
+            st.off8 = off8;
+            st.whdr = reinterpret_cast<const int2 *>(whdr);
+            st.wside = wside;
+            st.wt = off8 ? 1 : 0;
             st.list = 1;
             st.f = c->pdf;
             st.g = nullptr;

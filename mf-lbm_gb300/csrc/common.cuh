@@ -31,11 +31,6 @@ __host__ __device__ constexpr int OPP(int q) {
 static_assert(OPP(9) == 8 && OPP(17) == 16 && OPP(0) == 0, "opposite table");
 static_assert(EX(OPP(13)) == -EX(13) && EZ(OPP(13)) == -EZ(13), "opposite table");
 
-// Compressed neighbour table of the fluid-list layout: an int16 entry above kNb16Link is
-// the delta to a fluid neighbour's index; kNb16Link - 17 + r names the node's r-th link
-// slot (nf + lbase[x] + r).
-constexpr int kNb16Link = -32750;
-
 // Device layout of the PDF arrays.
 // Each direction q is one SoA plane over the halo-1 box i,j,k in [0, n+1].  Rows are
 // padded so that interior node i=1 starts on a 32-byte boundary for every storage type:

@@ -40,10 +40,10 @@ __host__ __device__ constexpr double WREST(int q) { return q == 0 ? 4.0 / 21.0 :
 
 // direction tables for run-time q (boundary-node lists): offsets and weight class
 // (0 rest, 1 axis, 2 diagonal); indexed 0..18
-__constant__ signed char c_ex[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
-__constant__ signed char c_ey[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
-__constant__ signed char c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
-__constant__ signed char c_opp[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+static __constant__ signed char c_ex[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+static __constant__ signed char c_ey[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+static __constant__ signed char c_ez[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+static __constant__ signed char c_opp[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
 __device__ __forceinline__ int OPP_RT(int q) { return c_opp[q]; }
 
 // neighbour offset of direction q in the padded PDF layout
@@ -579,8 +579,8 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, d
 // copies the one PDF per edge, and must run after the faces (it overrides four slots
 // that two face copies also write in the push direction, Mpi.F90:417-431).
 // ---------------------------------------------------------------------------------
-__device__ __constant__ int c_plus[3][5] = {{1, 7, 9, 11, 13}, {3, 7, 8, 15, 17}, {5, 11, 12, 15, 16}};
-__device__ __constant__ int c_minus[3][5] = {{2, 8, 10, 12, 14}, {4, 10, 9, 16, 18}, {6, 14, 13, 18, 17}};
+static __device__ __constant__ int c_plus[3][5] = {{1, 7, 9, 11, 13}, {3, 7, 8, 15, 17}, {5, 11, 12, 15, 16}};
+static __device__ __constant__ int c_minus[3][5] = {{2, 8, 10, 12, 14}, {4, 10, 9, 16, 18}, {6, 14, 13, 18, 17}};
 
 // one thread per (face cell, species); dim 0=x, 1=y, 2=z
 template <class S>
@@ -1724,45 +1724,42 @@ __device__ __forceinline__ void sp_collide(typename Store<S>::RS (&ft)[19], cons
     }
 }
 
-// one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
-// C16 = true: the odd step reads the compressed table (16-bit deltas and link ranks plus a
-// per-node link base, 40 bytes per node instead of 72) instead of nb.
-template <class S, bool ODD, bool UNIT, bool C16 = false>
-__device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
-                                             const int64_t nf, const int64_t t, const StepParams &P,
-                                             const MrtFold<typename Store<S>::RS> &cf, const float scale,
-                                             const int16_t *__restrict__ nb16 = nullptr,
-                                             const int32_t *__restrict__ lbase = nullptr) {
+// the odd step of one fluid node whose 18 neighbour slots are known
+template <class S, bool UNIT>
+__device__ __forceinline__ void sp_list_odd_node(S *__restrict__ A, const int64_t stride, const int64_t t,
+                                                 const int32_t (&nbr)[18], const StepParams &P,
+                                                 const MrtFold<typename Store<S>::RS> &cf, const float scale) {
     using R = typename Store<S>::RS;
     const R inv_scale = R(1.0f / scale);
     R ft[19];
-    int32_t nbr[18];
-    if constexpr (ODD && C16) {
-        const int32_t lb = (int32_t)nf + lbase[t] - (kNb16Link - 17);
+    ft[0] = ld_sweep<S>(A, t, 0, inv_scale);
 #pragma unroll
-        for (int d = 0; d < 18; ++d) {
-            const int v = nb16[(int64_t)d * nf + t];
-            nbr[d] = v > kNb16Link ? (int32_t)t + v : lb + v;
-        }
-    } else if constexpr (ODD) {
-#pragma unroll
-        for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * nf + t];
-    }
-    if (ODD) {
-        ft[0] = ld_sweep<S>(A, t, 0, inv_scale);
-#pragma unroll
-        for (int q = 1; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)q * stride + nbr[OPP(q) - 1], q, inv_scale);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
-    }
+    for (int q = 1; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)q * stride + nbr[OPP(q) - 1], q, inv_scale);
     sp_collide<S, UNIT>(ft, P, cf);
     const R sc = R(scale);
-    if (ODD) {
-        st_sweep<S>(A, t, 0, ft[0], sc);
+    st_sweep<S>(A, t, 0, ft[0], sc);
 #pragma unroll
-        for (int q = 1; q < 19; ++q) st_sweep<S>(A, (int64_t)OPP(q) * stride + nbr[q - 1], q, ft[q], sc);
+    for (int q = 1; q < 19; ++q) st_sweep<S>(A, (int64_t)OPP(q) * stride + nbr[q - 1], q, ft[q], sc);
+}
+
+// one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
+template <class S, bool ODD, bool UNIT>
+__device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
+                                             const int64_t nf, const int64_t t, const StepParams &P,
+                                             const MrtFold<typename Store<S>::RS> &cf, const float scale) {
+    if constexpr (ODD) {
+        int32_t nbr[18];
+#pragma unroll
+        for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * nf + t];
+        sp_list_odd_node<S, UNIT>(A, stride, t, nbr, P, cf, scale);
     } else {
+        using R = typename Store<S>::RS;
+        const R inv_scale = R(1.0f / scale);
+        R ft[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
+        sp_collide<S, UNIT>(ft, P, cf);
+        const R sc = R(scale);
 #pragma unroll
         for (int q = 0; q < 19; ++q) st_sweep<S>(A, (int64_t)q * stride + t, q, ft[q], sc);
     }
@@ -1777,15 +1774,35 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
 }
 
-// the odd step over the compressed neighbour table
+
+// The odd step over the warp-compressed neighbour table (listlayout.h): per warp and
+// direction an 8-byte header (fluid base, link base), per node and direction one byte.
+// A fluid neighbour is x + base + byte; the warp's link slots of one direction array are
+// consecutive, so a link's slot is the link base plus the number of lower lanes with a
+// link (a ballot and a population count); a "wide" warp-direction reads 32-bit entries from
+// the side table.  22.5 bytes of table per node instead of the 72 of the 32-bit table.
 template <class S, bool UNIT>
 __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks)
-    k_sp_list_odd16(S *__restrict__ A, const int64_t stride, const int16_t *__restrict__ nb16,
-                    const int32_t *__restrict__ lbase, const int nf, const StepParams P,
-                    const MrtFold<typename Store<S>::RS> cf, const float scale) {
+    k_sp_list_odd8(S *__restrict__ A, const int64_t stride, const uint8_t *__restrict__ off8,
+                   const int2 *__restrict__ hdr, const int32_t *__restrict__ side, const int nf, const StepParams P,
+                   const MrtFold<typename Store<S>::RS> cf, const float scale) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nf) return;
-    sp_list_node<S, true, UNIT, true>(A, stride, nullptr, nf, t, P, cf, scale, nb16, lbase);
+    if ((t & ~31) >= nf) return;   // the whole warp lies past the last node
+    const bool valid = t < nf;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t w = t >> 5;
+    int32_t nbr[18];
+#pragma unroll
+    for (int d = 0; d < 18; ++d) {
+        const int2 h = hdr[18 * w + d];
+        const int c = valid ? (int)off8[(int64_t)d * nf + t] : 0;
+        const unsigned lm = __ballot_sync(0xffffffffu, valid && c == 255);
+        if (h.y < 0) nbr[d] = valid ? side[h.x + lane] : 0;
+        else nbr[d] = c == 255 ? h.y + __popc(lm & below) : t + h.x + c;
+    }
+    if (!valid) return;
+    sp_list_odd_node<S, UNIT>(A, stride, t, nbr, P, cf, scale);
 }
 
 // ---------------------------------------------------------------------------------
@@ -2001,7 +2018,7 @@ __global__ void k_list_in(S *__restrict__ A, const int64_t stride, const int q, 
 // equilibrium w_q (the value the reference's untouched slots keep after
 // initialisation), then the fluid nodes and link slots are scattered, then the ghost
 // layers of periodic directions receive their periodic images.
-__global__ void k_list_plane_fill(double *__restrict__ stage, int64_t n, double v) {
+static __global__ void k_list_plane_fill(double *__restrict__ stage, int64_t n, double v) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) stage[t] = v;
 }
@@ -2023,7 +2040,7 @@ __global__ void k_list_out(const S *__restrict__ A, const int64_t stride, const 
     }
 }
 
-__global__ void k_list_ghosts(double *__restrict__ stage, const Layout L, int px, int py, int pz) {
+static __global__ void k_list_ghosts(double *__restrict__ stage, const Layout L, int px, int py, int pz) {
     const int64_t n = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;

@@ -11,19 +11,34 @@ inline dim3 row_block(int nx) {
     return dim3(bx, 128 / bx, 1);
 }
 
-template <class S> S *fs(const DevState &st) { return reinterpret_cast<S *>(st.f); }
-template <class S> S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g); }
+template <class S> inline S *fs(const DevState &st) { return reinterpret_cast<S *>(st.f); }
+template <class S> inline S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g); }
 // field arrays (phi, gradient) of the compute type T
-template <class T> T *fld(void *p) { return reinterpret_cast<T *>(p); }
+template <class T> inline T *fld(void *p) { return reinterpret_cast<T *>(p); }
 
 // storage type of the multiphase forms: FP64, or FP32 for the mixed form
 inline bool mp_fp32(const DevState &st) { return st.multiphase && st.prec == MFLBM_FP32; }
 
 template <class R> const MrtFold<R> &fold_of(const DevState &st);
-template <> const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
-template <> const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
-template <> const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldff; }
+template <> inline const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
+template <> inline const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
+template <> inline const MrtFold<ff> &fold_of<ff>(const DevState &st) { return st.foldff; }
 
+// The launchers are split over three translation units per flavour so that they compile
+// in parallel: MFLBM_PART 1 the collision sweeps, 2 the ensembles and the velocity
+// initialisation, 3 the rest and the launch table (which names the other two parts' entries).
+#ifndef MFLBM_PART
+#define MFLBM_PART 3
+#endif
+int collide(const DevState &st, bool odd, cudaStream_t s);
+int ens_run(const EnsArgs &a, int prec, int persistent, int grid, int block, cudaStream_t s);
+int ens_monitor(const EnsArgs &a, int prec, const int32_t *seg0, const int32_t *seg1, int nseg, double *out,
+                cudaStream_t s);
+int ens_init(const EnsArgs &a, int prec, cudaStream_t s);
+int ens_max_grid(int prec, int block);
+int init_velocity(const DevState &st, const double *rho, int rest_base, cudaStream_t s);
+
+#if MFLBM_PART == 1
 // The TMA even step: a persistent grid of as many blocks as fit on the device at once
 // (blocks per SM from the occupancy calculator, cached per device), at most one per tile.
 template <class S, bool UNIT>
@@ -60,13 +75,13 @@ int collide_list(const DevState &st, bool odd, cudaStream_t s) {
     }
     const unsigned nb = (unsigned)((st.nfl + 127) / 128);
     const auto &cf = fold_of<typename Store<S>::RS>(st);
-    if (odd && st.c16) {
+    if (odd && st.wt) {
         if (st.unit)
-            k_sp_list_odd16<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb16, st.lbase, st.nfl, st.P, cf,
-                                                        st.scale);
+            k_sp_list_odd8<S, true><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.off8, st.whdr, st.wside, st.nfl, st.P,
+                                                       cf, st.scale);
         else
-            k_sp_list_odd16<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.nb16, st.lbase, st.nfl, st.P, cf,
-                                                         st.scale);
+            k_sp_list_odd8<S, false><<<nb, 128, 0, s>>>(fs<S>(st), st.lstride, st.off8, st.whdr, st.wside, st.nfl, st.P,
+                                                        cf, st.scale);
         return 1;
     }
     if (st.unit) {
@@ -140,6 +155,9 @@ int collide(const DevState &st, bool odd, cudaStream_t s) {
     }
 }
 
+#endif  // MFLBM_PART == 1
+
+#if MFLBM_PART == 3
 template <class S>
 int wrap_t(const DevState &st, bool pull, cudaStream_t s) {
     int n_launch = 0;
@@ -468,6 +486,9 @@ int field_out(const DevState &st, const void *src, int64_t n, cudaStream_t s) {
     return 1;
 }
 
+#endif  // MFLBM_PART == 3
+
+#if MFLBM_PART == 2
 // ---- ensembles --------------------------------------------------------------------
 template <class S>
 int ens_run_t(const EnsArgs &a, int persistent, int grid, int block, cudaStream_t s) {
@@ -571,6 +592,9 @@ int init_velocity(const DevState &st, const double *rho, int rest_base, cudaStre
     }
 }
 
+#endif  // MFLBM_PART == 2
+
+#if MFLBM_PART == 3
 int steady(const DevState &st, void *phi_old, double *out, int obs_z, int copy_old, cudaStream_t s) {
     if (mp_fp32(st))
         k_steady<float><<<st.L.nz, MON_THREADS, 0, s>>>(fld<float>(st.phi), fld<float>(phi_old), st.rho, st.u, st.v,
@@ -595,6 +619,8 @@ const KernelTable table = {collide,          wrap,        boundary,   color_grad
                            init_equilibrium, convert_in,  convert_out, field_in,      field_out,
                            ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity,
                            steady,           change_inlet_phase};
+
+#endif  // MFLBM_PART == 3
 
 }  // namespace MFLBM_NS
 }  // namespace mflbm

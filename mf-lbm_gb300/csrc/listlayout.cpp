@@ -9,7 +9,7 @@
 namespace mflbm {
 
 bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper, int jper, int kper, ListLayout &out,
-                       std::string &why, bool node_links) {
+                       std::string &why) {
     const int64_t h2x = nx + 4, h2xy = (int64_t)(nx + 4) * (ny + 4);
     const int64_t h1x = nx + 2, h1xy = (int64_t)(nx + 2) * (ny + 2);
     auto wall = [&](int i, int j, int k) { return walls_h2[(i + 1) + h2x * (j + 1) + h2xy * (k + 1)]; };
@@ -39,30 +39,15 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
     const int per[3] = {iper, jper, kper};
     const int n[3] = {nx, ny, nz};
     std::array<int64_t, 19> links{};
-    // pass 0: count link slots per storage direction (and per node), check the ghost rule;
-    // pass 1: fill the tables
+    // pass 1: count link slots per storage direction, check the ghost rule
     out.nb.assign((size_t)18 * nf, 0);
-    std::vector<int32_t> nlk;   // links per node (node_links)
-    if (node_links) {
-        nlk.assign((size_t)nf, 0);
-        out.lbase.assign((size_t)nf, 0);
-    }
     for (int pass = 0; pass < 2; ++pass) {
         std::array<int64_t, 19> cnt{};
         int64_t x = 0;
-        if (pass == 1 && node_links) {
-            int64_t acc = 0;
-            for (int64_t t = 0; t < nf; ++t) {
-                if (acc > INT32_MAX - 18) { why = "too many link slots for 32-bit link bases"; return false; }
-                out.lbase[(size_t)t] = (int32_t)acc;
-                acc += nlk[(size_t)t];
-            }
-        }
         for (int k = 1; k <= nz; ++k)
             for (int j = 1; j <= ny; ++j)
                 for (int i = 1; i <= nx; ++i) {
                     if (wall(i, j, k) != 0) continue;
-                    int rank = 0;   // links of this node so far (node_links)
                     for (int d = 1; d <= 18; ++d) {
                         int c[3] = {i + EX(d), j + EY(d), k + EZ(d)};
                         for (int a = 0; a < 3; ++a) {
@@ -79,14 +64,7 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
                             slot = y;
                         } else {
                             const int qa = OPP(d);   // the solid node's slot opp(d) lives in array opp(d)
-                            ++cnt[qa];
-                            if (node_links) {
-                                slot = nf + (pass == 1 ? out.lbase[(size_t)x] : 0) + rank;
-                                if (pass == 0) ++nlk[(size_t)x];
-                            } else {
-                                slot = nf + cnt[qa] - 1;
-                            }
-                            ++rank;
+                            slot = nf + cnt[qa]++;
                             if (pass == 1) {
                                 out.link.push_back(qa);
                                 out.link.push_back((int32_t)slot);
@@ -102,29 +80,51 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
     int64_t maxl = 0, tot = 0;
     for (int q = 1; q <= 18; ++q) { maxl = std::max(maxl, links[q]); tot += links[q]; }
     out.nlink = tot;
-    out.stride = (nf + (node_links ? tot : maxl) + 31) / 32 * 32;
+    out.stride = (nf + maxl + 31) / 32 * 32;
     if (out.stride >= ((int64_t)1 << 31)) { why = "direction array exceeds 2^31 elements"; return false; }
-    if (node_links) {
-        // the compressed table, when every fluid neighbour is within the int16 range
-        out.c16 = true;
-        out.nb16.assign((size_t)18 * nf, 0);
-        for (int64_t x = 0; x < nf && out.c16; ++x) {
-            int rank = 0;
-            for (int d = 1; d <= 18; ++d) {
-                const int64_t v = out.nb[(size_t)(d - 1) * nf + x];
-                int64_t e;
-                if (v < nf) {
-                    e = v - x;
-                    if (e <= kNb16Link || e > 32767) { out.c16 = false; break; }
+    return true;
+}
+
+void build_warp_table(ListLayout &ll) {
+    const int64_t nf = ll.nf;
+    const int64_t nw = (nf + 31) / 32;
+    ll.off8.assign((size_t)18 * nf, 0);
+    ll.hdr.assign((size_t)nw * 18 * 2, 0);
+    ll.side.clear();
+    for (int64_t w = 0; w < nw; ++w) {
+        const int64_t x0 = 32 * w, x1 = std::min<int64_t>(x0 + 32, nf);
+        for (int d = 0; d < 18; ++d) {
+            const int32_t *row = ll.nb.data() + (size_t)d * nf;
+            int64_t fb = INT64_MAX, fmax = INT64_MIN, lb = -1;
+            for (int64_t x = x0; x < x1; ++x) {
+                const int64_t e = row[x];
+                if (e >= nf) {
+                    if (lb < 0) lb = e;
                 } else {
-                    e = kNb16Link - 17 + rank++;
+                    fb = std::min(fb, e - x);
+                    fmax = std::max(fmax, e - x);
                 }
-                out.nb16[(size_t)(d - 1) * nf + x] = (int16_t)e;
+            }
+            // the link slots of the warp in this direction array must be consecutive
+            bool ok = true;
+            int64_t next = lb;
+            for (int64_t x = x0; x < x1 && ok; ++x)
+                if (row[x] >= nf) ok = row[x] == next++;
+            if (fb == INT64_MAX) fb = 0, fmax = 0;
+            if (ok && fmax - fb <= 254 && fb >= INT32_MIN && fb <= INT32_MAX) {
+                for (int64_t x = x0; x < x1; ++x) {
+                    const int64_t e = row[x];
+                    ll.off8[(size_t)d * nf + x] = e >= nf ? (uint8_t)255 : (uint8_t)(e - x - fb);
+                }
+                ll.hdr[(size_t)2 * (18 * w + d)] = (int32_t)fb;
+                ll.hdr[(size_t)2 * (18 * w + d) + 1] = (int32_t)(lb < 0 ? 0 : lb);
+            } else {
+                ll.hdr[(size_t)2 * (18 * w + d)] = (int32_t)ll.side.size();
+                ll.hdr[(size_t)2 * (18 * w + d) + 1] = -1;
+                for (int64_t x = x0; x < x0 + 32; ++x) ll.side.push_back(x < x1 ? row[x] : 0);
             }
         }
-        if (!out.c16) out.nb16.clear();
     }
-    return true;
 }
 
 }  // namespace mflbm

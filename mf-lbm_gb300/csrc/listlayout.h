@@ -20,36 +20,36 @@
 #include <string>
 #include <vector>
 
-#include "common.cuh"
-
 namespace mflbm {
 
 struct ListLayout {
     int64_t nf = 0;                 // fluid nodes
-    int64_t stride = 0;             // elements per direction array (padded to 32)
+    int64_t stride = 0;             // elements per direction array (nf + max links, padded)
     int64_t nlink = 0;              // bounce-back link slots over all directions
     std::vector<int32_t> nb;        // [18][nf], direction d = 1..18 at row d-1
     std::vector<int32_t> cell1;     // halo-1 Fortran index of every fluid node
     std::vector<int32_t> link;      // [nlink][3]: direction array q, slot index, halo-1 index of the solid cell
     std::vector<int32_t> slice;     // [nz+1]: first fluid index of every z slice
-    // Compressed neighbour table (node_links layout only): nb16[d][x] = nb[d][x] - x for a
-    // fluid neighbour (kNb16Link < value), kNb16Link - 17 + r for the node's r-th link
-    // (r = 0..17 in direction order), whose slot is nf + lbase[x] + r.  Valid (c16) when
-    // every fluid neighbour lies within the int16 range of its node.
-    bool c16 = false;
-    std::vector<int16_t> nb16;      // [18][nf]
-    std::vector<int32_t> lbase;     // [nf] links of the nodes before x
+    // Warp-compressed neighbour table read by the odd step (22.5 bytes per node instead of
+    // 72).  The nodes of warp w are x = 32w .. 32w+31; for each direction d (row d-1):
+    //   hdr[2*(18w + d-1)] = fb, hdr[+1] = lb;  off8[d-1][x] = 8-bit code of nb[d][x]:
+    //   code < 255: fluid neighbour nb = x + fb + code;
+    //   code = 255: link slot nb = lb + (number of lanes below x in the warp with code 255),
+    //               the warp's link slots of one direction array being consecutive;
+    //   lb < 0 (a "wide" warp-direction, where the fluid offsets span more than 254):
+    //               nb = side[fb + lane] for every lane.
+    std::vector<uint8_t> off8;      // [18][nf]
+    std::vector<int32_t> hdr;       // [nwarp][18][2]
+    std::vector<int32_t> side;      // 32 entries per wide warp-direction
 };
+
+// Builds the warp-compressed table of `ll` from its nb table.
+void build_warp_table(ListLayout &ll);
 
 // Builds the layout for one sample from the halo-2 wall array (Fortran order, int8,
 // 1 = solid).  Returns false with a reason when a fluid node has a neighbour in the
 // ghost layer of a non-periodic direction (open boundaries need the dense layout).
-// node_links = false: the link slots of direction array q are numbered nf, nf+1, ... in
-// node order (the arrays hold nf + the largest per-direction count).  node_links = true:
-// the links of node x take the slots nf + lbase[x] + r in the array each one lives in (every
-// array then spans nf + nlink slots, most of the link range unused in any one array), so a
-// link slot is found from the node's base and its rank, and the compressed table is built.
 bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper, int jper, int kper, ListLayout &out,
-                       std::string &why, bool node_links = false);
+                       std::string &why);
 
 }  // namespace mflbm
