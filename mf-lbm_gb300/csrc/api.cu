@@ -208,7 +208,6 @@ int alloc_dense(mflbm_ctx *c) {
     c->st.g = c->p.multiphase ? (void *)((char *)c->pdf + plane) : nullptr;
     c->st.list = 0;
     c->st.tma = 0;
-    c->st.wt = 0;
     return MFLBM_OK;
 }
 
@@ -560,29 +559,7 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             CK(c, cudaMemcpy(cell1, ll.cell1.data(), sizeof(int32_t) * ll.cell1.size(), cudaMemcpyHostToDevice));
             if (ll.nlink) CK(c, cudaMemcpy(link, ll.link.data(), sizeof(int32_t) * ll.link.size(), cudaMemcpyHostToDevice));
             CK(c, cudaMemcpy(seg, ll.slice.data(), sizeof(int32_t) * ll.slice.size(), cudaMemcpyHostToDevice));
-            // the warp-compressed neighbour table of the odd step, unless MFLBM_NO_WARP_TABLE is
-            // set (a diagnostic switch that selects the 32-bit table, for comparisons)
-            uint8_t *off8 = nullptr;
-            int32_t *whdr = nullptr, *wside = nullptr;
-            const char *nowt = std::getenv("MFLBM_NO_WARP_TABLE");
-            if (!nowt || !*nowt || std::strcmp(nowt, "0") == 0) {
-                build_warp_table(ll);
-                if ((r = dalloc(c, &off8, (int64_t)ll.off8.size()))) return r;
-                c->list_bufs.push_back(off8);
-                if ((r = dalloc(c, &whdr, (int64_t)ll.hdr.size()))) return r;
-                c->list_bufs.push_back(whdr);
-                if ((r = dalloc(c, &wside, std::max<int64_t>(32, (int64_t)ll.side.size())))) return r;
-                c->list_bufs.push_back(wside);
-                CK(c, cudaMemcpy(off8, ll.off8.data(), ll.off8.size(), cudaMemcpyHostToDevice));
-                CK(c, cudaMemcpy(whdr, ll.hdr.data(), sizeof(int32_t) * ll.hdr.size(), cudaMemcpyHostToDevice));
-                if (!ll.side.empty())
-                    CK(c, cudaMemcpy(wside, ll.side.data(), sizeof(int32_t) * ll.side.size(), cudaMemcpyHostToDevice));
-            }
             DevState &st = c->st;
-            st.off8 = off8;
-            st.whdr = reinterpret_cast<const int2 *>(whdr);
-            st.wside = wside;
-            st.wt = off8 ? 1 : 0;
             st.list = 1;
             st.f = c->pdf;
             st.g = nullptr;

@@ -1750,7 +1750,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
     if constexpr (ODD) {
         int32_t nbr[18];
 #pragma unroll
-        for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * nf + t];
+        for (int d = 0; d < 18; ++d) nbr[d] = __ldcs(nb + (int64_t)d * nf + t);   // streamed: read once per step
         sp_list_odd_node<S, UNIT>(A, stride, t, nbr, P, cf, scale);
     } else {
         using R = typename Store<S>::RS;
@@ -1774,36 +1774,6 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
 }
 
-
-// The odd step over the warp-compressed neighbour table (listlayout.h): per warp and
-// direction an 8-byte header (fluid base, link base), per node and direction one byte.
-// A fluid neighbour is x + base + byte; the warp's link slots of one direction array are
-// consecutive, so a link's slot is the link base plus the number of lower lanes with a
-// link (a ballot and a population count); a "wide" warp-direction reads 32-bit entries from
-// the side table.  22.5 bytes of table per node instead of the 72 of the 32-bit table.
-template <class S, bool UNIT>
-__global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks)
-    k_sp_list_odd8(S *__restrict__ A, const int64_t stride, const uint8_t *__restrict__ off8,
-                   const int2 *__restrict__ hdr, const int32_t *__restrict__ side, const int nf, const StepParams P,
-                   const MrtFold<typename Store<S>::RS> cf, const float scale) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if ((t & ~31) >= nf) return;   // the whole warp lies past the last node
-    const bool valid = t < nf;
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    const int64_t w = t >> 5;
-    int32_t nbr[18];
-#pragma unroll
-    for (int d = 0; d < 18; ++d) {
-        const int2 h = hdr[18 * w + d];
-        const int c = valid ? (int)off8[(int64_t)d * nf + t] : 0;
-        const unsigned lm = __ballot_sync(0xffffffffu, valid && c == 255);
-        if (h.y < 0) nbr[d] = valid ? side[h.x + lane] : 0;
-        else nbr[d] = c == 255 ? h.y + __popc(lm & below) : t + h.x + c;
-    }
-    if (!valid) return;
-    sp_list_odd_node<S, UNIT>(A, stride, t, nbr, P, cf, scale);
-}
 
 // ---------------------------------------------------------------------------------
 // The even step of the list sweep through the tensor memory accelerator (TMA).  The even

@@ -55,11 +55,6 @@ struct DevState {
     int64_t nlink;
     int nfl;
     const int32_t *lseg;   // [nz+1] first fluid index of every z slice
-    // warp-compressed neighbour table of the odd step (listlayout.h); wt = 1 when present
-    const uint8_t *off8;   // [18][nfl]
-    const int2 *whdr;      // [nwarp][18]
-    const int32_t *wside;
-    int wt;
     // tensor map of the list arrays for the TMA even step: a 2-D tensor of 19 rows (one per
     // direction array, row pitch lstride elements) by nfl fluid nodes; tma = 1 when valid
     CUtensorMap tmap;

@@ -85,46 +85,4 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
     return true;
 }
 
-void build_warp_table(ListLayout &ll) {
-    const int64_t nf = ll.nf;
-    const int64_t nw = (nf + 31) / 32;
-    ll.off8.assign((size_t)18 * nf, 0);
-    ll.hdr.assign((size_t)nw * 18 * 2, 0);
-    ll.side.clear();
-    for (int64_t w = 0; w < nw; ++w) {
-        const int64_t x0 = 32 * w, x1 = std::min<int64_t>(x0 + 32, nf);
-        for (int d = 0; d < 18; ++d) {
-            const int32_t *row = ll.nb.data() + (size_t)d * nf;
-            int64_t fb = INT64_MAX, fmax = INT64_MIN, lb = -1;
-            for (int64_t x = x0; x < x1; ++x) {
-                const int64_t e = row[x];
-                if (e >= nf) {
-                    if (lb < 0) lb = e;
-                } else {
-                    fb = std::min(fb, e - x);
-                    fmax = std::max(fmax, e - x);
-                }
-            }
-            // the link slots of the warp in this direction array must be consecutive
-            bool ok = true;
-            int64_t next = lb;
-            for (int64_t x = x0; x < x1 && ok; ++x)
-                if (row[x] >= nf) ok = row[x] == next++;
-            if (fb == INT64_MAX) fb = 0, fmax = 0;
-            if (ok && fmax - fb <= 254 && fb >= INT32_MIN && fb <= INT32_MAX) {
-                for (int64_t x = x0; x < x1; ++x) {
-                    const int64_t e = row[x];
-                    ll.off8[(size_t)d * nf + x] = e >= nf ? (uint8_t)255 : (uint8_t)(e - x - fb);
-                }
-                ll.hdr[(size_t)2 * (18 * w + d)] = (int32_t)fb;
-                ll.hdr[(size_t)2 * (18 * w + d) + 1] = (int32_t)(lb < 0 ? 0 : lb);
-            } else {
-                ll.hdr[(size_t)2 * (18 * w + d)] = (int32_t)ll.side.size();
-                ll.hdr[(size_t)2 * (18 * w + d) + 1] = -1;
-                for (int64_t x = x0; x < x0 + 32; ++x) ll.side.push_back(x < x1 ? row[x] : 0);
-            }
-        }
-    }
-}
-
 }  // namespace mflbm

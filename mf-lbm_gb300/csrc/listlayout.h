@@ -30,21 +30,8 @@ struct ListLayout {
     std::vector<int32_t> cell1;     // halo-1 Fortran index of every fluid node
     std::vector<int32_t> link;      // [nlink][3]: direction array q, slot index, halo-1 index of the solid cell
     std::vector<int32_t> slice;     // [nz+1]: first fluid index of every z slice
-    // Warp-compressed neighbour table read by the odd step (22.5 bytes per node instead of
-    // 72).  The nodes of warp w are x = 32w .. 32w+31; for each direction d (row d-1):
-    //   hdr[2*(18w + d-1)] = fb, hdr[+1] = lb;  off8[d-1][x] = 8-bit code of nb[d][x]:
-    //   code < 255: fluid neighbour nb = x + fb + code;
-    //   code = 255: link slot nb = lb + (number of lanes below x in the warp with code 255),
-    //               the warp's link slots of one direction array being consecutive;
-    //   lb < 0 (a "wide" warp-direction, where the fluid offsets span more than 254):
-    //               nb = side[fb + lane] for every lane.
-    std::vector<uint8_t> off8;      // [18][nf]
-    std::vector<int32_t> hdr;       // [nwarp][18][2]
-    std::vector<int32_t> side;      // 32 entries per wide warp-direction
 };
 
-// Builds the warp-compressed table of `ll` from its nb table.
-void build_warp_table(ListLayout &ll);
 
 // Builds the layout for one sample from the halo-2 wall array (Fortran order, int8,
 // 1 = solid).  Returns false with a reason when a fluid node has a neighbour in the

@@ -67,23 +67,3 @@ def test_tma_even_step_equals_plain_even_step(precision):
             assert sa == 0 and np.array_equal(pa, pb)
 
 
-
-@pytest.mark.parametrize("precision", [0, 1, 4])
-def test_warp_table_equals_32bit_table(precision):
-    """The odd step over the warp-compressed neighbour table (per-warp bases, one byte per
-    node and direction, link slots by ballot; "wide" warps at the periodic wrap in z read
-    32-bit entries) reads and writes the same slots as over the 32-bit table."""
-    case = workloads.packing_permeability(n=64, porosity=0.3, seed=23, precision=precision, force_z=1e-5)
-    out = []
-    for switch in (None, "1"):
-        if switch:
-            os.environ["MFLBM_NO_WARP_TABLE"] = switch
-        try:
-            with Solver(case["params"]) as sim:
-                sim.set_geometry(case["walls"])
-                sim.init_equilibrium()
-                sim.run(1, 9)
-                out.append(sim.download_state()["f"])
-        finally:
-            os.environ.pop("MFLBM_NO_WARP_TABLE", None)
-    assert np.array_equal(out[0], out[1])
