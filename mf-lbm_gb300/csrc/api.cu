@@ -59,7 +59,9 @@ struct mflbm_ctx {
 
 static const int kEventRing = 512;
 // fluid fraction above which the colour-gradient stencils run as shared-memory tiles
-static const double kGradientTileFraction = 0.6;
+// (measured: lists faster on the C1 tube, 63 % fluid, 4,378 against 3,717 MLUPS in FP32,
+// and on the porous packings; tiles for nearly open domains such as free drops)
+static const double kGradientTileFraction = 0.9;
 
 static thread_local std::string g_last_create_error;
 

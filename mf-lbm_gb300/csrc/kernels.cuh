@@ -1084,23 +1084,36 @@ __global__ void k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *
     unpack_cell(s.ijk, ix, iy, iz);
     if (!(ix >= 0 && ix <= L.nx + 1 && iy >= 0 && iy <= L.ny + 1 && iz >= 0 && iz <= L.nz + 1)) return;
     const int64_t id = L.i2(ix, iy, iz);
-    T vx[18], vy[18], vz[18];
-#pragma unroll
-    for (int ie = 1; ie <= 18; ++ie) {
-        const bool on = (s.mask >> (ie - 1)) & 1u;
-        const int64_t nb = id + EX(ie) + L.h2x * EY(ie) + L.h2xy * EZ(ie);
-        vx[ie - 1] = on ? cnx[nb] : T(0.0);
-        vy[ie - 1] = on ? cny[nb] : T(0.0);
-        vz[ie - 1] = on ? cnz[nb] : T(0.0);
-    }
     T ax = T(0.0), ay = T(0.0), az = T(0.0);
+    if constexpr (sizeof(T) == 4) {
+        // FP32: all 54 gathers in flight before the sums
+        T vx[18], vy[18], vz[18];
 #pragma unroll
-    for (int ie = 1; ie <= 18; ++ie) {
-        if ((s.mask >> (ie - 1)) & 1u) {
+        for (int ie = 1; ie <= 18; ++ie) {
+            const bool on = (s.mask >> (ie - 1)) & 1u;
+            const int64_t nb = id + EX(ie) + L.h2x * EY(ie) + L.h2xy * EZ(ie);
+            vx[ie - 1] = on ? cnx[nb] : T(0.0);
+            vy[ie - 1] = on ? cny[nb] : T(0.0);
+            vz[ie - 1] = on ? cnz[nb] : T(0.0);
+        }
+#pragma unroll
+        for (int ie = 1; ie <= 18; ++ie) {
+            if ((s.mask >> (ie - 1)) & 1u) {
+                const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
+                ax = ax + vx[ie - 1] * w;
+                ay = ay + vy[ie - 1] * w;
+                az = az + vz[ie - 1] * w;
+            }
+        }
+    } else {
+        // FP64: 54 preloaded doubles would cost occupancy; gather direction by direction
+        for (uint32_t m = s.mask; m; m &= m - 1u) {
+            const int ie = __ffs((int)m);
             const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
-            ax = ax + vx[ie - 1] * w;
-            ay = ay + vy[ie - 1] * w;
-            az = az + vz[ie - 1] * w;
+            const int64_t nb = L.i2(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie]);
+            ax = ax + cnx[nb] * w;
+            ay = ay + cny[nb] * w;
+            az = az + cnz[nb] * w;
         }
     }
     const T lw = T(s.la_weight);
