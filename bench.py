@@ -42,7 +42,7 @@ METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 
 BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1, 4: 19 * 8 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
 BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1,
-                   3: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1}
+                   3: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 4: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1}
 # 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe;
 # 4: double-word storage (hi + lo FP32 pair, 8 bytes) and the double-word collision
 DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff", 4: "ff"}
@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="0 FP64, 1 FP32 (deviations for singlephase), 2 FP16 deviations, "
                          "3 FP64 storage with the double-word collision, 4 double-word storage and collision "
-                         "(3 and 4 singlephase)")
+                         "(FP16 singlephase only)")
     ap.add_argument("--e2e-round", type=int, default=100, help="steps per e2e round")
     ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

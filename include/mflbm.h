@@ -73,8 +73,9 @@ extern "C" {
 #define MFLBM_FP64FF 3 /* FP64 storage, collision in double-word (two-FP32, about 48-bit)
                           arithmetic on the FP32 pipe; every other kernel as MFLBM_FP64
                           (singlephase and multiphase) */
-#define MFLBM_FF 4     /* singlephase: double-word storage (hi + lo FP32 pair per population,
-                          8 bytes, about 48 bits) and the double-word collision */
+#define MFLBM_FF 4     /* double-word storage (hi + lo FP32 pair per population, 8 bytes,
+                          about 48 bits) and the double-word collision; multiphase: also the
+                          double-word normal and curvature stencils on FP64 fields */
 
 /* PDF storage layout (no counterpart in the reference, which stores every cell).
  * DENSE: one plane per direction over the halo-1 box, as the reference's arrays.

@@ -114,10 +114,6 @@ int validate(const mflbm_params *p, std::string &err) {
             err = "multiphase supports MFLBM_FP64 and MFLBM_FP32 storage (FP16 deviations cannot hold a vanishing species)";
             return MFLBM_EINVAL;
         }
-        if (p->precision == MFLBM_FF) {
-            err = "MFLBM_FF (double-word storage) is singlephase; multiphase takes MFLBM_FP64FF";
-            return MFLBM_EINVAL;
-        }
         if (p->la_nu2 <= 0.0) { err = "la_nu2 must be positive"; return MFLBM_EINVAL; }
     } else {
         if (p->iper == 1 && (p->wall_x_max == 1 || p->wall_x_min == 1)) {

@@ -496,13 +496,27 @@ __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restric
 // fold_rates_dev, the pair-form MRT collision with a general force, the recolouring.  Each
 // FP64 value is split on load and joined on store (one FP64 add), so the FP64 pipe carries
 // 39 adds per node instead of the whole collision.
-template <bool ODD>
-__global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, double *__restrict__ g,
+// S: double (MFLBM_FP64FF, FP64 storage split on load and joined on store) or ffs
+// (MFLBM_FF, the double-word pairs stored as they are, renormalised on store)
+template <bool ODD, class S = double>
+__global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__restrict__ g,
                                                     double *__restrict__ phi, const double *__restrict__ cnx,
                                                     const double *__restrict__ cny, const double *__restrict__ cnz,
                                                     const double *__restrict__ cnorm, const double *__restrict__ curv,
                                                     const int32_t *__restrict__ cells, const int ncell, const Layout L,
                                                     const MpConstFF K, const int mrt) {
+    auto ldp = [](const S &v) -> ff {
+        if constexpr (std::is_same<S, ffs>::value) return ff{v.hi, v.lo};
+        else return ff_from_f64(v);
+    };
+    auto stp = [](S &dst, ff v) {
+        if constexpr (std::is_same<S, ffs>::value) {
+            const ff n = ff_fast2sum(v.hi, v.lo);
+            dst = ffs{n.hi, n.lo};
+        } else {
+            dst = f64_of_ff(v);
+        }
+    };
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) return;
     const int64_t c = cells[t];
@@ -515,13 +529,13 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, d
     ff rho1, rho2;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const ff a = ff_from_f64(ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c]);
+        const ff a = ldp(ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c]);
         ft[q] = a;
         rho1 = q == 0 ? a : rho1 + a;
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const ff b = ff_from_f64(ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c]);
+        const ff b = ldp(ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c]);
         ft[q] = ft[q] + b;
         rho2 = q == 0 ? b : rho2 + b;
     }
@@ -550,8 +564,8 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, d
     // recolouring (Kernel_multiphase.F90:272-315)
     const ff tmp1 = rho1 * inv_den;
     const ff tmp = rho1 * rho2 * K.beta * inv_den;
-    f[c] = f64_of_ff(tmp1 * ft[0]);
-    g[c] = f64_of_ff(ft[0] * (ff(1.0f) - tmp1));
+    stp(f[c], tmp1 * ft[0]);
+    stp(g[c], ft[0] * (ff(1.0f) - tmp1));
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
         const ff sx = EX(q) > 0 ? cx : -cx, sy = EY(q) > 0 ? cy : -cy, sz = EZ(q) > 0 ? cz : -cz;
@@ -568,8 +582,8 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(double *__restrict__ f, d
         const ff a = tmp1 * ft[q] + wt * proj;
         const ff b = ft[q] - a;
         const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
-        f[o] = f64_of_ff(a);
-        g[o] = f64_of_ff(b);
+        stp(f[o], a);
+        stp(g[o], b);
     }
 }
 
@@ -2258,13 +2272,20 @@ __global__ void k_change_inlet_phase(T *__restrict__ f, T *__restrict__ g, const
     const int64_t r2 = r - k * nplane;
     const int j = (int)(r2 / nrow), i = (int)(r2 - j * nrow);
     const int64_t id = (int64_t)q * L.qs + L.cell(i, j, k);
-    const T a = f[id], b = g[id];
-    if (to_f) {
-        f[id] = a + b;
-        g[id] = T(0);
+    if constexpr (std::is_same<T, ffs>::value) {
+        // double-word storage: join both to FP64, add, split
+        const double a = Store<ffs>::ld(f, id, 0.0, 0.0), b = Store<ffs>::ld(g, id, 0.0, 0.0);
+        Store<ffs>::st(to_f ? f : g, id, a + b, 0.0, 0.0);
+        Store<ffs>::st(to_f ? g : f, id, 0.0, 0.0, 0.0);
     } else {
-        g[id] = a + b;
-        f[id] = T(0);
+        const T a = f[id], b = g[id];
+        if (to_f) {
+            f[id] = a + b;
+            g[id] = T(0);
+        } else {
+            g[id] = a + b;
+            f[id] = T(0);
+        }
     }
 }
 

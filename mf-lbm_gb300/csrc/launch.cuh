@@ -18,6 +18,11 @@ template <class T> inline T *fld(void *p) { return reinterpret_cast<T *>(p); }
 
 // storage type of the multiphase forms: FP64, or FP32 for the mixed form
 inline bool mp_fp32(const DevState &st) { return st.multiphase && st.prec == MFLBM_FP32; }
+// the multiphase double-word forms (FP64 storage or double-word storage): FP64 fields, the
+// normal and curvature stencils in double-word arithmetic
+inline bool dw_grad(const DevState &st) {
+    return st.multiphase && (st.prec == MFLBM_FP64FF || st.prec == MFLBM_FF);
+}
 
 template <class R> const MrtFold<R> &fold_of(const DevState &st);
 template <> inline const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
@@ -119,16 +124,17 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
     return 1;
 }
 
+template <class S>
 int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
-    double *f = fs<double>(st), *gg = gs<double>(st);
+    S *f = fs<S>(st), *gg = gs<S>(st);
     if (odd)
-        k_mp_step_ff<true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
+        k_mp_step_ff<true, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
                                              fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
                                              st.ncell, st.L, st.mpff, st.P.mrt);
     else
-        k_mp_step_ff<false><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
+        k_mp_step_ff<false, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
                                               fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
                                               st.ncell, st.L, st.mpff, st.P.mrt);
     return 1;
@@ -136,7 +142,8 @@ int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
 
 int collide(const DevState &st, bool odd, cudaStream_t s) {
     if (st.multiphase) {
-        if (st.prec == MFLBM_FP64FF) return collide_mp_ff(st, odd, s);
+        if (st.prec == MFLBM_FP64FF) return collide_mp_ff<double>(st, odd, s);
+        if (st.prec == MFLBM_FF) return collide_mp_ff<ffs>(st, odd, s);
         return mp_fp32(st) ? collide_mp<float>(st, odd, s) : collide_mp<double>(st, odd, s);
     }
     switch (st.prec) {
@@ -267,7 +274,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         else k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
     }
 #ifndef MFLBM_STRICT
-    if (st.gtile && st.prec != MFLBM_FP64FF) {
+    if (st.gtile && !dw_grad(st)) {
         const dim3 b(GRAD_TX, GRAD_TY);
         const dim3 g((L.nx + 4 + GRAD_TX - 1) / GRAD_TX, (L.ny + 4 + GRAD_TY - 1) / GRAD_TY,
                      (L.nz + 4 + GRAD_KCH - 1) / GRAD_KCH);
@@ -276,7 +283,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         if (st.n_gcell_n > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {
-                if (st.prec == MFLBM_FP64FF) {
+                if (dw_grad(st)) {
                     k_normals_list_ff<<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny,
                                                                                 cnz, cnorm, L);
                     done = true;
@@ -296,7 +303,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
     }
     if (st.nf > 0) {
-        const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (st.prec == MFLBM_FP64FF ? T(1e-12) : T(0.0));
+        const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (dw_grad(st) ? T(1e-12) : T(0.0));
         k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L, min_one_m);
     }
     if (st.ns > 0) {
@@ -304,7 +311,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
     }
 #ifndef MFLBM_STRICT
-    if (st.gtile && st.prec != MFLBM_FP64FF) {
+    if (st.gtile && !dw_grad(st)) {
         const dim3 b(GRAD_TX, GRAD_TY);
         const dim3 g((L.nx + GRAD_TX - 1) / GRAD_TX, (L.ny + GRAD_TY - 1) / GRAD_TY, (L.nz + GRAD_KCH - 1) / GRAD_KCH);
         k_curvature_tile<T><<<g, b, 0, s>>>(cnx, cny, cnz, curv, st.walls, L);
@@ -312,7 +319,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         if (st.n_gcell_c > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {
-                if (st.prec == MFLBM_FP64FF) {
+                if (dw_grad(st)) {
                     k_curvature_list_ff<<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
                                                                                   st.n_gcell_c, L);
                     done = true;
@@ -604,6 +611,7 @@ int change_inlet_phase(const DevState &st, int cmd, int kmax, cudaStream_t s) {
     const int64_t n = (int64_t)19 * (L.nx + 2) * (L.ny + 2) * (kmax + 1);
     const unsigned nb = (unsigned)((n + 255) / 256);
     if (mp_fp32(st)) k_change_inlet_phase<float><<<nb, 256, 0, s>>>(fs<float>(st), gs<float>(st), L, kmax, cmd == 1);
+    else if (st.prec == MFLBM_FF) k_change_inlet_phase<ffs><<<nb, 256, 0, s>>>(fs<ffs>(st), gs<ffs>(st), L, kmax, cmd == 1);
     else k_change_inlet_phase<double><<<nb, 256, 0, s>>>(fs<double>(st), gs<double>(st), L, kmax, cmd == 1);
     return 1;
 }

@@ -21,7 +21,7 @@ def make_params(**kw):
     """mflbm_params with the reference's template defaults, overridden by kw.
 
     precision: MFLBM_FP64 (0, the drop-in), MFLBM_FP32 (1), MFLBM_FP16 (2, singlephase),
-    MFLBM_FP64FF (3, FP64 storage with the double-word collision), MFLBM_FF (4, singlephase
+    MFLBM_FP64FF (3, FP64 storage with the double-word collision), MFLBM_FF (4,
     double-word storage); layout: 0 auto, 1 dense, 2 fluid list (singlephase)."""
     p = Params()
     p.abi_version = MFLBM_ABI_VERSION

@@ -54,7 +54,7 @@ def _create(**kw):
     (dict(multiphase=1, mrt=7), "mrt"),
     (dict(nx=2), "dimensions"),
     (dict(precision=5), "precision"),
-    (dict(multiphase=1, precision=4), "double-word storage"),
+    (dict(multiphase=1, precision=2), "FP16 deviations cannot hold a vanishing species"),
 ])
 def test_invalid_parameters_rejected_before_any_device_work(kw, needle):
     rc, msg = _create(**kw)

@@ -112,16 +112,18 @@ MP_CASES = {
 }
 
 
+@pytest.mark.parametrize("precision", [MFLBM_FP64FF, MFLBM_FF])
 @pytest.mark.parametrize("name", list(MP_CASES))
 @pytest.mark.parametrize("steps", [1, 9, 40])
-def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
-    """Multiphase, FP64 storage with the double-word collision and colour-gradient stencils,
-    against the FP64 oracle after n = 1, 9, 40 steps (populations of order 0.1; a wrong term
-    shows at 1e-6 and above): f, g, phi and |grad phi| within 1e-10, the gradient
-    n |grad phi| within 1e-10 away from the wetting nodes and 1e-8 at them, kappa |grad phi|
-    at fluid nodes within 1e-8.  Measured: f within 3e-11, phi within 2e-12."""
+def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps, precision):
+    """Multiphase, the double-word collision and colour-gradient stencils on FP64 storage
+    (MFLBM_FP64FF) or on double-word storage (MFLBM_FF, f and g kept as FP32 pairs), against
+    the FP64 oracle after n = 1, 9, 40 steps (populations of order 0.1; a wrong term shows
+    at 1e-6 and above): f, g, phi and |grad phi| within 1e-10, the gradient n |grad phi|
+    within 1e-10 away from the wetting nodes and 1e-8 at them, kappa |grad phi| at fluid
+    nodes within 1e-8.  Measured (FP64 storage): f within 3e-11, phi within 2e-12."""
     from cases import mp_case
-    case = mp_case(strict=0, precision=MFLBM_FP64FF, **MP_CASES[name])
+    case = mp_case(strict=0, precision=precision, **MP_CASES[name])
     with Solver(case["params"]) as gpu:
         load_case(gpu, case)
         for n in range(1, steps + 1):
@@ -163,7 +165,7 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     ka = (ga["curv"] * ga["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
     kb = (gb["curv"] * gb["c_norm"][1:-1, 1:-1, 1:-1])[1:-1, 1:-1, 1:-1][fl]
     dforce = np.abs(ka - kb).max()
-    print(f"{name} steps {steps}: max |df| {df:.3e} |dphi| {dphi:.3e} |d(n|g|)| {dgrad:.3e} (wetting nodes "
+    print(f"precision {precision} {name} steps {steps}: max |df| {df:.3e} |dphi| {dphi:.3e} |d(n|g|)| {dgrad:.3e} (wetting nodes "
           f"{dgrad_wet:.3e}) |d|g|| {dnorm:.3e} |d(kappa|g|)| {dforce:.3e}")
     assert df <= 1e-10
     assert dphi <= 1e-10
@@ -173,7 +175,7 @@ def test_multiphase_double_word_collision_tracks_fp64_oracle(name, steps):
     assert dforce <= 1e-8
 
 
-@pytest.mark.parametrize("precision", [1, MFLBM_FP64FF])
+@pytest.mark.parametrize("precision", [1, MFLBM_FP64FF, MFLBM_FF])
 def test_wetting_with_wall_parallel_phase_normals_stays_finite(precision):
     """A flat phase slab across a channel walled in x (uniform in y and z, exact rest states):
     every phase normal is parallel to the wall normal, where the reference's wetting factor

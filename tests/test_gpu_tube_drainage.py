@@ -123,3 +123,28 @@ def test_double_word_collision_after_2000_steps(oracle_result):
     assert du <= 1e-9
     assert abs(s_gpu - s_orc) / s_orc <= 1e-9
     gpu.close()
+
+
+def test_double_word_storage_after_2000_steps(oracle_result):
+    """Double-word storage of f and g (FP32 pairs, about 48 bits) with the double-word
+    collision and stencils, against the FP64 oracle: the gates of the FP64-storage form."""
+    case, st, sat, mac = oracle_result
+    p = case["params"]
+    p.strict_fp = 0
+    p.precision = 4
+    gpu = Solver(p)
+    _setup(gpu, case)
+    gpu.run(1, STEPS)
+    a = gpu.download_state()
+    inner = (slice(4, -4),) * 3
+    dphi = np.abs(a["phi"][inner] - st["phi"][inner]).max()
+    m = gpu.macro()
+    du = max(np.abs(m[k][1:-1, 1:-1, 1:-1] - mac[k][1:-1, 1:-1, 1:-1]).max() for k in ("u", "v", "w"))
+    v1, v2 = gpu.saturation()
+    s_gpu, s_orc = v1 / (v1 + v2), sat[0] / (sat[0] + sat[1])
+    print(f"double-word storage after {STEPS} steps: max|dphi|={dphi:.3e} max|du|={du:.3e} "
+          f"dS/S={abs(s_gpu - s_orc) / s_orc:.3e}")
+    assert dphi <= 1e-7
+    assert du <= 1e-9
+    assert abs(s_gpu - s_orc) / s_orc <= 1e-9
+    gpu.close()
