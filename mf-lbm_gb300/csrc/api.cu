@@ -143,8 +143,8 @@ int validate(const mflbm_params *p, std::string &err) {
     }
     if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FF) { err = "unknown precision"; return MFLBM_EINVAL; }
     if (p->layout < MFLBM_LAYOUT_AUTO || p->layout > MFLBM_LAYOUT_LIST) { err = "unknown layout"; return MFLBM_EINVAL; }
-    if (p->layout == MFLBM_LAYOUT_LIST && (p->multiphase || p->inlet_bc != 0 || p->outlet_bc != 0)) {
-        err = "the fluid-list layout is singlephase without inlet/outlet boundary conditions";
+    if (p->layout == MFLBM_LAYOUT_LIST && !p->multiphase && (p->inlet_bc != 0 || p->outlet_bc != 0)) {
+        err = "the singlephase fluid-list layout has no inlet/outlet boundary conditions";
         return MFLBM_EINVAL;
     }
     if (p->la_nu1 <= 0.0) { err = "la_nu1 must be positive"; return MFLBM_EINVAL; }
@@ -205,6 +205,8 @@ int alloc_dense(mflbm_ctx *c) {
     c->st.f = c->pdf;
     c->st.g = c->p.multiphase ? (void *)((char *)c->pdf + plane) : nullptr;
     c->st.list = 0;
+    c->st.mplist = 0;
+    c->st.pmap = nullptr;
     c->st.tma = 0;
     return MFLBM_OK;
 }
@@ -432,7 +434,8 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     (void)nsp;
     // the singlephase storage layout is settled by mflbm_set_geometry; the other cases
     // are dense from the start
-    if (p.multiphase || p.layout == MFLBM_LAYOUT_DENSE || p.inlet_bc != 0 || p.outlet_bc != 0) {
+    if ((p.multiphase && p.layout != MFLBM_LAYOUT_LIST) || p.layout == MFLBM_LAYOUT_DENSE ||
+        (!p.multiphase && (p.inlet_bc != 0 || p.outlet_bc != 0))) {
         if ((r = alloc_dense(c))) goto fail_create;
     }
     if ((r = dalloc(c, &c->st.walls, n2(p)))) goto fail_create;
@@ -446,7 +449,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.err, 1))) goto fail_create;
     // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
     // phase field when that is larger
-    if ((!f64_storage(p) || !p.multiphase) &&
+    if ((!f64_storage(p) || !p.multiphase || p.layout == MFLBM_LAYOUT_LIST) &&
         (r = dalloc(c, &c->st.stage, p.multiphase ? std::max(n1(p), n4(p)) : n1(p)))) goto fail_create;
     if (p.multiphase) {
         const size_t fe = (size_t)c->st.felt;
@@ -580,6 +583,54 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             return MFLBM_OK;
         }
         if (p.layout == MFLBM_LAYOUT_LIST) return fail(c, MFLBM_EINVAL, "fluid-list layout: " + why);
+        int r = alloc_dense(c);
+        if (r) return r;
+    }
+    // multiphase fluid list (MpListLayout in listlayout.h): f and g hold the fluid nodes, the
+    // boundary planes' private slots and the link slots; phi and the gradient fields stay dense
+    if (p.multiphase && p.layout == MFLBM_LAYOUT_LIST) {
+        std::vector<int> planes;
+        if (c->open_z)
+            for (int k : {0, 1, 2, p.nz - 1, p.nz, p.nz + 1}) planes.push_back(k);
+        if (p.porous_plate_cmd != 0)
+            for (int dz = -1; dz <= 1; ++dz) planes.push_back(p.z_porous_plate + dz);
+        MpListLayout ml;
+        std::string why;
+        if (!build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, planes, ml, why))
+            return fail(c, MFLBM_EINVAL, "multiphase fluid-list layout: " + why);
+        for (void *b : c->list_bufs) dfree(c, b);
+        c->list_bufs.clear();
+        int r = alloc_pdf(c, (size_t)2 * 19 * ml.stride * c->elt);
+        if (r) return r;
+        int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *map = nullptr;
+        if ((r = dalloc(c, &nb, 18 * ml.nf))) return r;
+        c->list_bufs.push_back(nb);
+        if ((r = dalloc(c, &cell1, ml.nf))) return r;
+        c->list_bufs.push_back(cell1);
+        if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * ml.nlink)))) return r;
+        c->list_bufs.push_back(link);
+        if ((r = dalloc(c, &map, (int64_t)ml.map.size()))) return r;
+        c->list_bufs.push_back(map);
+        CK(c, cudaMemcpy(nb, ml.nb.data(), sizeof(int32_t) * ml.nb.size(), cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(cell1, ml.cell1.data(), sizeof(int32_t) * ml.cell1.size(), cudaMemcpyHostToDevice));
+        if (ml.nlink) CK(c, cudaMemcpy(link, ml.link.data(), sizeof(int32_t) * ml.link.size(), cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(map, ml.map.data(), sizeof(int32_t) * ml.map.size(), cudaMemcpyHostToDevice));
+        DevState &st = c->st;
+        st.list = 1;
+        st.mplist = 1;
+        st.tma = 0;
+        st.f = c->pdf;
+        st.g = (void *)((char *)c->pdf + (size_t)19 * ml.stride * c->elt);
+        st.lstride = ml.stride;
+        st.nb = nb;
+        st.cell1 = cell1;
+        st.link = link;
+        st.nlink = ml.nlink;
+        st.nfl = (int)ml.nf;
+        st.lseg = nullptr;
+        st.pmap = map;
+        st.pspare = ml.spare;
+    } else if (p.multiphase && (!c->pdf || c->st.list)) {
         int r = alloc_dense(c);
         if (r) return r;
     }

@@ -60,6 +60,28 @@ struct Layout {
     __host__ __device__ __forceinline__ int64_t ic(int i, int j, int q) const { return (int64_t)i + h1x * j + h1xy * q; }
 };
 
+// Where population q of the halo-1 cell (i, j, k) is stored, for the kernels that address
+// PDFs by cell (boundary conditions, monitor, initialisation): the dense planes (map ==
+// nullptr, qs = Layout::qs) or the multiphase fluid list (map: slot of every halo-1 cell,
+// >= 0 owned, <= -2 the periodic image's slot -m-2, -1 none; qs = the list stride).
+struct PdfAt {
+    int64_t qs;
+    const int32_t *map;
+    int64_t spare;     // list: the slot of cells that have none (never read for a value)
+    __host__ __device__ __forceinline__ int64_t slot(const Layout &L, int i, int j, int k) const {
+        if (!map) return L.cell(i, j, k);
+        const int32_t m = map[L.i1(i, j, k)];
+        return m >= 0 ? (int64_t)m : (m <= -2 ? (int64_t)(-m - 2) : spare);
+    }
+    // the cell owns its slot (dense: every cell)
+    __host__ __device__ __forceinline__ bool owned(const Layout &L, int i, int j, int k) const {
+        return !map || map[L.i1(i, j, k)] >= 0;
+    }
+    __host__ __device__ __forceinline__ int64_t operator()(const Layout &L, int q, int i, int j, int k) const {
+        return (int64_t)q * qs + slot(L, i, j, k);
+    }
+};
+
 // Parameters read by the per-step kernels.
 struct StepParams {
     double force_z;

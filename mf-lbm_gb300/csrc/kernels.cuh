@@ -372,33 +372,68 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
 // ---------------------------------------------------------------------------------
 // T = double: the FP64 drop-in; T = float: the mixed form (FP32 storage of f, g, phi
 // and the gradient fields, FP32 arithmetic).
-template <class T, bool ODD>
+// The node of a multiphase collision thread and the slots of its populations: the dense
+// planes (cells[t] is the padded-layout index; pull from c - e_q on odd steps) or the fluid
+// list (cells[t] is the halo-1 index of fluid node t; nb[d-1][t] is the slot of t + e_d).
+// Defines c, i, j, k and the slot functions src(q) (read) and dst(q) (write, q >= 1).
+#define MP_NODE_ADDRESSING                                                                          \
+    int64_t c;                                                                                      \
+    int i, j, k;                                                                                    \
+    int32_t nbr[18];                                                                                \
+    if constexpr (LIST) {                                                                           \
+        c = t;                                                                                      \
+        const int64_t h = cells[t];                                                                 \
+        k = (int)(h / L.h1xy);                                                                      \
+        const int64_t r_ = h - (int64_t)k * L.h1xy;                                                 \
+        j = (int)(r_ / L.h1x);                                                                      \
+        i = (int)(r_ - (int64_t)j * L.h1x);                                                         \
+        if constexpr (ODD) {                                                                        \
+            _Pragma("unroll") for (int d = 0; d < 18; ++d) nbr[d] = nb[(int64_t)d * ncell + t];     \
+        }                                                                                           \
+    } else {                                                                                        \
+        c = cells[t];                                                                               \
+        k = (int)(c / L.pz);                                                                        \
+        const int64_t r_ = c - (int64_t)k * L.pz;                                                   \
+        j = (int)(r_ / L.pitch);                                                                    \
+        i = (int)(r_ - (int64_t)j * L.pitch) - L.xo;                                                \
+        (void)nbr;                                                                                  \
+    }                                                                                               \
+    auto src = [&](int q) -> int64_t {                                                              \
+        if constexpr (LIST)                                                                         \
+            return ODD ? (q == 0 ? c : (int64_t)q * stride + nbr[OPP(q) - 1]) : (int64_t)OPP(q) * stride + c; \
+        else                                                                                        \
+            return ODD ? (int64_t)q * L.qs + c - qoff(L, q) : (int64_t)OPP(q) * L.qs + c;           \
+    };                                                                                              \
+    auto dst = [&](int q) -> int64_t {                                                              \
+        if constexpr (LIST)                                                                         \
+            return ODD ? (int64_t)OPP(q) * stride + nbr[q - 1] : (int64_t)q * stride + c;           \
+        else                                                                                        \
+            return ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;           \
+    };
+
+template <class T, bool ODD, bool LIST = false>
 __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
                                                  const T *__restrict__ cnx, const T *__restrict__ cny,
                                                  const T *__restrict__ cnz, const T *__restrict__ cnorm,
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
-                                                 const int ncell, const Layout L, const StepParams P, const double rk_weight2) {
+                                                 const int ncell, const Layout L, const StepParams P, const double rk_weight2,
+                                                 const int32_t *__restrict__ nb = nullptr, const int64_t stride = 0) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) return;
-    const int64_t c = cells[t];
-    // lattice coordinates of the cell, for the auxiliary arrays in Fortran layout
-    const int k = (int)(c / L.pz);
-    const int64_t r = c - (int64_t)k * L.pz;
-    const int j = (int)(r / L.pitch);
-    const int i = (int)(r - (int64_t)j * L.pitch) - L.xo;
+    MP_NODE_ADDRESSING
     const int64_t w2 = L.i2(i, j, k);
     T ft[19];
     T rho1 = T(0.0), rho2 = T(0.0);
     // pull (odd) or local swapped read (even); rho1/rho2 accumulate in the written order
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const T a = ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c];
+        const T a = f[src(q)];
         ft[q] = a;
         rho1 = q == 0 ? a : rho1 + a;
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const T b = ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c];
+        const T b = g[src(q)];
         ft[q] = ft[q] + b;
         rho2 = q == 0 ? b : rho2 + b;
     }
@@ -483,7 +518,7 @@ __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restric
         const T wq = q <= 6 ? T(w_equ_1) : rkw2;
         const T a = tmp1 * ft[q] + wq * tmp * (proj);
         const T b = ft[q] - a;
-        const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
+        const int64_t o = dst(q);
         f[o] = a;
         g[o] = b;
     }
@@ -498,13 +533,14 @@ __global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restric
 // 39 adds per node instead of the whole collision.
 // S: double (MFLBM_FP64FF, FP64 storage split on load and joined on store) or ffs
 // (MFLBM_FF, the double-word pairs stored as they are, renormalised on store)
-template <bool ODD, class S = double>
+template <bool ODD, class S = double, bool LIST = false>
 __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__restrict__ g,
                                                     double *__restrict__ phi, const double *__restrict__ cnx,
                                                     const double *__restrict__ cny, const double *__restrict__ cnz,
                                                     const double *__restrict__ cnorm, const double *__restrict__ curv,
                                                     const int32_t *__restrict__ cells, const int ncell, const Layout L,
-                                                    const MpConstFF K, const int mrt) {
+                                                    const MpConstFF K, const int mrt,
+                                                    const int32_t *__restrict__ nb = nullptr, const int64_t stride = 0) {
     auto ldp = [](const S &v) -> ff {
         if constexpr (std::is_same<S, ffs>::value) return ff{v.hi, v.lo};
         else return ff_from_f64(v);
@@ -519,23 +555,19 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__r
     };
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) return;
-    const int64_t c = cells[t];
-    const int k = (int)(c / L.pz);
-    const int64_t r = c - (int64_t)k * L.pz;
-    const int j = (int)(r / L.pitch);
-    const int i = (int)(r - (int64_t)j * L.pitch) - L.xo;
+    MP_NODE_ADDRESSING
     const int64_t w2 = L.i2(i, j, k);
     ff ft[19];
     ff rho1, rho2;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const ff a = ldp(ODD ? f[(int64_t)q * L.qs + c - qoff(L, q)] : f[(int64_t)OPP(q) * L.qs + c]);
+        const ff a = ldp(f[src(q)]);
         ft[q] = a;
         rho1 = q == 0 ? a : rho1 + a;
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const ff b = ldp(ODD ? g[(int64_t)q * L.qs + c - qoff(L, q)] : g[(int64_t)OPP(q) * L.qs + c]);
+        const ff b = ldp(g[src(q)]);
         ft[q] = ft[q] + b;
         rho2 = q == 0 ? b : rho2 + b;
     }
@@ -581,7 +613,7 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__r
         const ff wt = q <= 6 ? K.w1_tmp_scale * tmp : K.rkw2 * tmp;
         const ff a = tmp1 * ft[q] + wt * proj;
         const ff b = ft[q] - a;
-        const int64_t o = ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;
+        const int64_t o = dst(q);
         stp(f[o], a);
         stp(g[o], b);
     }
@@ -735,7 +767,7 @@ template <class R> __device__ __forceinline__ R sel(R x, R y, int w) { return x 
 // velocity inlet (Boundary_multiphase_inlet.F90:6-102; singlephase Boundary.F90:5-73)
 template <class S>
 __global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
-                                 const int8_t *__restrict__ walls, const double *__restrict__ w_in, const Layout L,
+                                 const int8_t *__restrict__ walls, const double *__restrict__ w_in, const Layout L, const PdfAt pa,
                                  const StepParams P, int before_odd, int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
@@ -763,8 +795,8 @@ __global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, typename 
         S *A = s == 0 ? f : g;
         const R t = R(s == 0 ? tmp1 : tmp2);
         const float rf = ref;
-        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
-        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, pa(L, q, ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, pa(L, q, ii, jj, kk), v, R(WREST(q) * rf), sc); };
         const R c1 = R(6.0 * w_equ_1), c2 = R(6.0 * w_equ_2);
         if (before_odd) {
             st(5, i, j, 0, sel<R>(ld(6, i, j, 1) + c1 * t, ld(5, i, j, 0), wi));
@@ -785,7 +817,7 @@ __global__ void k_inlet_velocity(S *__restrict__ f, S *__restrict__ g, typename 
 // Zou-He pressure inlet (Boundary_multiphase_inlet.F90:115-294; Boundary.F90:80-187)
 template <class S>
 __global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
-                              const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                              const int8_t *__restrict__ walls, const Layout L, const PdfAt pa, const StepParams P, int before_odd,
                               int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
@@ -813,8 +845,8 @@ __global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Sto
     for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
         S *A = s == 0 ? f : g;
         const float rf = ref;
-        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
-        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, pa(L, q, ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, pa(L, q, ii, jj, kk), v, R(WREST(q) * rf), sc); };
         const R c3 = R(0.333333333333333333), c6 = R(0.166666666666666667);
         if (before_odd) {
             const R t = (R(rhos[s]) - (ld(0, i, j, 1) + ld(1, i - 1, j, 1) + ld(2, i + 1, j, 1) + ld(3, i, j - 1, 1) +
@@ -853,7 +885,7 @@ __global__ void k_inlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Sto
 template <class S>
 __global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
                                     double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
-                                    const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                                    const int8_t *__restrict__ walls, const Layout L, const PdfAt pa, const StepParams P, int before_odd,
                                     int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
@@ -879,8 +911,8 @@ __global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, typena
         S *A = s == 0 ? f : g;
         double *C = s == 0 ? fconv : gconv;
         const float rf = ref;
-        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
-        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        auto ld = [&](int q, int ii, int jj, int kk) { return St::ld(A, pa(L, q, ii, jj, kk), R(WREST(q) * rf), inv); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, pa(L, q, ii, jj, kk), v, R(WREST(q) * rf), sc); };
         auto cv = [&](int q) -> double & { return C[L.ic(i, j, q)]; };
         if (before_odd) {
             st(6, i, j, nz + 1, sel<R>((R(cv(6)) + uc * ld(6, i, j, nz)) * tp, ld(6, i, j, nz + 1), wi));
@@ -911,7 +943,7 @@ __global__ void k_outlet_convective(S *__restrict__ f, S *__restrict__ g, typena
 // Zou-He pressure outlet (Boundary_multiphase_outlet.F90:139-311; Boundary.F90:284-389)
 template <class S>
 __global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename Store<S>::R *__restrict__ phi,
-                               const int8_t *__restrict__ walls, const Layout L, const StepParams P, int before_odd,
+                               const int8_t *__restrict__ walls, const Layout L, const PdfAt pa, const StepParams P, int before_odd,
                                int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
@@ -930,7 +962,7 @@ __global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename St
     }
     const R inv = R(1.0f / scale), sc = R(scale);
     const float rf = ref;
-    auto LD = [&](S *A, int q, int ii, int jj, int kk) { return St::ld(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), R(WREST(q) * rf), inv); };
+    auto LD = [&](S *A, int q, int ii, int jj, int kk) { return St::ld(A, pa(L, q, ii, jj, kk), R(WREST(q) * rf), inv); };
     R t1;
     for (int s = 0; s < (multiphase ? 2 : 1); ++s) {
         S *A = s == 0 ? f : g;
@@ -964,7 +996,7 @@ __global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename St
         S *A = s == 0 ? f : g;
         const R t = s == 0 ? t1 : t2;
         auto ld = [&](int q, int ii, int jj, int kk) { return LD(A, q, ii, jj, kk); };
-        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, (int64_t)q * L.qs + L.cell(ii, jj, kk), v, R(WREST(q) * rf), sc); };
+        auto st = [&](int q, int ii, int jj, int kk, R v) { St::st(A, pa(L, q, ii, jj, kk), v, R(WREST(q) * rf), sc); };
         if (before_odd) {
             const R tnx = R(0.5) * (ld(1, i - 1, j, nz) + ld(7, i - 1, j - 1, nz) + ld(9, i - 1, j + 1, nz) -
                                     (ld(2, i + 1, j, nz) + ld(8, i + 1, j - 1, nz) + ld(10, i + 1, j + 1, nz)));
@@ -990,13 +1022,13 @@ __global__ void k_outlet_zouhe(S *__restrict__ f, S *__restrict__ g, typename St
 // porous plate (Boundary_multiphase_other.F90:8-184); blocked = the species that is
 // reflected, passing = the species copied across.
 template <class T>
-__global__ void k_porous_plate(T *__restrict__ blocked, T *__restrict__ passing, const Layout L, int z,
+__global__ void k_porous_plate(T *__restrict__ blocked, T *__restrict__ passing, const Layout L, const PdfAt pa, int z,
                                int before_odd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1;
     if (i > L.nx) return;
-    auto b = [&](int q, int ii, int jj, int kk) -> T & { return blocked[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
-    auto c = [&](int q, int ii, int jj, int kk) -> T & { return passing[(int64_t)q * L.qs + L.cell(ii, jj, kk)]; };
+    auto b = [&](int q, int ii, int jj, int kk) -> T & { return blocked[pa(L, q, ii, jj, kk)]; };
+    auto c = [&](int q, int ii, int jj, int kk) -> T & { return passing[pa(L, q, ii, jj, kk)]; };
     if (before_odd) {
         b(6, i, j, z) = b(5, i, j, z - 1);
         b(13, i - 1, j, z) = b(12, i, j, z - 1);
@@ -1525,8 +1557,9 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
                                                          const typename Store<S>::R *__restrict__ cnz, const typename Store<S>::R *__restrict__ cnorm,
                                                          const typename Store<S>::R *__restrict__ curv, double *__restrict__ u,
                                                          double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho,
-                                                         double *__restrict__ out, const Layout L, const StepParams P,
-                                                         int multiphase, int write_fields, float ref, float scale) {
+                                                         double *__restrict__ out, const Layout L, const PdfAt pa,
+                                                         const StepParams P, int multiphase, int write_fields, float ref,
+                                                         float scale) {
     using St = Store<S>;
     using R = typename St::R;
     const int k = blockIdx.x + 1;
@@ -1538,12 +1571,12 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
     for (int64_t t = threadIdx.x; t < n; t += MON_THREADS) {
         const int i = (int)(t % L.nx) + 1, j = (int)(t / L.nx) + 1;
         const int wi = walls[L.i2(i, j, k)];
-        const int64_t c = L.cell(i, j, k);
+        const int64_t c = pa.slot(L, i, j, k);
         double ft[19];
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            double a = St::ld64(f, (int64_t)q * L.qs + c, WREST(q) * ref, inv);
-            if (multiphase) a = a + St::ld64(g, (int64_t)q * L.qs + c, WREST(q) * ref, inv);
+            double a = St::ld64(f, (int64_t)q * pa.qs + c, WREST(q) * ref, inv);
+            if (multiphase) a = a + St::ld64(g, (int64_t)q * pa.qs + c, WREST(q) * ref, inv);
             ft[q] = a;
         }
         const double m = (double)(1 - wi);
@@ -1639,7 +1672,7 @@ __global__ void __launch_bounds__(MON_THREADS) k_saturation(const T *__restrict_
 template <class S>
 __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const typename Store<S>::R *__restrict__ phi, double *__restrict__ u,
                           double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho, const Layout L,
-                          int multiphase, float ref, float scale) {
+                          const PdfAt pa, int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
@@ -1648,12 +1681,13 @@ __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const typename S
     const int i = (int)(t % (L.nx + 2));
     const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
     const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
-    const int64_t c = L.cell(i, j, k);
     // t enumerates the halo-1 box in Fortran order, so it is also the u/v/w/rho index
     u[t] = 0.0;
     v[t] = 0.0;
     w[t] = 0.0;
     rho[t] = 1.0;
+    if (!pa.owned(L, i, j, k)) return;   // fluid list: the cell has no slot of its own
+    const int64_t c = pa.slot(L, i, j, k);
     const double usqrt = 0.0;
     double r0, r1 = 0.0;
     if (multiphase) {
@@ -1669,10 +1703,10 @@ __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const typename S
         const double wq = WEQ(q);
         const double cu = 0.0;
         const double a = q == 0 ? r0 * wq + r0 * wq * (-1.5 * usqrt) : r0 * wq + r0 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
-        St::st64(f, (int64_t)q * L.qs + c, a, WREST(q) * ref, scale);
+        St::st64(f, (int64_t)q * pa.qs + c, a, WREST(q) * ref, scale);
         if (multiphase) {
             const double b = q == 0 ? r1 * wq + r1 * wq * (-1.5 * usqrt) : r1 * wq + r1 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
-            St::st64(g, (int64_t)q * L.qs + c, b, WREST(q) * ref, scale);
+            St::st64(g, (int64_t)q * pa.qs + c, b, WREST(q) * ref, scale);
         }
     }
 }
@@ -1680,7 +1714,7 @@ __global__ void k_init_eq(S *__restrict__ f, S *__restrict__ g, const typename S
 template <class S>
 __global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, const typename Store<S>::R *__restrict__ phi,
                               double *__restrict__ fconv, double *__restrict__ gconv, double *__restrict__ phiconv,
-                              const Layout L, int multiphase, float ref, float scale) {
+                              const Layout L, const PdfAt pa, int multiphase, float ref, float scale) {
     using St = Store<S>;
     using R = typename St::R;
     const int64_t np = (int64_t)(L.nx + 2) * (L.ny + 2);
@@ -1689,9 +1723,9 @@ __global__ void k_init_convec(const S *__restrict__ f, const S *__restrict__ g, 
     const int i = (int)(t % (L.nx + 2)), j = (int)(t / (L.nx + 2));
     const R inv = R(1.0f / scale);
     for (int q = 0; q < 19; ++q) {
-        fconv[L.ic(i, j, q)] = St::ld64(f, (int64_t)q * L.qs + L.cell(i, j, L.nz), WREST(q) * ref, inv);
+        fconv[L.ic(i, j, q)] = St::ld64(f, pa(L, q, i, j, L.nz), WREST(q) * ref, inv);
         if (multiphase)
-            gconv[L.ic(i, j, q)] = St::ld64(g, (int64_t)q * L.qs + L.cell(i, j, L.nz), WREST(q) * ref, inv);
+            gconv[L.ic(i, j, q)] = St::ld64(g, pa(L, q, i, j, L.nz), WREST(q) * ref, inv);
     }
     if (multiphase) phiconv[L.ip(i, j)] = (double)phi[L.i4(i, j, L.nz)];
 }
@@ -2037,6 +2071,53 @@ __global__ void k_list_out(const S *__restrict__ A, const int64_t stride, const 
     }
 }
 
+// ---------------------------------------------------------------------------------
+// The multiphase fluid list (listlayout.h, MpListLayout): the boundary planes' private slots
+// (map >= nf) against a dense FP64 image of one direction in `stage` (halo-1 Fortran
+// order), the equilibrium of the link slots, and change_inlet_fluid_phase on them.  Fluid
+// nodes and link slots move through k_list_in / k_list_out as in the singlephase list.
+// ---------------------------------------------------------------------------------
+template <class S>
+__global__ void k_mp_planes_in(S *__restrict__ A, const int64_t stride, const int q, const int32_t *__restrict__ map,
+                               const int nf, const int64_t n1, const double *__restrict__ stage) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1) return;
+    const int32_t m = map[t];
+    if (m >= nf) Store<S>::st64(A + (int64_t)q * stride, m, stage[t], WREST(q), 1.0f);
+}
+
+template <class S>
+__global__ void k_mp_planes_out(const S *__restrict__ A, const int64_t stride, const int q,
+                                const int32_t *__restrict__ map, const int nf, const int64_t n1,
+                                double *__restrict__ stage) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1) return;
+    const int32_t m = map[t];
+    if (m >= nf) stage[t] = Store<S>::ld64(A + (int64_t)q * stride, m, WREST(q), 1.0f);
+}
+
+// the equilibrium at rest of every link slot, from phi at its solid cell: k_init_eq's
+// expression for that cell and direction
+template <class S>
+__global__ void k_mp_init_links(S *__restrict__ f, S *__restrict__ g, const typename Store<S>::R *__restrict__ phi,
+                                const int64_t stride, const int32_t *__restrict__ link, const int64_t nlink,
+                                const Layout L) {
+    const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nlink) return;
+    const int q = link[3 * l];
+    const int64_t slot = link[3 * l + 1], h = link[3 * l + 2];
+    const int k = (int)(h / L.h1xy);
+    const int64_t r = h - (int64_t)k * L.h1xy;
+    const int j = (int)(r / L.h1x), i = (int)(r - (int64_t)j * L.h1x);
+    const double ph = (double)phi[L.i4(i, j, k)];
+    const double r0 = 1.0 * (1.0 + ph) * 0.5, r1 = 1.0 * (1.0 - ph) * 0.5;
+    const double usqrt = 0.0, cu = 0.0, wq = WEQ(q);
+    const double a = q == 0 ? r0 * wq + r0 * wq * (-1.5 * usqrt) : r0 * wq + r0 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
+    const double b = q == 0 ? r1 * wq + r1 * wq * (-1.5 * usqrt) : r1 * wq + r1 * wq * (3.0 * cu + 4.5 * cu * cu - 1.5 * usqrt);
+    Store<S>::st64(f, (int64_t)q * stride + slot, a, WREST(q), 1.0f);
+    Store<S>::st64(g, (int64_t)q * stride + slot, b, WREST(q), 1.0f);
+}
+
 static __global__ void k_list_ghosts(double *__restrict__ stage, const Layout L, int px, int py, int pz) {
     const int64_t n = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2262,7 +2343,8 @@ __global__ void __launch_bounds__(MON_THREADS) k_steady(const T *__restrict__ ph
 // both populations and the other is emptied; to_f = 1 (cmd 1): f <- f + g, g <- 0;
 // to_f = 0 (cmd 2): g <- f + g, f <- 0.  One thread per (q, cell).
 template <class T>
-__global__ void k_change_inlet_phase(T *__restrict__ f, T *__restrict__ g, const Layout L, int kmax, int to_f) {
+__global__ void k_change_inlet_phase(T *__restrict__ f, T *__restrict__ g, const Layout L, const PdfAt pa, int kmax,
+                                     int to_f) {
     const int64_t nrow = L.nx + 2, nplane = nrow * (L.ny + 2), ncell = nplane * (kmax + 1);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 19 * ncell) return;
@@ -2271,9 +2353,36 @@ __global__ void k_change_inlet_phase(T *__restrict__ f, T *__restrict__ g, const
     const int k = (int)(r / nplane);
     const int64_t r2 = r - k * nplane;
     const int j = (int)(r2 / nrow), i = (int)(r2 - j * nrow);
-    const int64_t id = (int64_t)q * L.qs + L.cell(i, j, k);
+    if (!pa.owned(L, i, j, k)) return;   // fluid list: link slots are updated from the link table
+    const int64_t id = pa(L, q, i, j, k);
     if constexpr (std::is_same<T, ffs>::value) {
         // double-word storage: join both to FP64, add, split
+        const double a = Store<ffs>::ld(f, id, 0.0, 0.0), b = Store<ffs>::ld(g, id, 0.0, 0.0);
+        Store<ffs>::st(to_f ? f : g, id, a + b, 0.0, 0.0);
+        Store<ffs>::st(to_f ? g : f, id, 0.0, 0.0, 0.0);
+    } else {
+        const T a = f[id], b = g[id];
+        if (to_f) {
+            f[id] = a + b;
+            g[id] = T(0);
+        } else {
+            g[id] = a + b;
+            f[id] = T(0);
+        }
+    }
+}
+
+// the same for the link slots of the multiphase fluid list whose solid cell has k <= kmax
+template <class T>
+__global__ void k_change_inlet_links(T *__restrict__ f, T *__restrict__ g, const int64_t stride,
+                                     const int32_t *__restrict__ link, const int64_t nlink, const Layout L, int kmax,
+                                     int to_f) {
+    const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nlink) return;
+    const int k = (int)(link[3 * l + 2] / L.h1xy);
+    if (k > kmax) return;
+    const int64_t id = (int64_t)link[3 * l] * stride + link[3 * l + 1];
+    if constexpr (std::is_same<T, ffs>::value) {
         const double a = Store<ffs>::ld(f, id, 0.0, 0.0), b = Store<ffs>::ld(g, id, 0.0, 0.0);
         Store<ffs>::st(to_f ? f : g, id, a + b, 0.0, 0.0);
         Store<ffs>::st(to_f ? g : f, id, 0.0, 0.0, 0.0);

@@ -24,6 +24,15 @@ inline bool dw_grad(const DevState &st) {
     return st.multiphase && (st.prec == MFLBM_FP64FF || st.prec == MFLBM_FF);
 }
 
+// where the cell-addressed kernels find a population: dense planes or the multiphase list
+inline PdfAt pdf_at(const DevState &st) {
+    PdfAt a;
+    a.qs = st.mplist ? st.lstride : st.L.qs;
+    a.map = st.mplist ? st.pmap : nullptr;
+    a.spare = st.pspare;
+    return a;
+}
+
 template <class R> const MrtFold<R> &fold_of(const DevState &st);
 template <> inline const MrtFold<double> &fold_of<double>(const DevState &st) { return st.fold; }
 template <> inline const MrtFold<float> &fold_of<float>(const DevState &st) { return st.fold32; }
@@ -110,6 +119,19 @@ int collide_t(const DevState &st, bool odd, cudaStream_t s) {
 
 template <class T>
 int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
+    if (st.mplist) {
+        const unsigned nb = (unsigned)((st.nfl + 127) / 128);
+        T *f = fs<T>(st), *gg = gs<T>(st);
+        if (odd)
+            k_mp_step<T, true, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny),
+                                                        fld<T>(st.cnz), fld<T>(st.cnorm), fld<T>(st.curv), st.cell1,
+                                                        st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
+        else
+            k_mp_step<T, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny),
+                                                         fld<T>(st.cnz), fld<T>(st.cnorm), fld<T>(st.curv), st.cell1,
+                                                         st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
+        return 1;
+    }
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     T *f = fs<T>(st), *gg = gs<T>(st);
@@ -126,6 +148,21 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
 
 template <class S>
 int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
+    if (st.mplist) {
+        const unsigned nb = (unsigned)((st.nfl + 127) / 128);
+        S *f = fs<S>(st), *gg = gs<S>(st);
+        if (odd)
+            k_mp_step_ff<true, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx),
+                                                           fld<double>(st.cny), fld<double>(st.cnz), fld<double>(st.cnorm),
+                                                           fld<double>(st.curv), st.cell1, st.nfl, st.L, st.mpff, st.P.mrt,
+                                                           st.nb, st.lstride);
+        else
+            k_mp_step_ff<false, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx),
+                                                            fld<double>(st.cny), fld<double>(st.cnz),
+                                                            fld<double>(st.cnorm), fld<double>(st.curv), st.cell1, st.nfl,
+                                                            st.L, st.mpff, st.P.mrt, st.nb, st.lstride);
+        return 1;
+    }
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     S *f = fs<S>(st), *gg = gs<S>(st);
@@ -188,10 +225,11 @@ int wrap_t(const DevState &st, bool pull, cudaStream_t s) {
 }
 
 int wrap(const DevState &st, bool pull, cudaStream_t s) {
-    // the fluid-list neighbour table already wraps periodic directions
-    if (st.list || !(st.P.iper || st.P.jper || st.P.kper)) return 0;
-    int n_launch;
-    switch (st.prec) {
+    // the fluid-list neighbour table already wraps periodic directions (phi, dense in every
+    // layout, is wrapped below)
+    if ((st.list && !st.mplist) || !(st.P.iper || st.P.jper || st.P.kper)) return 0;
+    int n_launch = 0;
+    if (!st.mplist) switch (st.prec) {
         case MFLBM_FP32: n_launch = st.multiphase ? wrap_t<float>(st, pull, s) : wrap_t<dfloat>(st, pull, s); break;
         case MFLBM_FP16: n_launch = wrap_t<__half>(st, pull, s); break;
         case MFLBM_FF: n_launch = wrap_t<ffs>(st, pull, s); break;
@@ -222,14 +260,17 @@ int boundary_t(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc,
     const int bo = before_odd ? 1 : 0;
     if (open_z) {
         if (inlet_bc == 1)
-            k_inlet_velocity<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, st.w_in, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_inlet_velocity<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, st.w_in, L, pdf_at(st), st.P, bo, st.multiphase,
+                                                st.ref, st.scale);
         else if (inlet_bc == 2)
-            k_inlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_inlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, pdf_at(st), st.P, bo, st.multiphase, st.ref,
+                                             st.scale);
         if (outlet_bc == 1)
-            k_outlet_convective<S><<<g, b, 0, s>>>(f, gg, phi, st.fconv, st.gconv, st.phiconv, st.walls, L, st.P, bo,
-                                                   st.multiphase, st.ref, st.scale);
+            k_outlet_convective<S><<<g, b, 0, s>>>(f, gg, phi, st.fconv, st.gconv, st.phiconv, st.walls, L, pdf_at(st),
+                                                   st.P, bo, st.multiphase, st.ref, st.scale);
         else if (outlet_bc == 2)
-            k_outlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, st.P, bo, st.multiphase, st.ref, st.scale);
+            k_outlet_zouhe<S><<<g, b, 0, s>>>(f, gg, phi, st.walls, L, pdf_at(st), st.P, bo, st.multiphase, st.ref,
+                                              st.scale);
         n_launch += (inlet_bc == 1 || inlet_bc == 2) + (outlet_bc == 1 || outlet_bc == 2);
     }
     return n_launch;
@@ -253,10 +294,10 @@ int boundary(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc, b
         void *passing = st.P.porous_plate_cmd == 1 ? st.g : st.f;
         const dim3 gp((L.nx + bx - 1) / bx, L.ny);
         if (mp_fp32(st))
-            k_porous_plate<float><<<gp, bx, 0, s>>>(fld<float>(blocked), fld<float>(passing), L, st.P.z_porous_plate,
-                                                    before_odd ? 1 : 0);
+            k_porous_plate<float><<<gp, bx, 0, s>>>(fld<float>(blocked), fld<float>(passing), L, pdf_at(st),
+                                                    st.P.z_porous_plate, before_odd ? 1 : 0);
         else
-            k_porous_plate<double><<<gp, bx, 0, s>>>(fld<double>(blocked), fld<double>(passing), L,
+            k_porous_plate<double><<<gp, bx, 0, s>>>(fld<double>(blocked), fld<double>(passing), L, pdf_at(st),
                                                      st.P.z_porous_plate, before_odd ? 1 : 0);
         ++n_launch;
     }
@@ -348,7 +389,7 @@ int color_gradient(const DevState &st, cudaStream_t s) {
 template <class S>
 int monitor_t(const DevState &st, cudaStream_t s) {
     using FT = typename Store<S>::R;
-    if (st.list) {
+    if (st.list && !st.mplist) {
         const size_t b1 = sizeof(double) * (size_t)(st.L.nx + 2) * (st.L.ny + 2) * (st.L.nz + 2);
         cudaMemsetAsync(st.u, 0, b1, s);
         cudaMemsetAsync(st.v, 0, b1, s);
@@ -361,7 +402,7 @@ int monitor_t(const DevState &st, cudaStream_t s) {
     }
     k_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.multiphase ? gs<S>(st) : nullptr, fld<FT>(st.phi), st.walls,
                                                  fld<FT>(st.cnx), fld<FT>(st.cny), fld<FT>(st.cnz), fld<FT>(st.cnorm),
-                                                 fld<FT>(st.curv), st.u, st.v, st.w, st.rho, st.mon, st.L,
+                                                 fld<FT>(st.curv), st.u, st.v, st.w, st.rho, st.mon, st.L, pdf_at(st),
                                                  st.P, st.multiphase, 1, st.ref, st.scale);
     return 1;
 }
@@ -387,7 +428,7 @@ int saturation(const DevState &st, cudaStream_t s) {
 template <class S>
 int init_t(const DevState &st, bool convec, cudaStream_t s) {
     const Layout &L = st.L;
-    if (st.list) {
+    if (st.list && !st.mplist) {
         const int64_t n = 19 * st.lstride;
         k_list_init<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.scale);
         const size_t b1 = sizeof(double) * (size_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
@@ -402,14 +443,20 @@ int init_t(const DevState &st, bool convec, cudaStream_t s) {
     S *g = st.multiphase ? gs<S>(st) : nullptr;
     using FT = typename Store<S>::R;
     k_init_eq<S><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(fs<S>(st), g, fld<FT>(st.phi), st.u, st.v, st.w, st.rho, L,
-                                                              st.multiphase, st.ref, st.scale);
+                                                              pdf_at(st), st.multiphase, st.ref, st.scale);
+    int n = 1;
+    if (st.mplist && st.nlink > 0) {
+        k_mp_init_links<S><<<(unsigned)((st.nlink + 255) / 256), 256, 0, s>>>(fs<S>(st), g, fld<FT>(st.phi), st.lstride,
+                                                                              st.link, st.nlink, L);
+        ++n;
+    }
     if (convec) {
         const int64_t np = (int64_t)(L.nx + 2) * (L.ny + 2);
         k_init_convec<S><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(fs<S>(st), g, fld<FT>(st.phi), st.fconv, st.gconv, st.phiconv,
-                                                                      L, st.multiphase, st.ref, st.scale);
-        return 2;
+                                                                      L, pdf_at(st), st.multiphase, st.ref, st.scale);
+        ++n;
     }
-    return 1;
+    return n;
 }
 
 int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
@@ -424,6 +471,15 @@ int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
 template <class S>
 int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
+    if (st.mplist) {
+        S *A = sp == 0 ? fs<S>(st) : gs<S>(st);
+        const int64_t n = st.nfl + st.nlink;
+        const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        k_list_in<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.cell1, st.nfl, st.link, st.nlink,
+                                                                 st.stage, st.scale);
+        k_mp_planes_in<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage);
+        return 2;
+    }
     if (st.list) {
         const int64_t n = st.nfl + st.nlink;
         k_list_in<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, q, st.cell1, st.nfl, st.link,
@@ -439,6 +495,19 @@ int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
 template <class S>
 int convert_out_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
+    if (st.mplist) {
+        // fluid nodes, link slots, periodic ghosts as their images, boundary-plane slots; the
+        // cells that no update reads keep the rest weight
+        const S *A = sp == 0 ? fs<S>(st) : gs<S>(st);
+        const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        const int64_t n = st.nfl + st.nlink;
+        k_list_plane_fill<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(st.stage, n1, WEQ(q));
+        k_list_out<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.cell1, st.nfl, st.link, st.nlink,
+                                                                  st.stage, st.scale);
+        k_list_ghosts<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(st.stage, L, st.P.iper, st.P.jper, st.P.kper);
+        k_mp_planes_out<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage);
+        return 4;
+    }
     if (st.list) {
         const int64_t nb1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
         const int64_t n = st.nfl + st.nlink;
@@ -610,10 +679,25 @@ int change_inlet_phase(const DevState &st, int cmd, int kmax, cudaStream_t s) {
     const Layout &L = st.L;
     const int64_t n = (int64_t)19 * (L.nx + 2) * (L.ny + 2) * (kmax + 1);
     const unsigned nb = (unsigned)((n + 255) / 256);
-    if (mp_fp32(st)) k_change_inlet_phase<float><<<nb, 256, 0, s>>>(fs<float>(st), gs<float>(st), L, kmax, cmd == 1);
-    else if (st.prec == MFLBM_FF) k_change_inlet_phase<ffs><<<nb, 256, 0, s>>>(fs<ffs>(st), gs<ffs>(st), L, kmax, cmd == 1);
-    else k_change_inlet_phase<double><<<nb, 256, 0, s>>>(fs<double>(st), gs<double>(st), L, kmax, cmd == 1);
-    return 1;
+    const PdfAt pa = pdf_at(st);
+    const unsigned nl = (unsigned)((st.nlink + 255) / 256);
+    const bool links = st.mplist && st.nlink > 0;
+    if (mp_fp32(st)) {
+        k_change_inlet_phase<float><<<nb, 256, 0, s>>>(fs<float>(st), gs<float>(st), L, pa, kmax, cmd == 1);
+        if (links) k_change_inlet_links<float><<<nl, 256, 0, s>>>(fs<float>(st), gs<float>(st), st.lstride, st.link,
+                                                                  st.nlink, L, kmax, cmd == 1);
+        return links ? 2 : 1;
+    }
+    if (st.prec == MFLBM_FF) {
+        k_change_inlet_phase<ffs><<<nb, 256, 0, s>>>(fs<ffs>(st), gs<ffs>(st), L, pa, kmax, cmd == 1);
+        if (links) k_change_inlet_links<ffs><<<nl, 256, 0, s>>>(fs<ffs>(st), gs<ffs>(st), st.lstride, st.link, st.nlink,
+                                                                L, kmax, cmd == 1);
+        return links ? 2 : 1;
+    }
+    if (links) k_change_inlet_links<double><<<nl, 256, 0, s>>>(fs<double>(st), gs<double>(st), st.lstride, st.link,
+                                                               st.nlink, L, kmax, cmd == 1);
+    k_change_inlet_phase<double><<<nb, 256, 0, s>>>(fs<double>(st), gs<double>(st), L, pa, kmax, cmd == 1);
+    return links ? 2 : 1;
 }
 
 const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,

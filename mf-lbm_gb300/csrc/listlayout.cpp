@@ -85,4 +85,104 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
     return true;
 }
 
+bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jper, int kper,
+                          const std::vector<int> &planes, MpListLayout &out, std::string &why) {
+    const int64_t h2x = nx + 4, h2xy = (int64_t)(nx + 4) * (ny + 4);
+    const int64_t h1x = nx + 2, h1xy = (int64_t)(nx + 2) * (ny + 2);
+    const int64_t n1 = h1xy * (nz + 2);
+    if (n1 >= ((int64_t)1 << 31) - 64) { why = "lattice too large for 32-bit slot maps"; return false; }
+    auto wall = [&](int i, int j, int k) { return walls_h2[(i + 1) + h2x * (j + 1) + h2xy * (k + 1)]; };
+    auto h1 = [&](int i, int j, int k) { return (int64_t)i + h1x * j + h1xy * k; };
+    out = MpListLayout();
+    out.map.assign((size_t)n1, -1);
+    out.slice.assign((size_t)nz + 1, 0);
+    int64_t nf = 0;
+    for (int k = 1; k <= nz; ++k) {
+        out.slice[k - 1] = (int32_t)nf;
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (wall(i, j, k) == 0) {
+                    out.map[(size_t)h1(i, j, k)] = (int32_t)nf++;
+                    out.cell1.push_back((int32_t)h1(i, j, k));
+                }
+    }
+    out.slice[nz] = (int32_t)nf;
+    out.nf = nf;
+    if (nf == 0) { why = "no fluid nodes"; return false; }
+    // the periodic image the halo exchange copies into a ghost cell (Mpi.F90 for one rank:
+    // y faces over i in [1, nx], k in [1, nz]; z faces over i in [1, nx], j in [1, ny]; the
+    // x-aligned edges when y and z are both periodic); false when the cell is not such a ghost
+    auto image = [&](int i, int j, int k, int &ii, int &jj, int &kk) {
+        if (i < 1 || i > nx) return false;
+        const bool gy = j < 1 || j > ny, gz = k < 1 || k > nz;
+        if (!gy && !gz) return false;
+        if (gy && !jper) return false;
+        if (gz && !kper) return false;
+        ii = i;
+        jj = gy ? (j < 1 ? j + ny : j - ny) : j;
+        kk = gz ? (k < 1 ? k + nz : k - nz) : k;
+        return true;
+    };
+    // private slots of the boundary planes
+    int64_t next = nf;
+    std::vector<char> inplane((size_t)nz + 2, 0);
+    for (int k : planes)
+        if (k >= 0 && k <= nz + 1) inplane[(size_t)k] = 1;
+    for (int k = 0; k <= nz + 1; ++k) {
+        if (!inplane[(size_t)k]) continue;
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i) {
+                int ii, jj, kk;
+                if (out.map[(size_t)h1(i, j, k)] >= 0 || image(i, j, k, ii, jj, kk)) continue;
+                out.map[(size_t)h1(i, j, k)] = (int32_t)next++;
+            }
+    }
+    out.nplane = next - nf;
+    out.spare = next++;
+    // images of the periodic ghosts, after every owned slot is known
+    for (int k = 0; k <= nz + 1; ++k)
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i) {
+                int ii, jj, kk;
+                if (!image(i, j, k, ii, jj, kk)) continue;
+                const int32_t m = out.map[(size_t)h1(ii, jj, kk)];
+                if (m >= 0) out.map[(size_t)h1(i, j, k)] = -m - 2;
+            }
+    const int64_t base = next;
+    // neighbour table and the link slots of solid cells outside the boundary planes
+    std::array<int64_t, 19> cnt{};
+    out.nb.assign((size_t)18 * nf, 0);
+    for (int64_t x = 0; x < nf; ++x) {
+        const int64_t c = out.cell1[(size_t)x];
+        const int i = (int)(c % h1x), j = (int)((c / h1x) % (ny + 2)), k = (int)(c / h1xy);
+        for (int d = 1; d <= 18; ++d) {
+            int ci = i + EX(d), cj = j + EY(d), ck = k + EZ(d);
+            int ii, jj, kk;
+            if (image(ci, cj, ck, ii, jj, kk)) { ci = ii; cj = jj; ck = kk; }
+            if (ci < 0 || ci > nx + 1 || cj < 0 || cj > ny + 1 || ck < 0 || ck > nz + 1) {
+                why = "a neighbour outside the halo-1 box";
+                return false;
+            }
+            const int32_t m = out.map[(size_t)h1(ci, cj, ck)];
+            int64_t slot;
+            if (m >= 0) {
+                slot = m;
+            } else {
+                const int qa = OPP(d);   // the solid cell's slot opp(d), in array opp(d)
+                slot = base + cnt[qa]++;
+                out.link.push_back(qa);
+                out.link.push_back((int32_t)slot);
+                out.link.push_back((int32_t)h1(ci, cj, ck));
+            }
+            out.nb[(size_t)(d - 1) * nf + x] = (int32_t)slot;
+        }
+    }
+    int64_t maxl = 0, tot = 0;
+    for (int q = 1; q <= 18; ++q) { maxl = std::max(maxl, cnt[q]); tot += cnt[q]; }
+    out.nlink = tot;
+    out.stride = (base + maxl + 31) / 32 * 32;
+    if (out.stride >= ((int64_t)1 << 31)) { why = "direction array exceeds 2^31 elements"; return false; }
+    return true;
+}
+
 }  // namespace mflbm

@@ -39,4 +39,30 @@ struct ListLayout {
 bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper, int jper, int kper, ListLayout &out,
                        std::string &why);
 
+// The multiphase fluid-list layout (f and g each as 19 direction arrays of `stride` slots):
+//   [0, nf)                     fluid nodes, in cell order (k, j, i)
+//   [nf, nf + nplane)           private slots of the boundary planes: every solid or ghost
+//                               cell of the planes the inlet, outlet and porous-plate
+//                               conditions read or write (k = 0, 1, 2, nz-1, nz, nz+1 when z
+//                               is open; z_pp - 1 .. z_pp + 1 for a porous plate), one slot
+//                               per cell, the same index in every direction array
+//   nf + nplane                 a spare slot for cells that have none (never read for a value)
+//   [nf + nplane + 1, ...)      one slot per bounce-back link into a solid cell outside the
+//                               boundary planes, in the array that holds the solid cell's slot
+// nb[d][x] is the slot of x + e_d, resolved as the dense layout reads it: a neighbour in a
+// periodic face, edge or corner that the reference's halo exchange fills is its periodic
+// image; a cell of a boundary plane is its own slot (fluid index or private slot); any other
+// solid cell is a link slot.  map[c] (every cell of the halo-1 box) is the slot a boundary
+// condition addresses: >= 0 a slot the cell owns, <= -2 the image's slot -map-2 (a periodic
+// ghost), -1 none.  The update is the dense layout's slot for slot, so every fluid and
+// boundary-plane value is bit-identical to it.
+struct MpListLayout : ListLayout {
+    std::vector<int32_t> map;
+    int64_t nplane = 0;
+    int64_t spare = 0;
+};
+
+bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jper, int kper,
+                          const std::vector<int> &planes, MpListLayout &out, std::string &why);
+
 }  // namespace mflbm

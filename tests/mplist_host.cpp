@@ -1,0 +1,70 @@
+// mplist_host.cpp -- the multiphase fluid-list layout builder (mf-lbm_gb300/csrc/listlayout.cpp)
+// built for the host, with checks of every index it hands to the device: neighbour slots and
+// map entries inside the direction arrays, one slot per (solid cell, array) for the links,
+// boundary-plane cells all resolved to a slot, and the neighbour of a fluid node in a
+// boundary plane equal to the slot a boundary condition addresses for that cell.
+#include <cstdint>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../mf-lbm_gb300/csrc/listlayout.cpp"
+
+extern "C" {
+
+// Returns the number of failed checks, or -1 when the layout cannot be built.
+int64_t mph_check(const int8_t *walls, int nx, int ny, int nz, int jper, int kper, int open_z, int z_pp, int64_t *nf,
+                  int64_t *nplane, int64_t *nlink, int64_t *stride) {
+    std::vector<int> planes;
+    if (open_z)
+        for (int k : {0, 1, 2, nz - 1, nz, nz + 1}) planes.push_back(k);
+    if (z_pp > 0)
+        for (int dz = -1; dz <= 1; ++dz) planes.push_back(z_pp + dz);
+    mflbm::MpListLayout ml;
+    std::string why;
+    if (!mflbm::build_mp_list_layout(walls, nx, ny, nz, jper, kper, planes, ml, why)) return -1;
+    *nf = ml.nf;
+    *nplane = ml.nplane;
+    *nlink = ml.nlink;
+    *stride = ml.stride;
+    int64_t bad = 0;
+    const int64_t h1x = nx + 2, h1xy = (int64_t)(nx + 2) * (ny + 2);
+    auto resolve = [&](int64_t m) -> int64_t { return m >= 0 ? m : (m <= -2 ? -m - 2 : -1); };
+    for (size_t t = 0; t < ml.nb.size(); ++t)
+        if (ml.nb[t] < 0 || ml.nb[t] >= ml.stride) ++bad;
+    for (int32_t m : ml.map) {
+        const int64_t r = resolve(m);
+        if (m != -1 && (r < 0 || r >= ml.spare)) ++bad;
+    }
+    if (ml.spare >= ml.stride) ++bad;
+    std::set<std::pair<int, int32_t>> seen;
+    for (int64_t l = 0; l < ml.nlink; ++l) {
+        const int q = ml.link[3 * l];
+        const int32_t slot = ml.link[3 * l + 1];
+        if (q < 1 || q > 18 || slot <= ml.spare || slot >= ml.stride) ++bad;
+        if (!seen.insert({q, slot}).second) ++bad;
+    }
+    for (int k : planes) {
+        if (k < 0 || k > nz + 1) continue;
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i)
+                if (resolve(ml.map[(size_t)(i + h1x * j + h1xy * k)]) < 0) ++bad;
+    }
+    // a fluid node's neighbour inside a boundary plane: the table's slot is the map's slot
+    std::vector<char> inplane((size_t)nz + 2, 0);
+    for (int k : planes)
+        if (k >= 0 && k <= nz + 1) inplane[(size_t)k] = 1;
+    for (int64_t x = 0; x < ml.nf; ++x) {
+        const int64_t c = ml.cell1[(size_t)x];
+        const int i = (int)(c % h1x), j = (int)((c / h1x) % (ny + 2)), k = (int)(c / h1xy);
+        if (resolve(ml.map[(size_t)c]) != x) ++bad;
+        for (int d = 1; d <= 18; ++d) {
+            const int ci = i + mflbm::EX(d), cj = j + mflbm::EY(d), ck = k + mflbm::EZ(d);
+            if (!inplane[(size_t)ck]) continue;
+            const int64_t m = resolve(ml.map[(size_t)(ci + h1x * cj + h1xy * ck)]);
+            if (m != ml.nb[(size_t)(d - 1) * ml.nf + x]) ++bad;
+        }
+    }
+    return bad;
+}
+}
