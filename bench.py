@@ -91,7 +91,7 @@ def parse():
                     help="skip the time-to-steady permeability study (singlephase workload only)")
     ap.add_argument("--conv-tol", type=float, default=1e-7)
     ap.add_argument("--layout", type=int, default=0, choices=[0, 1, 2],
-                    help="singlephase storage: 0 auto (fluid list when possible), 1 dense, 2 fluid list")
+                    help="PDF storage: 0 auto, 1 dense planes, 2 fluid list (fluid nodes + link slots)")
     return ap.parse_args()
 
 
@@ -115,10 +115,10 @@ def workload(args, device=0):
     else:
         case = workloads.packing_permeability(n=args.n, porosity=args.porosity, precision=args.precision,
                                               device=device)
-        case["params"].layout = args.layout
         desc = (f"singlephase permeability, {args.n}^3 sphere packing porosity {args.porosity} "
                 "(seeded lognormal radii mean 8 sd 2, isolated pores removed), periodic xyz, F_z=1e-6, tau=1, "
                 "MRT preset 1")
+    case["params"].layout = args.layout
     return case, desc
 
 

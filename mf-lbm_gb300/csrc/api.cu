@@ -151,6 +151,11 @@ int validate(const mflbm_params *p, std::string &err) {
     return MFLBM_OK;
 }
 
+// A new device buffer, zero-filled.  The fill completes before the call returns: the
+// context's stream is non-blocking, so a zero fill still queued on it is not ordered
+// against the plain cudaMemcpy that set_geometry then uses to fill the same buffer (a table
+// zeroed after its upload sent every thread of the gradient kernels to one cell outside the
+// box).  Allocation is not on the time-stepping path.
 int dalloc_bytes(mflbm_ctx *c, void **ptr, size_t bytes) {
     void *p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes);
@@ -158,17 +163,16 @@ int dalloc_bytes(mflbm_ctx *c, void **ptr, size_t bytes) {
     c->allocs.push_back(p);
     e = cudaMemsetAsync(p, 0, bytes, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync");
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
     *ptr = p;
     return MFLBM_OK;
 }
 
 template <class T> int dalloc(mflbm_ctx *c, T **ptr, int64_t count) {
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, (size_t)count * sizeof(T));
-    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
-    c->allocs.push_back(p);
-    e = cudaMemsetAsync(p, 0, (size_t)count * sizeof(T), c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemsetAsync");
+    const int r = dalloc_bytes(c, &p, (size_t)count * sizeof(T));
+    if (r) return r;
     *ptr = reinterpret_cast<T *>(p);
     return MFLBM_OK;
 }
@@ -207,6 +211,8 @@ int alloc_dense(mflbm_ctx *c) {
     c->st.list = 0;
     c->st.mplist = 0;
     c->st.pmap = nullptr;
+    c->st.pwrap = nullptr;
+    c->st.nwrap = 0;
     c->st.tma = 0;
     return MFLBM_OK;
 }
@@ -589,14 +595,17 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     // multiphase fluid list (MpListLayout in listlayout.h): f and g hold the fluid nodes, the
     // boundary planes' private slots and the link slots; phi and the gradient fields stay dense
     if (p.multiphase && p.layout == MFLBM_LAYOUT_LIST) {
-        std::vector<int> planes;
+        std::vector<int> planes, ghost_planes;
         if (c->open_z)
             for (int k : {0, 1, 2, p.nz - 1, p.nz, p.nz + 1}) planes.push_back(k);
-        if (p.porous_plate_cmd != 0)
-            for (int dz = -1; dz <= 1; ++dz) planes.push_back(p.z_porous_plate + dz);
+        if (p.porous_plate_cmd != 0 && p.z_porous_plate >= 1 && p.z_porous_plate <= p.nz)
+            for (int dz = -1; dz <= 1; ++dz) {
+                planes.push_back(p.z_porous_plate + dz);
+                ghost_planes.push_back(p.z_porous_plate + dz);
+            }
         MpListLayout ml;
         std::string why;
-        if (!build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, planes, ml, why))
+        if (!build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, planes, ghost_planes, ml, why))
             return fail(c, MFLBM_EINVAL, "multiphase fluid-list layout: " + why);
         for (void *b : c->list_bufs) dfree(c, b);
         c->list_bufs.clear();
@@ -611,6 +620,12 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
         c->list_bufs.push_back(link);
         if ((r = dalloc(c, &map, (int64_t)ml.map.size()))) return r;
         c->list_bufs.push_back(map);
+        int32_t *wrap = nullptr;
+        if (ml.nwrap > 0) {
+            if ((r = dalloc(c, &wrap, 4 * ml.nwrap))) return r;
+            c->list_bufs.push_back(wrap);
+            CK(c, cudaMemcpy(wrap, ml.wrap.data(), sizeof(int32_t) * ml.wrap.size(), cudaMemcpyHostToDevice));
+        }
         CK(c, cudaMemcpy(nb, ml.nb.data(), sizeof(int32_t) * ml.nb.size(), cudaMemcpyHostToDevice));
         CK(c, cudaMemcpy(cell1, ml.cell1.data(), sizeof(int32_t) * ml.cell1.size(), cudaMemcpyHostToDevice));
         if (ml.nlink) CK(c, cudaMemcpy(link, ml.link.data(), sizeof(int32_t) * ml.link.size(), cudaMemcpyHostToDevice));
@@ -630,6 +645,8 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
         st.lseg = nullptr;
         st.pmap = map;
         st.pspare = ml.spare;
+        st.pwrap = wrap;
+        st.nwrap = ml.nwrap;
     } else if (p.multiphase && (!c->pdf || c->st.list)) {
         int r = alloc_dense(c);
         if (r) return r;

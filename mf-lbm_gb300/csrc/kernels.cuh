@@ -2118,6 +2118,31 @@ __global__ void k_mp_init_links(S *__restrict__ f, S *__restrict__ g, const type
     Store<S>::st64(g, (int64_t)q * stride + slot, b, WREST(q), 1.0f);
 }
 
+// the y-face exchange of the porous-plate planes' private ghosts (the dense k_wrap_faces for
+// dim 1 over those planes): one thread per (i, k) entry {ghost 0, image ny, ghost ny+1,
+// image 1} and species; pull after an even step (ghosts from images), push after an odd
+// step (images from the ghosts the odd step wrote)
+template <class S>
+__global__ void k_mp_wrap_ghosts(S *__restrict__ f, S *__restrict__ g, const int64_t stride,
+                                 const int32_t *__restrict__ wrap, const int64_t nwrap, int pull) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nwrap) return;
+    S *A = t < nwrap ? f : g;
+    const int64_t e = t < nwrap ? t : t - nwrap;
+    const int64_t g0 = wrap[4 * e], in_n = wrap[4 * e + 1], g1 = wrap[4 * e + 2], in_1 = wrap[4 * e + 3];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        const int64_t qp = (int64_t)c_plus[1][m] * stride, qm = (int64_t)c_minus[1][m] * stride;
+        if (pull) {
+            A[qp + g0] = A[qp + in_n];
+            A[qm + g1] = A[qm + in_1];
+        } else {
+            A[qm + in_1] = A[qm + g1];
+            A[qp + in_n] = A[qp + g0];
+        }
+    }
+}
+
 static __global__ void k_list_ghosts(double *__restrict__ stage, const Layout L, int px, int py, int pz) {
     const int64_t n = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -58,10 +58,14 @@ struct DevState {
     // tensor map of the list arrays for the TMA even step: a 2-D tensor of 19 rows (one per
     // direction array, row pitch lstride elements) by nfl fluid nodes; tma = 1 when valid
     // multiphase fluid list (mplist = 1; list = 1 as well): the boundary-condition slot map
-    // of every halo-1 cell and the spare slot (listlayout.h, MpListLayout)
+    // of every halo-1 cell and the spare slot; the exchange of the porous-plate planes'
+    // private y ghosts, nwrap x {ghost 0, image ny, ghost ny+1, image 1} (listlayout.h,
+    // MpListLayout)
     int mplist;
     const int32_t *pmap;
     int64_t pspare;
+    const int32_t *pwrap;
+    int64_t nwrap;
     CUtensorMap tmap;
     int tma;
     int32_t *err;          // device word set when a bounded wait of a sweep kernel gave up

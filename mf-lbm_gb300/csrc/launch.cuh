@@ -235,6 +235,18 @@ int wrap(const DevState &st, bool pull, cudaStream_t s) {
         case MFLBM_FF: n_launch = wrap_t<ffs>(st, pull, s); break;
         default: n_launch = wrap_t<double>(st, pull, s); break;
     }
+    if (st.mplist && st.nwrap > 0) {
+        const unsigned nb = (unsigned)((2 * st.nwrap + 255) / 256);
+        const int pl = pull ? 1 : 0;
+        // plain copies: moved as 4- or 8-byte words whatever the storage type
+        if (mp_fp32(st))
+            k_mp_wrap_ghosts<uint32_t><<<nb, 256, 0, s>>>(fs<uint32_t>(st), gs<uint32_t>(st), st.lstride, st.pwrap,
+                                                          st.nwrap, pl);
+        else
+            k_mp_wrap_ghosts<uint64_t><<<nb, 256, 0, s>>>(fs<uint64_t>(st), gs<uint64_t>(st), st.lstride, st.pwrap,
+                                                          st.nwrap, pl);
+        ++n_launch;
+    }
     if (st.multiphase && (st.P.jper || st.P.kper)) {
         const Layout &L = st.L;
         const int64_t n = (st.P.kper ? (int64_t)4 * L.nx * L.ny : 0) + (st.P.jper ? (int64_t)4 * L.nx * L.nz : 0) +

@@ -86,7 +86,8 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
 }
 
 bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jper, int kper,
-                          const std::vector<int> &planes, MpListLayout &out, std::string &why) {
+                          const std::vector<int> &planes, const std::vector<int> &ghost_planes, MpListLayout &out,
+                          std::string &why) {
     const int64_t h2x = nx + 4, h2xy = (int64_t)(nx + 4) * (ny + 4);
     const int64_t h1x = nx + 2, h1xy = (int64_t)(nx + 2) * (ny + 2);
     const int64_t n1 = h1xy * (nz + 2);
@@ -123,17 +124,27 @@ bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jp
         kk = gz ? (k < 1 ? k + nz : k - nz) : k;
         return true;
     };
-    // private slots of the boundary planes
+    // private slots of the boundary planes (and of the y ghosts of the ghost planes)
     int64_t next = nf;
-    std::vector<char> inplane((size_t)nz + 2, 0);
+    std::vector<char> inplane((size_t)nz + 2, 0), ownghost((size_t)nz + 2, 0);
     for (int k : planes)
         if (k >= 0 && k <= nz + 1) inplane[(size_t)k] = 1;
+    for (int k : ghost_planes) {
+        if (!jper) continue;
+        if (k < 1 || k > nz) { why = "porous-plate planes outside [1, nz]"; return false; }
+        inplane[(size_t)k] = 1;
+        ownghost[(size_t)k] = 1;
+    }
+    auto private_ghost = [&](int i, int j, int k) {
+        return ownghost[(size_t)k] && i >= 1 && i <= nx && (j == 0 || j == ny + 1);
+    };
     for (int k = 0; k <= nz + 1; ++k) {
         if (!inplane[(size_t)k]) continue;
         for (int j = 0; j <= ny + 1; ++j)
             for (int i = 0; i <= nx + 1; ++i) {
                 int ii, jj, kk;
-                if (out.map[(size_t)h1(i, j, k)] >= 0 || image(i, j, k, ii, jj, kk)) continue;
+                if (out.map[(size_t)h1(i, j, k)] >= 0) continue;
+                if (image(i, j, k, ii, jj, kk) && !private_ghost(i, j, k)) continue;
                 out.map[(size_t)h1(i, j, k)] = (int32_t)next++;
             }
     }
@@ -144,10 +155,22 @@ bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jp
         for (int j = 0; j <= ny + 1; ++j)
             for (int i = 0; i <= nx + 1; ++i) {
                 int ii, jj, kk;
-                if (!image(i, j, k, ii, jj, kk)) continue;
+                if (private_ghost(i, j, k) || !image(i, j, k, ii, jj, kk)) continue;
                 const int32_t m = out.map[(size_t)h1(ii, jj, kk)];
                 if (m >= 0) out.map[(size_t)h1(i, j, k)] = -m - 2;
             }
+    // the exchange of the private y ghosts: {ghost 0, image ny, ghost ny + 1, image 1}
+    for (int k = 1; k <= nz; ++k) {
+        if (!ownghost[(size_t)k]) continue;
+        for (int i = 1; i <= nx; ++i) {
+            const int32_t s[4] = {out.map[(size_t)h1(i, 0, k)], out.map[(size_t)h1(i, ny, k)],
+                                  out.map[(size_t)h1(i, ny + 1, k)], out.map[(size_t)h1(i, 1, k)]};
+            for (int32_t v : s)
+                if (v < 0) { why = "a porous-plate plane cell without a slot"; return false; }
+            out.wrap.insert(out.wrap.end(), s, s + 4);
+            ++out.nwrap;
+        }
+    }
     const int64_t base = next;
     // neighbour table and the link slots of solid cells outside the boundary planes
     std::array<int64_t, 19> cnt{};
@@ -158,11 +181,11 @@ bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jp
         for (int d = 1; d <= 18; ++d) {
             int ci = i + EX(d), cj = j + EY(d), ck = k + EZ(d);
             int ii, jj, kk;
-            if (image(ci, cj, ck, ii, jj, kk)) { ci = ii; cj = jj; ck = kk; }
             if (ci < 0 || ci > nx + 1 || cj < 0 || cj > ny + 1 || ck < 0 || ck > nz + 1) {
                 why = "a neighbour outside the halo-1 box";
                 return false;
             }
+            if (!private_ghost(ci, cj, ck) && image(ci, cj, ck, ii, jj, kk)) { ci = ii; cj = jj; ck = kk; }
             const int32_t m = out.map[(size_t)h1(ci, cj, ck)];
             int64_t slot;
             if (m >= 0) {

@@ -46,6 +46,8 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
 //                               conditions read or write (k = 0, 1, 2, nz-1, nz, nz+1 when z
 //                               is open; z_pp - 1 .. z_pp + 1 for a porous plate), one slot
 //                               per cell, the same index in every direction array
+//                               (for the porous plate's planes with y periodic, the y ghosts
+//                               too: see `wrap` below)
 //   nf + nplane                 a spare slot for cells that have none (never read for a value)
 //   [nf + nplane + 1, ...)      one slot per bounce-back link into a solid cell outside the
 //                               boundary planes, in the array that holds the solid cell's slot
@@ -56,13 +58,24 @@ bool build_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int iper,
 // condition addresses: >= 0 a slot the cell owns, <= -2 the image's slot -map-2 (a periodic
 // ghost), -1 none.  The update is the dense layout's slot for slot, so every fluid and
 // boundary-plane value is bit-identical to it.
+//
+// The porous plate rewrites interior slots of its planes after the halo exchange, so the
+// exchanged ghost copies of those slots keep the values from before the plate (the
+// reference exchanges, then applies the plate).  A ghost that aliased its image would see
+// the plate's value instead; the y ghosts of the `ghost_planes` therefore own private slots
+// and `wrap` lists, per (i, k) of those planes, the slots {ghost j = 0, image j = ny,
+// ghost j = ny + 1, image j = 1} that the device exchanges like the dense y-face exchange
+// (the five directions that cross the face; pull after an even step, push after an odd one).
 struct MpListLayout : ListLayout {
     std::vector<int32_t> map;
+    std::vector<int32_t> wrap;   // [nwrap][4]
     int64_t nplane = 0;
     int64_t spare = 0;
+    int64_t nwrap = 0;
 };
 
 bool build_mp_list_layout(const int8_t *walls_h2, int nx, int ny, int nz, int jper, int kper,
-                          const std::vector<int> &planes, MpListLayout &out, std::string &why);
+                          const std::vector<int> &planes, const std::vector<int> &ghost_planes, MpListLayout &out,
+                          std::string &why);
 
 }  // namespace mflbm

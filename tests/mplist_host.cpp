@@ -15,14 +15,17 @@ extern "C" {
 // Returns the number of failed checks, or -1 when the layout cannot be built.
 int64_t mph_check(const int8_t *walls, int nx, int ny, int nz, int jper, int kper, int open_z, int z_pp, int64_t *nf,
                   int64_t *nplane, int64_t *nlink, int64_t *stride) {
-    std::vector<int> planes;
+    std::vector<int> planes, ghost_planes;
     if (open_z)
         for (int k : {0, 1, 2, nz - 1, nz, nz + 1}) planes.push_back(k);
     if (z_pp > 0)
-        for (int dz = -1; dz <= 1; ++dz) planes.push_back(z_pp + dz);
+        for (int dz = -1; dz <= 1; ++dz) {
+            planes.push_back(z_pp + dz);
+            ghost_planes.push_back(z_pp + dz);
+        }
     mflbm::MpListLayout ml;
     std::string why;
-    if (!mflbm::build_mp_list_layout(walls, nx, ny, nz, jper, kper, planes, ml, why)) return -1;
+    if (!mflbm::build_mp_list_layout(walls, nx, ny, nz, jper, kper, planes, ghost_planes, ml, why)) return -1;
     *nf = ml.nf;
     *nplane = ml.nplane;
     *nlink = ml.nlink;
@@ -50,6 +53,13 @@ int64_t mph_check(const int8_t *walls, int nx, int ny, int nz, int jper, int kpe
             for (int i = 0; i <= nx + 1; ++i)
                 if (resolve(ml.map[(size_t)(i + h1x * j + h1xy * k)]) < 0) ++bad;
     }
+    // the porous-plate ghost exchange: private ghost slots, images inside the owned range
+    for (int64_t w = 0; w < ml.nwrap; ++w) {
+        const int32_t *e = &ml.wrap[(size_t)(4 * w)];
+        if (e[0] < ml.nf || e[0] >= ml.spare || e[2] < ml.nf || e[2] >= ml.spare) ++bad;
+        if (e[1] < 0 || e[1] >= ml.spare || e[3] < 0 || e[3] >= ml.spare) ++bad;
+    }
+    if (jper && z_pp > 0 && ml.nwrap != 3 * (int64_t)nx) ++bad;
     // a fluid node's neighbour inside a boundary plane: the table's slot is the map's slot
     std::vector<char> inplane((size_t)nz + 2, 0);
     for (int k : planes)

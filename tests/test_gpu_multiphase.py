@@ -192,3 +192,25 @@ def test_unordered_neighbour_lists_use_record_kernels(strict):
             assert np.abs(a[k] - b[k]).max() <= 1e-12, k
     gpu.close()
     orc.close()
+
+
+def test_gradient_tables_ready_in_every_context():
+    """Device tables filled right after allocation (the gradient cell lists, boundary
+    records, fluid-list tables) hold their uploaded contents in every new context: a zero
+    fill still queued on the context's stream once landed after the upload, emptied the
+    normals list and sent its threads outside the box.  Sixteen contexts from the same
+    deck give the same phase field and gradient fields, with the normals computed."""
+    case = mp_case(strict=0, **MP_CASES["ragged_sizes"])
+    ref = None
+    for _ in range(16):
+        with Solver(case["params"]) as gpu:
+            load_case(gpu, case)
+            phi = gpu.download_state()["phi"]
+            gr = gpu.get_gradient()
+        assert np.count_nonzero(gr["c_norm"]) > 100
+        if ref is None:
+            ref = (phi, gr)
+            continue
+        assert np.array_equal(phi, ref[0])
+        for k in gr:
+            assert np.array_equal(gr[k], ref[1][k]), k

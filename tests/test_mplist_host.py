@@ -2,7 +2,8 @@
 compiled for the host, and checks of every index it hands to the device (neighbour slots
 and slot-map entries inside the arrays, one link slot per solid cell and array, every
 boundary-plane cell resolved, a boundary-plane neighbour equal to the slot the boundary
-conditions address), for open and periodic z, periodic and walled y, and a porous plate."""
+conditions address, the porous-plate planes' private y ghosts and their exchange list),
+for open and periodic z, periodic and walled y, and a porous plate."""
 import ctypes as C
 import os
 import shutil
@@ -39,7 +40,8 @@ def lib():
     return L
 
 
-@pytest.mark.parametrize("jper,kper,open_z,zpp", [(1, 1, 0, 0), (0, 0, 1, 0), (1, 0, 1, 0), (0, 1, 0, 7), (1, 0, 1, 9)])
+@pytest.mark.parametrize("jper,kper,open_z,zpp", [(1, 1, 0, 0), (0, 0, 1, 0), (1, 0, 1, 0), (0, 1, 0, 7), (1, 0, 1, 9),
+                                                      (1, 1, 0, 5)])
 def test_multiphase_list_indices(lib, jper, kper, open_z, zpp):
     nx, ny, nz = 14, 12, 18
     p = make_params(multiphase=1, nx=nx, ny=ny, nz=nz, iper=0, jper=jper, kper=kper, wall_x_min=1, wall_x_max=1,
