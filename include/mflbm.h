@@ -81,7 +81,10 @@ extern "C" {
  * DENSE: one plane per direction over the halo-1 box, as the reference's arrays.
  * LIST:  only the fluid nodes plus one slot per solid bounce-back link, with an
  *        18-entry neighbour table; singlephase samples that are periodic or walled in
- *        every direction (no inlet/outlet).  Same update, same results.
+ *        every direction (no inlet/outlet), and multiphase runs with any boundary
+ *        conditions (the cells of the inlet, outlet and porous-plate planes keep their own
+ *        slots).  Same update, same results on every fluid node; downloads give the other
+ *        slots, which no update reads, the rest weight w_q.
  * AUTO:  LIST when the geometry allows it, else DENSE (decided by mflbm_set_geometry). */
 #define MFLBM_LAYOUT_AUTO  0
 #define MFLBM_LAYOUT_DENSE 1
@@ -153,7 +156,7 @@ int32_t mflbm_init_velocity(mflbm_ctx *ctx, const double *rho, const double *u, 
                             const double *w, int32_t rest_base);
 
 /* Storage layout in use: MFLBM_LAYOUT_DENSE or MFLBM_LAYOUT_LIST, or
- * MFLBM_LAYOUT_AUTO while a singlephase context has no geometry yet.
+ * MFLBM_LAYOUT_AUTO while a context has no geometry yet.
  * No counterpart in the reference. */
 int32_t mflbm_layout(const mflbm_ctx *ctx);
 

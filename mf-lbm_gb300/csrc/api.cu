@@ -438,10 +438,9 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     const int nsp = p.multiphase ? 2 : 1;
     int r = MFLBM_OK;
     (void)nsp;
-    // the singlephase storage layout is settled by mflbm_set_geometry; the other cases
-    // are dense from the start
-    if ((p.multiphase && p.layout != MFLBM_LAYOUT_LIST) || p.layout == MFLBM_LAYOUT_DENSE ||
-        (!p.multiphase && (p.inlet_bc != 0 || p.outlet_bc != 0))) {
+    // the storage layout is settled by mflbm_set_geometry unless it can only be dense
+    // (requested, or a singlephase deck with an inlet or outlet)
+    if (p.layout == MFLBM_LAYOUT_DENSE || (!p.multiphase && (p.inlet_bc != 0 || p.outlet_bc != 0))) {
         if ((r = alloc_dense(c))) goto fail_create;
     }
     if ((r = dalloc(c, &c->st.walls, n2(p)))) goto fail_create;
@@ -455,7 +454,7 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.err, 1))) goto fail_create;
     // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
     // phase field when that is larger
-    if ((!f64_storage(p) || !p.multiphase || p.layout == MFLBM_LAYOUT_LIST) &&
+    if ((!f64_storage(p) || !p.multiphase || p.layout != MFLBM_LAYOUT_DENSE) &&
         (r = dalloc(c, &c->st.stage, p.multiphase ? std::max(n1(p), n4(p)) : n1(p)))) goto fail_create;
     if (p.multiphase) {
         const size_t fe = (size_t)c->st.felt;
@@ -594,7 +593,8 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     }
     // multiphase fluid list (MpListLayout in listlayout.h): f and g hold the fluid nodes, the
     // boundary planes' private slots and the link slots; phi and the gradient fields stay dense
-    if (p.multiphase && p.layout == MFLBM_LAYOUT_LIST) {
+    bool mp_list = false;
+    if (p.multiphase && p.layout != MFLBM_LAYOUT_DENSE) {
         std::vector<int> planes, ghost_planes;
         if (c->open_z)
             for (int k : {0, 1, 2, p.nz - 1, p.nz, p.nz + 1}) planes.push_back(k);
@@ -605,49 +605,53 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
             }
         MpListLayout ml;
         std::string why;
-        if (!build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, planes, ghost_planes, ml, why))
+        mp_list = build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, planes, ghost_planes, ml, why);
+        if (!mp_list && p.layout == MFLBM_LAYOUT_LIST)
             return fail(c, MFLBM_EINVAL, "multiphase fluid-list layout: " + why);
-        for (void *b : c->list_bufs) dfree(c, b);
-        c->list_bufs.clear();
-        int r = alloc_pdf(c, (size_t)2 * 19 * ml.stride * c->elt);
-        if (r) return r;
-        int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *map = nullptr;
-        if ((r = dalloc(c, &nb, 18 * ml.nf))) return r;
-        c->list_bufs.push_back(nb);
-        if ((r = dalloc(c, &cell1, ml.nf))) return r;
-        c->list_bufs.push_back(cell1);
-        if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * ml.nlink)))) return r;
-        c->list_bufs.push_back(link);
-        if ((r = dalloc(c, &map, (int64_t)ml.map.size()))) return r;
-        c->list_bufs.push_back(map);
-        int32_t *wrap = nullptr;
-        if (ml.nwrap > 0) {
-            if ((r = dalloc(c, &wrap, 4 * ml.nwrap))) return r;
-            c->list_bufs.push_back(wrap);
-            CK(c, cudaMemcpy(wrap, ml.wrap.data(), sizeof(int32_t) * ml.wrap.size(), cudaMemcpyHostToDevice));
+        if (mp_list) {
+            for (void *b : c->list_bufs) dfree(c, b);
+            c->list_bufs.clear();
+            int r = alloc_pdf(c, (size_t)2 * 19 * ml.stride * c->elt);
+            if (r) return r;
+            int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *map = nullptr;
+            if ((r = dalloc(c, &nb, 18 * ml.nf))) return r;
+            c->list_bufs.push_back(nb);
+            if ((r = dalloc(c, &cell1, ml.nf))) return r;
+            c->list_bufs.push_back(cell1);
+            if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * ml.nlink)))) return r;
+            c->list_bufs.push_back(link);
+            if ((r = dalloc(c, &map, (int64_t)ml.map.size()))) return r;
+            c->list_bufs.push_back(map);
+            int32_t *wrap = nullptr;
+            if (ml.nwrap > 0) {
+                if ((r = dalloc(c, &wrap, 4 * ml.nwrap))) return r;
+                c->list_bufs.push_back(wrap);
+                CK(c, cudaMemcpy(wrap, ml.wrap.data(), sizeof(int32_t) * ml.wrap.size(), cudaMemcpyHostToDevice));
+            }
+            CK(c, cudaMemcpy(nb, ml.nb.data(), sizeof(int32_t) * ml.nb.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(cell1, ml.cell1.data(), sizeof(int32_t) * ml.cell1.size(), cudaMemcpyHostToDevice));
+            if (ml.nlink) CK(c, cudaMemcpy(link, ml.link.data(), sizeof(int32_t) * ml.link.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(map, ml.map.data(), sizeof(int32_t) * ml.map.size(), cudaMemcpyHostToDevice));
+            DevState &st = c->st;
+            st.list = 1;
+            st.mplist = 1;
+            st.tma = 0;
+            st.f = c->pdf;
+            st.g = (void *)((char *)c->pdf + (size_t)19 * ml.stride * c->elt);
+            st.lstride = ml.stride;
+            st.nb = nb;
+            st.cell1 = cell1;
+            st.link = link;
+            st.nlink = ml.nlink;
+            st.nfl = (int)ml.nf;
+            st.lseg = nullptr;
+            st.pmap = map;
+            st.pspare = ml.spare;
+            st.pwrap = wrap;
+            st.nwrap = ml.nwrap;
         }
-        CK(c, cudaMemcpy(nb, ml.nb.data(), sizeof(int32_t) * ml.nb.size(), cudaMemcpyHostToDevice));
-        CK(c, cudaMemcpy(cell1, ml.cell1.data(), sizeof(int32_t) * ml.cell1.size(), cudaMemcpyHostToDevice));
-        if (ml.nlink) CK(c, cudaMemcpy(link, ml.link.data(), sizeof(int32_t) * ml.link.size(), cudaMemcpyHostToDevice));
-        CK(c, cudaMemcpy(map, ml.map.data(), sizeof(int32_t) * ml.map.size(), cudaMemcpyHostToDevice));
-        DevState &st = c->st;
-        st.list = 1;
-        st.mplist = 1;
-        st.tma = 0;
-        st.f = c->pdf;
-        st.g = (void *)((char *)c->pdf + (size_t)19 * ml.stride * c->elt);
-        st.lstride = ml.stride;
-        st.nb = nb;
-        st.cell1 = cell1;
-        st.link = link;
-        st.nlink = ml.nlink;
-        st.nfl = (int)ml.nf;
-        st.lseg = nullptr;
-        st.pmap = map;
-        st.pspare = ml.spare;
-        st.pwrap = wrap;
-        st.nwrap = ml.nwrap;
-    } else if (p.multiphase && (!c->pdf || c->st.list)) {
+    }
+    if (p.multiphase && !mp_list && (!c->pdf || c->st.list)) {
         int r = alloc_dense(c);
         if (r) return r;
     }

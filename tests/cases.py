@@ -70,13 +70,13 @@ def smooth_phase(shape4, seed, kind="blob"):
 
 def mp_case(nx=14, ny=12, nz=16, per=(0, 1, 1), inlet=0, outlet=0, force=0.0, spheres=2, seed=3, theta_deg=45.0,
             mrt=2, nu1=1.0 / 6.0, nu2=1.0 / 6.0, gamma=0.01, beta=0.95, strict=1, uin=1e-3, rho_in=1.001,
-            plate=0, zplate=0, sa_inject=1.0, precision=0):
+            plate=0, zplate=0, sa_inject=1.0, precision=0, layout=1):
     _, jper, kper = per
     p = make_params(multiphase=1, nx=nx, ny=ny, nz=nz, iper=0, jper=jper, kper=kper, wall_x_min=1, wall_x_max=1,
                     wall_y_min=0 if jper else 1, wall_y_max=0 if jper else 1, wall_z_min=0, wall_z_max=0,
                     inlet_bc=inlet, outlet_bc=outlet, mrt=mrt, la_nu1=nu1, la_nu2=nu2, gamma=gamma, beta=beta,
                     sa_inject=sa_inject, force_z=force, uin_avg=uin, rho_in=rho_in, rho_out=1.0, strict_fp=strict,
-                    porous_plate_cmd=plate, z_porous_plate=zplate, precision=precision)
+                    porous_plate_cmd=plate, z_porous_plate=zplate, precision=precision, layout=layout)
     wg = random_spheres((nz, ny, nx), spheres, 1.5, 3.0, seed) if spheres else np.zeros((nz, ny, nx), np.int8)
     walls, pore, wchan = geometry.set_walls(p, wg)
     solid, fluid = geometry.preprocess(p, wchan, geometry.contact_angle_rad(theta_deg))
