@@ -223,17 +223,18 @@ def hbm_peak():
 
 
 def stored_traffic(prec, layout, multiphase, pore):
-    """DRAM bytes per launch of the collision sweep from the committed ncu capture
-    (profiles/sp_collide_traffic.json: bytes per fluid node x the fluid nodes here)."""
-    tf = os.path.join(ROOT, "profiles", "sp_collide_traffic.json")
-    if multiphase or not os.path.exists(tf):
+    """DRAM bytes per launch of the collision sweep from the committed ncu captures
+    (profiles/sp_collide_traffic.json, profiles/mp_collide_traffic.json: bytes per fluid
+    node x the fluid nodes here)."""
+    tf = os.path.join(ROOT, "profiles", "mp_collide_traffic.json" if multiphase else "sp_collide_traffic.json")
+    if not os.path.exists(tf):
         return None
     try:
         t = json.load(open(tf))
     except Exception:
         return None
-    # FP64 storage with the double-word collision moves the FP64 form's bytes
-    key = f"{DTYPE[0 if prec == 3 else prec]}_{layout}"
+    # singlephase FP64 storage with the double-word collision moves the FP64 form's bytes
+    key = f"{DTYPE[prec if multiphase or prec != 3 else 0]}_{layout}"
     return t[key] * pore if key in t else None
 
 
@@ -245,7 +246,7 @@ def roofline_of(prof, pore, prec, multiphase, layout, hbm, peak_src):
     achieved = pore * bpl / avg_s / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": stored_traffic(prec, layout, multiphase, pore), "traffic_source": "ncu capture "
-            "(profiles/sp_collide_traffic.json, bytes per fluid node x fluid nodes)", "bytes_per_lu": bpl,
+            f"(profiles/{'mp' if multiphase else 'sp'}_collide_traffic.json, bytes per fluid node x fluid nodes)", "bytes_per_lu": bpl,
             "peak_source": peak_src, "avg_launch_ms": avg_s * 1e3, "launches_timed": prof["collide_launches"]}
 
 

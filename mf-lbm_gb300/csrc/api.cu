@@ -143,8 +143,9 @@ int validate(const mflbm_params *p, std::string &err) {
     }
     if (p->precision < MFLBM_FP64 || p->precision > MFLBM_FF) { err = "unknown precision"; return MFLBM_EINVAL; }
     if (p->layout < MFLBM_LAYOUT_AUTO || p->layout > MFLBM_LAYOUT_LIST) { err = "unknown layout"; return MFLBM_EINVAL; }
-    if (p->layout == MFLBM_LAYOUT_LIST && !p->multiphase && (p->inlet_bc != 0 || p->outlet_bc != 0)) {
-        err = "the singlephase fluid-list layout has no inlet/outlet boundary conditions";
+    if (p->layout == MFLBM_LAYOUT_LIST && !p->multiphase && p->iper && p->kper == 0 && p->wall_z_min == 0 &&
+        p->wall_z_max == 0) {
+        err = "the singlephase fluid-list layout with an open z direction needs walls in x";
         return MFLBM_EINVAL;
     }
     if (p->la_nu1 <= 0.0) { err = "la_nu1 must be positive"; return MFLBM_EINVAL; }
@@ -438,9 +439,8 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     const int nsp = p.multiphase ? 2 : 1;
     int r = MFLBM_OK;
     (void)nsp;
-    // the storage layout is settled by mflbm_set_geometry unless it can only be dense
-    // (requested, or a singlephase deck with an inlet or outlet)
-    if (p.layout == MFLBM_LAYOUT_DENSE || (!p.multiphase && (p.inlet_bc != 0 || p.outlet_bc != 0))) {
+    // the storage layout is settled by mflbm_set_geometry unless dense is requested
+    if (p.layout == MFLBM_LAYOUT_DENSE) {
         if ((r = alloc_dense(c))) goto fail_create;
     }
     if ((r = dalloc(c, &c->st.walls, n2(p)))) goto fail_create;
@@ -542,40 +542,66 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
         if (r) return r;
         c->st.fb = fbd;
     }
-    // storage layout of a singlephase run: the fluid list when the geometry allows it
-    if (!p.multiphase && p.layout != MFLBM_LAYOUT_DENSE && p.inlet_bc == 0 && p.outlet_bc == 0) {
+    // storage layout of a singlephase run: the fluid list when the geometry allows it.  With
+    // an open z direction (inlet / outlet conditions) the list keeps private slots for the
+    // cells of the planes the conditions address (the multiphase builder's planes), found
+    // through a slot map; otherwise every non-fluid slot is a bounce-back link.
+    if (!p.multiphase && p.layout != MFLBM_LAYOUT_DENSE) {
         ListLayout ll;
+        MpListLayout ml;
         std::string why;
-        const bool ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why);
+        const bool planes = c->open_z;
+        bool ok;
+        if (planes && p.iper) {
+            ok = false;
+            why = "an open z direction needs walls in x";
+        } else if (planes) {
+            ok = build_mp_list_layout(walls, p.nx, p.ny, p.nz, p.jper, p.kper, {0, 1, 2, p.nz - 1, p.nz, p.nz + 1}, {},
+                                      ml, why);
+        } else {
+            ok = build_list_layout(walls, p.nx, p.ny, p.nz, p.iper, p.jper, p.kper, ll, why);
+        }
+        const ListLayout &lay = planes ? static_cast<const ListLayout &>(ml) : ll;
         for (void *b : c->list_bufs) dfree(c, b);
         c->list_bufs.clear();
         if (ok) {
-            int r = alloc_pdf(c, (size_t)19 * ll.stride * c->elt);
+            int r = alloc_pdf(c, (size_t)19 * lay.stride * c->elt);
             if (r) return r;
-            int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *seg = nullptr;
-            if ((r = dalloc(c, &nb, 18 * ll.nf))) return r;
+            int32_t *nb = nullptr, *cell1 = nullptr, *link = nullptr, *seg = nullptr, *map = nullptr;
+            if ((r = dalloc(c, &nb, 18 * lay.nf))) return r;
             c->list_bufs.push_back(nb);
-            if ((r = dalloc(c, &cell1, ll.nf))) return r;
+            if ((r = dalloc(c, &cell1, lay.nf))) return r;
             c->list_bufs.push_back(cell1);
-            if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * ll.nlink)))) return r;
+            if ((r = dalloc(c, &link, std::max<int64_t>(3, 3 * lay.nlink)))) return r;
             c->list_bufs.push_back(link);
             if ((r = dalloc(c, &seg, p.nz + 1))) return r;
             c->list_bufs.push_back(seg);
-            CK(c, cudaMemcpy(nb, ll.nb.data(), sizeof(int32_t) * ll.nb.size(), cudaMemcpyHostToDevice));
-            CK(c, cudaMemcpy(cell1, ll.cell1.data(), sizeof(int32_t) * ll.cell1.size(), cudaMemcpyHostToDevice));
-            if (ll.nlink) CK(c, cudaMemcpy(link, ll.link.data(), sizeof(int32_t) * ll.link.size(), cudaMemcpyHostToDevice));
-            CK(c, cudaMemcpy(seg, ll.slice.data(), sizeof(int32_t) * ll.slice.size(), cudaMemcpyHostToDevice));
+            if (planes) {
+                if ((r = dalloc(c, &map, (int64_t)ml.map.size()))) return r;
+                c->list_bufs.push_back(map);
+                CK(c, cudaMemcpy(map, ml.map.data(), sizeof(int32_t) * ml.map.size(), cudaMemcpyHostToDevice));
+            }
+            CK(c, cudaMemcpy(nb, lay.nb.data(), sizeof(int32_t) * lay.nb.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(cell1, lay.cell1.data(), sizeof(int32_t) * lay.cell1.size(), cudaMemcpyHostToDevice));
+            if (lay.nlink)
+                CK(c, cudaMemcpy(link, lay.link.data(), sizeof(int32_t) * lay.link.size(), cudaMemcpyHostToDevice));
+            CK(c, cudaMemcpy(seg, lay.slice.data(), sizeof(int32_t) * lay.slice.size(), cudaMemcpyHostToDevice));
             DevState &st = c->st;
             st.list = 1;
+            st.mplist = 0;
             st.f = c->pdf;
             st.g = nullptr;
-            st.lstride = ll.stride;
+            st.lstride = lay.stride;
             st.nb = nb;
             st.cell1 = cell1;
             st.link = link;
-            st.nlink = ll.nlink;
-            st.nfl = (int)ll.nf;
+            st.nlink = lay.nlink;
+            st.nfl = (int)lay.nf;
             st.lseg = seg;
+            st.pmap = map;
+            st.pspare = planes ? ml.spare : 0;
+            st.pwrap = nullptr;
+            st.nwrap = 0;
             st.ncell = 0;
             // the TMA even step, unless MFLBM_NO_TMA is set (a diagnostic switch that selects
             // the plain even step, for comparisons)

@@ -2079,21 +2079,21 @@ __global__ void k_list_out(const S *__restrict__ A, const int64_t stride, const 
 // ---------------------------------------------------------------------------------
 template <class S>
 __global__ void k_mp_planes_in(S *__restrict__ A, const int64_t stride, const int q, const int32_t *__restrict__ map,
-                               const int nf, const int64_t n1, const double *__restrict__ stage) {
+                               const int nf, const int64_t n1, const double *__restrict__ stage, float scale) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n1) return;
     const int32_t m = map[t];
-    if (m >= nf) Store<S>::st64(A + (int64_t)q * stride, m, stage[t], WREST(q), 1.0f);
+    if (m >= nf) Store<S>::st64(A + (int64_t)q * stride, m, stage[t], WREST(q), scale);
 }
 
 template <class S>
 __global__ void k_mp_planes_out(const S *__restrict__ A, const int64_t stride, const int q,
                                 const int32_t *__restrict__ map, const int nf, const int64_t n1,
-                                double *__restrict__ stage) {
+                                double *__restrict__ stage, float scale) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n1) return;
     const int32_t m = map[t];
-    if (m >= nf) stage[t] = Store<S>::ld64(A + (int64_t)q * stride, m, WREST(q), 1.0f);
+    if (m >= nf) stage[t] = Store<S>::ld64(A + (int64_t)q * stride, m, WREST(q), 1.0f / scale);
 }
 
 // the equilibrium at rest of every link slot, from phi at its solid cell: k_init_eq's
@@ -2301,6 +2301,41 @@ __global__ void k_init_vel_links(S *__restrict__ A, const int64_t stride, const 
         const int32_t slot = nb[(int64_t)(d - 1) * nf + x];
         if (slot >= nf)
             St::st64(A, (int64_t)OPP_RT(d) * stride + slot, feq_vel(d, r, u[c], v[c], w[c], rest_base), WREST(d), scale);
+    }
+}
+
+// list layout with boundary-plane slots, pass 3: every cell that owns a plane slot, as
+// k_init_vel_dense writes that cell (after pass 2, which also reaches plane slots through
+// the neighbour table)
+template <class S>
+__global__ void k_init_vel_planes(S *__restrict__ A, const PdfAt pa, const int nf, const double *__restrict__ rho,
+                                  const double *__restrict__ u, const double *__restrict__ v,
+                                  const double *__restrict__ w, const int8_t *__restrict__ walls, const Layout L,
+                                  int rest_base, float scale) {
+    using St = Store<S>;
+    const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1) return;
+    const int32_t m = pa.map[t];
+    if (m < nf) return;   // a fluid node, a periodic ghost or a cell without a slot
+    const int i = (int)(t % (L.nx + 2));
+    const int j = (int)((t / (L.nx + 2)) % (L.ny + 2));
+    const int k = (int)(t / ((int64_t)(L.nx + 2) * (L.ny + 2)));
+    if (walls[L.i2(i, j, k)] == 0) {
+        const double r = rho ? rho[t] : 1.0;
+        for (int q = 0; q < 19; ++q)
+            St::st64(A, (int64_t)q * pa.qs + m, feq_vel(q, r, u[t], v[t], w[t], rest_base), WREST(q), scale);
+        return;
+    }
+    for (int q = 0; q < 19; ++q) {
+        double val = rest_base ? WREST(q) : WEQ(q);
+        const int ni = i + c_ex[q], nj = j + c_ey[q], nk = k + c_ez[q];
+        if (q > 0 && ni >= 0 && ni <= L.nx + 1 && nj >= 0 && nj <= L.ny + 1 && nk >= 0 && nk <= L.nz + 1 &&
+            walls[L.i2(ni, nj, nk)] == 0) {
+            const int64_t mm = L.i1(ni, nj, nk);
+            val = feq_vel(OPP_RT(q), rho ? rho[mm] : 1.0, u[mm], v[mm], w[mm], rest_base);
+        }
+        St::st64(A, (int64_t)q * pa.qs + m, val, WREST(q), scale);
     }
 }
 

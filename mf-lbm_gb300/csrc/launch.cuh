@@ -24,11 +24,12 @@ inline bool dw_grad(const DevState &st) {
     return st.multiphase && (st.prec == MFLBM_FP64FF || st.prec == MFLBM_FF);
 }
 
-// where the cell-addressed kernels find a population: dense planes or the multiphase list
+// where the cell-addressed kernels find a population: dense planes, or a fluid list with
+// boundary-plane slots (multiphase; singlephase with an inlet or outlet) through its slot map
 inline PdfAt pdf_at(const DevState &st) {
     PdfAt a;
-    a.qs = st.mplist ? st.lstride : st.L.qs;
-    a.map = st.mplist ? st.pmap : nullptr;
+    a.qs = st.pmap ? st.lstride : st.L.qs;
+    a.map = st.pmap;
     a.spare = st.pspare;
     return a;
 }
@@ -441,6 +442,7 @@ template <class S>
 int init_t(const DevState &st, bool convec, cudaStream_t s) {
     const Layout &L = st.L;
     if (st.list && !st.mplist) {
+        // the rest equilibrium in every slot (fluid nodes, boundary-plane cells, links)
         const int64_t n = 19 * st.lstride;
         k_list_init<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.scale);
         const size_t b1 = sizeof(double) * (size_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
@@ -449,7 +451,11 @@ int init_t(const DevState &st, bool convec, cudaStream_t s) {
         cudaMemsetAsync(st.w, 0, b1, s);
         const int64_t nb1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
         k_list_plane_fill<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.rho, nb1, 1.0);
-        return 2;
+        if (!convec) return 2;
+        const int64_t np = (int64_t)(L.nx + 2) * (L.ny + 2);
+        k_init_convec<S><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(fs<S>(st), nullptr, nullptr, st.fconv, nullptr,
+                                                                      nullptr, L, pdf_at(st), 0, st.ref, st.scale);
+        return 3;
     }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     S *g = st.multiphase ? gs<S>(st) : nullptr;
@@ -483,20 +489,16 @@ int init_equilibrium(const DevState &st, bool convec, cudaStream_t s) {
 template <class S>
 int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
-    if (st.mplist) {
+    if (st.list) {
         S *A = sp == 0 ? fs<S>(st) : gs<S>(st);
         const int64_t n = st.nfl + st.nlink;
-        const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
         k_list_in<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.cell1, st.nfl, st.link, st.nlink,
                                                                  st.stage, st.scale);
-        k_mp_planes_in<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage);
+        if (!st.pmap) return 1;
+        const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        k_mp_planes_in<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage,
+                                                                       st.scale);
         return 2;
-    }
-    if (st.list) {
-        const int64_t n = st.nfl + st.nlink;
-        k_list_in<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, q, st.cell1, st.nfl, st.link,
-                                                                 st.nlink, st.stage, st.scale);
-        return 1;
     }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     S *base = (sp == 0 ? fs<S>(st) : gs<S>(st)) + (int64_t)q * L.qs;
@@ -507,7 +509,7 @@ int convert_in_t(const DevState &st, int sp, int q, cudaStream_t s) {
 template <class S>
 int convert_out_t(const DevState &st, int sp, int q, cudaStream_t s) {
     const Layout &L = st.L;
-    if (st.mplist) {
+    if (st.list) {
         // fluid nodes, link slots, periodic ghosts as their images, boundary-plane slots; the
         // cells that no update reads keep the rest weight
         const S *A = sp == 0 ? fs<S>(st) : gs<S>(st);
@@ -517,17 +519,10 @@ int convert_out_t(const DevState &st, int sp, int q, cudaStream_t s) {
         k_list_out<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.cell1, st.nfl, st.link, st.nlink,
                                                                   st.stage, st.scale);
         k_list_ghosts<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(st.stage, L, st.P.iper, st.P.jper, st.P.kper);
-        k_mp_planes_out<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage);
+        if (!st.pmap) return 3;
+        k_mp_planes_out<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(A, st.lstride, q, st.pmap, st.nfl, n1, st.stage,
+                                                                        st.scale);
         return 4;
-    }
-    if (st.list) {
-        const int64_t nb1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
-        const int64_t n = st.nfl + st.nlink;
-        k_list_plane_fill<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.stage, nb1, WEQ(q));
-        k_list_out<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, q, st.cell1, st.nfl, st.link,
-                                                                  st.nlink, st.stage, st.scale);
-        k_list_ghosts<<<(unsigned)((nb1 + 255) / 256), 256, 0, s>>>(st.stage, L, st.P.iper, st.P.jper, st.P.kper);
-        return 3;
     }
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
     const S *base = (sp == 0 ? fs<S>(st) : gs<S>(st)) + (int64_t)q * L.qs;
@@ -655,7 +650,13 @@ int init_velocity_t(const DevState &st, const double *rho, int rest_base, cudaSt
         k_init_vel_links<S><<<(unsigned)((st.nfl + 255) / 256), 256, 0, s>>>(fs<S>(st), st.lstride, st.nb, st.cell1,
                                                                              st.nfl, rho, st.u, st.v, st.w, rest_base,
                                                                              st.scale);
-        return 2;
+        if (!st.pmap) return 2;
+        // the boundary-plane cells last, as the dense kernel writes them
+        const Layout &L = st.L;
+        const int64_t n1 = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        k_init_vel_planes<S><<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(fs<S>(st), pdf_at(st), st.nfl, rho, st.u,
+                                                                          st.v, st.w, st.walls, L, rest_base, st.scale);
+        return 3;
     }
     const Layout &L = st.L;
     const int64_t nb = (int64_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);

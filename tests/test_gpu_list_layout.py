@@ -103,27 +103,25 @@ def test_graph_run_equals_steps_and_init():
         s.close()
 
 
-def test_auto_falls_back_to_dense_and_list_request_rejected():
-    # open z (velocity inlet): dense
+def test_layout_choice_with_open_z():
+    """An open z direction (inlet / outlet conditions, or neither) takes the fluid list with
+    boundary-plane slots when x is walled; with x periodic it falls back to the dense planes
+    under AUTO, and an explicit list request is refused when the context is created."""
     case = sp_case(nx=10, ny=8, nz=12, per=(0, 0, 0), inlet=1, outlet=1, force=0.0, spheres=1)
     with Solver(case["params"]) as s:
         s.set_geometry(case["walls"], w_in=case["w_in"])
+        assert s.layout == LAYOUT_LIST
+    case = sp_case(nx=10, ny=8, nz=12, per=(0, 1, 0), spheres=1)
+    with Solver(case["params"]) as s:
+        s.set_geometry(case["walls"])
+        assert s.layout == LAYOUT_LIST
+    case = sp_case(nx=10, ny=8, nz=12, per=(1, 1, 0), inlet=1, outlet=1, force=0.0, spheres=1)
+    with Solver(case["params"]) as s:
+        s.set_geometry(case["walls"], w_in=case["w_in"])
         assert s.layout == LAYOUT_DENSE
-    case = sp_case(nx=10, ny=8, nz=12, per=(0, 0, 0), inlet=1, outlet=1, force=0.0, spheres=1)
     case["params"].layout = LAYOUT_LIST
     with pytest.raises(MflbmError):
         Solver(case["params"])
-    # z neither periodic nor walled, no inlet: a fluid node borders the z ghost layer
-    case = sp_case(nx=10, ny=8, nz=12, per=(0, 1, 0), spheres=1)
-    case["params"].layout = LAYOUT_LIST
-    s = Solver(case["params"])
-    with pytest.raises(MflbmError):
-        s.set_geometry(case["walls"])
-    s.close()
-    case["params"].layout = 0
-    with Solver(case["params"]) as s:
-        s.set_geometry(case["walls"])
-        assert s.layout == LAYOUT_DENSE
 
 
 def test_unit_rate_collision_matches_oracle():
