@@ -90,6 +90,10 @@ def parse():
     ap.add_argument("--no-convergence", action="store_true",
                     help="skip the time-to-steady permeability study (singlephase workload only)")
     ap.add_argument("--conv-tol", type=float, default=1e-7)
+    ap.add_argument("--open-z", action="store_true",
+                    help="c2: the packing between 16-layer inlet and outlet buffers with a velocity inlet "
+                         "(mean 1e-4) and a convective outlet instead of periodic z with a body force "
+                         "(skips the per-form and convergence studies)")
     ap.add_argument("--layout", type=int, default=0, choices=[0, 1, 2],
                     help="PDF storage: 0 auto, 1 dense planes, 2 fluid list (fluid nodes + link slots)")
     return ap.parse_args()
@@ -112,6 +116,12 @@ def workload(args, device=0):
         case = workloads.packing_drainage(nxy=args.n, nzp=args.n, buffer=32, device=device, precision=args.precision)
         desc = (f"multiphase drainage, {args.n}^2x{args.n} sphere packing porosity 0.22 + 32-layer buffers, "
                 f"inlet velocity 5e-5, gamma=0.01, theta=30, {DTYPE[args.precision]}")
+    elif args.open_z:
+        case = workloads.packing_throughflow(n=args.n, porosity=args.porosity, precision=args.precision,
+                                             device=device)
+        desc = (f"singlephase through-flow, {args.n}^3 sphere packing porosity {args.porosity} between 16-layer "
+                "inlet and outlet buffers, walls in x and y, velocity inlet 1e-4, convective outlet, tau=1, "
+                "MRT preset 1")
     else:
         case = workloads.packing_permeability(n=args.n, porosity=args.porosity, precision=args.precision,
                                               device=device)
@@ -755,7 +765,7 @@ def main():
 
     # ---- every other storage form of the singlephase workload, measured the same way
     forms = None
-    if rank == 0 and args.workload == "c2" and not args.no_forms:
+    if rank == 0 and args.workload == "c2" and not args.no_forms and not args.open_z:
         forms = {}
         for prec in (0, 3, 4, 1, 2):
             if prec == args.precision:
@@ -791,7 +801,7 @@ def main():
         }
         if forms is not None:
             line["forms"] = forms
-    if rank == 0 and args.workload == "c2" and not args.no_convergence:
+    if rank == 0 and args.workload == "c2" and not args.no_convergence and not args.open_z:
         try:
             line["convergence"] = convergence_study(args, case, local)
         except Exception as exc:

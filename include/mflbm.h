@@ -80,11 +80,11 @@ extern "C" {
 /* PDF storage layout (no counterpart in the reference, which stores every cell).
  * DENSE: one plane per direction over the halo-1 box, as the reference's arrays.
  * LIST:  only the fluid nodes plus one slot per solid bounce-back link, with an
- *        18-entry neighbour table; singlephase samples that are periodic or walled in
- *        every direction (no inlet/outlet), and multiphase runs with any boundary
- *        conditions (the cells of the inlet, outlet and porous-plate planes keep their own
- *        slots).  Same update, same results on every fluid node; downloads give the other
- *        slots, which no update reads, the rest weight w_q.
+ *        18-entry neighbour table; with an open z direction (inlet / outlet conditions)
+ *        or a porous plate, the cells of the planes those conditions address keep their
+ *        own slots.  Multiphase runs with any boundary conditions; singlephase runs with
+ *        walls in x when z is open.  Same update, same results on every fluid node;
+ *        downloads give the other slots, which no update reads, the rest weight w_q.
  * AUTO:  LIST when the geometry allows it, else DENSE (decided by mflbm_set_geometry). */
 #define MFLBM_LAYOUT_AUTO  0
 #define MFLBM_LAYOUT_DENSE 1

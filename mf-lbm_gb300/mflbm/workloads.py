@@ -5,6 +5,7 @@ with the sizes, porosities and flow settings of each configuration.
 
   tube_drainage         64x64x160 tube with a spherical obstacle, multiphase drainage
   packing_permeability  n^3 sphere packing, singlephase body-force permeability
+  packing_throughflow   n^3 sphere packing between inlet/outlet buffers, singlephase
   packing_drainage      sphere packing with inlet/outlet buffers, multiphase drainage
 """
 import numpy as np
@@ -53,6 +54,23 @@ def packing_permeability(n=256, porosity=0.22, seed=2024, precision=0, strict_fp
     wg = geometry.sphere_packing((n, n, n), porosity, mean_r=8.0, sd_r=2.0, seed=seed)
     walls, pore, _ = geometry.set_walls(p, wg)
     return dict(params=p, walls=walls, pore=pore, walls_global=wg)
+
+
+def packing_throughflow(n=256, buffer=16, porosity=0.22, seed=11, precision=0, strict_fp=0, device=0, uin=1e-4):
+    """Singlephase flow through an n^3 sphere packing (as packing_permeability, not periodic)
+    between open inlet and outlet buffers of `buffer` layers: walls on the x and y faces,
+    velocity inlet (rectangular-duct profile, mean uin), convective outlet, tau = 1, MRT
+    preset 1."""
+    nz = n + 2 * buffer
+    p = make_params(multiphase=0, nx=n, ny=n, nz=nz, iper=0, jper=0, kper=0, wall_x_min=1, wall_x_max=1,
+                    wall_y_min=1, wall_y_max=1, wall_z_min=0, wall_z_max=0, inlet_bc=1, outlet_bc=1, mrt=1,
+                    la_nu1=1.0 / 6.0, uin_avg=uin, precision=precision, strict_fp=strict_fp, device=device)
+    pack = geometry.sphere_packing((n, n, n), porosity, mean_r=8.0, sd_r=2.0, seed=seed,
+                                   periodic=(False, False, False))
+    wg = np.zeros((nz, n, n), dtype=np.int8)
+    wg[buffer:buffer + n] = pack
+    walls, pore, _ = geometry.set_walls(p, wg)
+    return dict(params=p, walls=walls, pore=pore, w_in=geometry.inlet_profile(n, n, uin))
 
 
 def packing_drainage(nxy=512, nzp=512, buffer=32, porosity=0.22, seed=7, strict_fp=0, device=0, precision=0,
