@@ -411,8 +411,22 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
             return ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;           \
     };
 
+// Resident blocks per SM (128 threads each) the compiler must allow for the multiphase
+// collision, i.e. its register cap.  FP32: 5 (at most 102 registers, no spills in the
+// fluid-list odd step that preloads its 18 table entries; the sweep 1/4/5/6 gave 0.579 /
+// 0.646 / 0.691 / 0.689 of the roofline on the C3 packing).  FP64: 3 (FP64-pipe bound; 4
+// and above spill).  Tuning parameters: MFLBM_NVCC_FLAGS=-DMFLBM_MP_MIN_BLOCKS_F32=n.
+#ifndef MFLBM_MP_MIN_BLOCKS_F32
+#define MFLBM_MP_MIN_BLOCKS_F32 5
+#endif
+#ifndef MFLBM_MP_MIN_BLOCKS_F64
+#define MFLBM_MP_MIN_BLOCKS_F64 3
+#endif
+template <class T> struct MpOcc { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F64; };
+template <> struct MpOcc<float> { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F32; };
+
 template <class T, bool ODD, bool LIST = false>
-__global__ void __launch_bounds__(128) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
+__global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
                                                  const T *__restrict__ cnx, const T *__restrict__ cny,
                                                  const T *__restrict__ cnz, const T *__restrict__ cnorm,
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
@@ -1094,6 +1108,31 @@ __global__ void k_extrap_phi(T *__restrict__ phi, const SolidBnd *__restrict__ s
     phi[L.i4(s.ix, s.iy, s.iz)] = acc / T(s.la_weight);
 }
 
+// Register caps of the fluid-cell gradient kernels (256 threads) and of the compact-record
+// normal extrapolation (128 threads): resident blocks per SM.  The FP32 gradient lists take 5
+// (curvature 52 -> 48 registers, 5 blocks instead of 4; C3 packing FP32 step 2.4 % faster;
+// 6 blocks spilled and gained less), the FP64 ones 3 (80 registers, as the compiler's own
+// choice; 5 spilled).  The extrapolation keeps the compiler's choice (72 registers in FP32;
+// caps of 8 and 10 blocks spilled and made the step slower), 0 below.
+// Tuning parameters (MFLBM_NVCC_FLAGS=-DMFLBM_GRAD_MIN_BLOCKS_F32=n, -DMFLBM_EXTRAP_MIN_BLOCKS=n).
+#ifndef MFLBM_GRAD_MIN_BLOCKS_F32
+#define MFLBM_GRAD_MIN_BLOCKS_F32 5
+#endif
+#ifndef MFLBM_GRAD_MIN_BLOCKS_F64
+#define MFLBM_GRAD_MIN_BLOCKS_F64 3
+#endif
+#ifndef MFLBM_EXTRAP_MIN_BLOCKS
+#define MFLBM_EXTRAP_MIN_BLOCKS 0
+#endif
+template <class T> struct GradOcc { static constexpr int kMinBlocks = MFLBM_GRAD_MIN_BLOCKS_F64; };
+template <> struct GradOcc<float> { static constexpr int kMinBlocks = MFLBM_GRAD_MIN_BLOCKS_F32; };
+#define MFLBM_GRAD_BOUNDS __launch_bounds__(256, GradOcc<T>::kMinBlocks)
+#if MFLBM_EXTRAP_MIN_BLOCKS > 0
+#define MFLBM_EXTRAP_BOUNDS __launch_bounds__(128, MFLBM_EXTRAP_MIN_BLOCKS)
+#else
+#define MFLBM_EXTRAP_BOUNDS __launch_bounds__(128)
+#endif
+
 // The same two extrapolations over the compact solid-boundary records (SolidBndC: packed
 // cell, bit mask of the fluid-neighbour directions, la_weight): 16 bytes read per node
 // instead of 96.  The 18 directions are visited in ascending order, which is the order of
@@ -1121,7 +1160,7 @@ __global__ void k_extrap_phi_c(T *__restrict__ phi, const SolidBndC *__restrict_
 }
 
 template <class T>
-__global__ void k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+__global__ void MFLBM_EXTRAP_BOUNDS k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
                                    const SolidBndC *__restrict__ sb, int ns, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
@@ -1228,7 +1267,7 @@ __global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, cons
 // this skips about two thirds of the cells, and every lane of a warp does work.
 
 template <class T>
-__global__ void __launch_bounds__(256) k_normals_list(const T *__restrict__ phi, const uint32_t *__restrict__ cl, int n,
+__global__ void MFLBM_GRAD_BOUNDS k_normals_list(const T *__restrict__ phi, const uint32_t *__restrict__ cl, int n,
                                                       T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
                                                       T *__restrict__ cnorm, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1410,7 +1449,7 @@ __global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, co
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_curvature_list(const T *__restrict__ cnx, const T *__restrict__ cny,
+__global__ void MFLBM_GRAD_BOUNDS k_curvature_list(const T *__restrict__ cnx, const T *__restrict__ cny,
                                                         const T *__restrict__ cnz, T *__restrict__ curv,
                                                         const uint32_t *__restrict__ cl, int n, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
