@@ -35,6 +35,7 @@ struct mflbm_ctx {
     bool open_z = false;
     int64_t cells_cap = 0;
     int64_t gn_cap = 0, gc_cap = 0, sbc_cap = 0;  // capacities of the colour-gradient lists
+    int64_t stage_len = 0;                         // FP64 elements of st.stage
     SolidBndC *sbc_buf = nullptr;
     void *pdf = nullptr;          // PDF storage (dense planes or fluid-list arrays)
     size_t pdf_bytes = 0;
@@ -452,17 +453,15 @@ int32_t mflbm_create(const mflbm_params *params, mflbm_ctx **out) {
     if ((r = dalloc(c, &c->st.rho, n1(p)))) goto fail_create;
     if ((r = dalloc(c, &c->st.mon, (int64_t)kMonNQ * p.nz))) goto fail_create;
     if ((r = dalloc(c, &c->st.err, 1))) goto fail_create;
-    // FP64 staging for the converted uploads/downloads: one PDF plane, or the halo-4
+    // FP64 staging for the converted uploads/downloads (every context: the normal records
+    // are downloaded one component at a time through it): one PDF plane, or the halo-4
     // phase field when that is larger
-    if ((!f64_storage(p) || !p.multiphase || p.layout != MFLBM_LAYOUT_DENSE) &&
-        (r = dalloc(c, &c->st.stage, p.multiphase ? std::max(n1(p), n4(p)) : n1(p)))) goto fail_create;
+    c->stage_len = p.multiphase ? std::max(n1(p), n4(p)) : n1(p);
+    if ((r = dalloc(c, &c->st.stage, c->stage_len))) goto fail_create;
     if (p.multiphase) {
         const size_t fe = (size_t)c->st.felt;
         if ((r = dalloc_bytes(c, &c->st.phi, fe * n4(p)))) goto fail_create;
-        if ((r = dalloc_bytes(c, &c->st.cnx, fe * n2(p)))) goto fail_create;
-        if ((r = dalloc_bytes(c, &c->st.cny, fe * n2(p)))) goto fail_create;
-        if ((r = dalloc_bytes(c, &c->st.cnz, fe * n2(p)))) goto fail_create;
-        if ((r = dalloc_bytes(c, &c->st.cnorm, fe * n2(p)))) goto fail_create;
+        if ((r = dalloc_bytes(c, &c->st.cn, 4 * fe * n2(p)))) goto fail_create;
         if ((r = dalloc_bytes(c, &c->st.curv, fe * n1(p)))) goto fail_create;
         if ((r = dalloc(c, &c->st.gconv, nplane(p) * 19))) goto fail_create;
         if ((r = dalloc(c, &c->st.phiconv, nplane(p)))) goto fail_create;
@@ -725,10 +724,7 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     const mflbm_params &p = c->p;
     const Layout &L = c->st.L;
     const size_t fe = (size_t)c->st.felt;
-    CK(c, cudaMemsetAsync(c->st.cnx, 0, fe * n2(p), c->stream));
-    CK(c, cudaMemsetAsync(c->st.cny, 0, fe * n2(p), c->stream));
-    CK(c, cudaMemsetAsync(c->st.cnz, 0, fe * n2(p), c->stream));
-    CK(c, cudaMemsetAsync(c->st.cnorm, 0, fe * n2(p), c->stream));
+    CK(c, cudaMemsetAsync(c->st.cn, 0, 4 * fe * n2(p), c->stream));
     CK(c, cudaMemsetAsync(c->st.curv, 0, fe * n1(p), c->stream));
     c->st.glist = 0;
     c->st.n_gcell_n = 0;
@@ -814,12 +810,15 @@ static int field_put(mflbm_ctx *c, void *dev, const double *host, int64_t n) {
     return MFLBM_OK;
 }
 
-// device field -> FP64 host array; synchronises the context stream
-static int field_get(mflbm_ctx *c, double *host, const void *dev, int64_t n) {
-    if (c->st.felt == 8) {
+// device field -> FP64 host array; synchronises the context stream.  stride > 1: every
+// stride-th element (one component of the normal records)
+static int field_get(mflbm_ctx *c, double *host, const void *dev, int64_t n, int stride = 1) {
+    if (!c->st.stage || n > c->stage_len)
+        return fail(c, MFLBM_ESTATE, "field download: staging buffer missing or too small");
+    if (c->st.felt == 8 && stride == 1) {
         CK(c, cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     } else {
-        c->kt->field_out(c->st, dev, n, c->stream);
+        c->kt->field_out(c->st, dev, n, stride, c->stream);
         CK(c, cudaPeekAtLastError());
         CK(c, cudaMemcpyAsync(host, c->st.stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     }
@@ -1122,10 +1121,11 @@ int32_t mflbm_get_gradient(mflbm_ctx *c, double *cn_x, double *cn_y, double *cn_
     CK(c, cudaSetDevice(c->dev));
     CK(c, cudaStreamSynchronize(c->stream));
     double *const dst[5] = {cn_x, cn_y, cn_z, c_norm, curv};
-    const void *src[5] = {c->st.cnx, c->st.cny, c->st.cnz, c->st.cnorm, c->st.curv};
     for (int a = 0; a < 5; ++a) {
         if (!dst[a]) continue;
-        int r = field_get(c, dst[a], src[a], a < 4 ? n2(p) : n1(p));
+        // components 0..3 of the normal records (x, y, z, |grad phi|), then curvature
+        const void *src = a < 4 ? (const void *)((const char *)c->st.cn + (size_t)a * c->st.felt) : c->st.curv;
+        int r = field_get(c, dst[a], src, a < 4 ? n2(p) : n1(p), a < 4 ? 4 : 1);
         if (r) return r;
     }
     return MFLBM_OK;

@@ -102,6 +102,15 @@ struct FluidBnd {
     double nwx, nwy, nwz, cos_t, sin_t;
 };
 
+// The colour-gradient normal of one halo-2 cell (the reference's cn_x, cn_y, cn_z, c_norm
+// arrays, Phase_gradient.F90:33-79) as one record: unit normal (x, y, z) and |grad phi| (n).
+// A stencil gathers a neighbour with one 16-byte load (FP32; two in FP64) instead of three
+// or four scalar loads from separate arrays.
+template <class T>
+struct alignas(4 * sizeof(T)) Nrm {
+    T x, y, z, n;
+};
+
 struct SolidBnd {  // identical to mflbm_solid_bnd (96 bytes)
     int ix, iy, iz, i_fluid_num;
     int nbr[18];

@@ -427,8 +427,7 @@ template <> struct MpOcc<float> { static constexpr int kMinBlocks = MFLBM_MP_MIN
 
 template <class T, bool ODD, bool LIST = false>
 __global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
-                                                 const T *__restrict__ cnx, const T *__restrict__ cny,
-                                                 const T *__restrict__ cnz, const T *__restrict__ cnorm,
+                                                 const Nrm<T> *__restrict__ cn,
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
                                                  const int ncell, const Layout L, const StepParams P, const double rk_weight2,
                                                  const int32_t *__restrict__ nb = nullptr, const int64_t stride = 0) {
@@ -458,8 +457,9 @@ __global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__rest
     const T ph = (rho1 - rho2) * inv_den;
 #endif
     phi[L.i4(i, j, k)] = ph;
-    const T cx = cnx[w2], cy = cny[w2], cz = cnz[w2];
-    T tmp = T(0.5) * T(P.gamma) * curv[L.i1(i, j, k)] * cnorm[w2];
+    const Nrm<T> nr = cn[w2];
+    const T cx = nr.x, cy = nr.y, cz = nr.z;
+    T tmp = T(0.5) * T(P.gamma) * curv[L.i1(i, j, k)] * nr.n;
     const T fx = tmp * cx;
     const T fy = tmp * cy;
     const T fz = tmp * cz + T(P.force_z);
@@ -549,9 +549,8 @@ __global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__rest
 // (MFLBM_FF, the double-word pairs stored as they are, renormalised on store)
 template <bool ODD, class S = double, bool LIST = false>
 __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__restrict__ g,
-                                                    double *__restrict__ phi, const double *__restrict__ cnx,
-                                                    const double *__restrict__ cny, const double *__restrict__ cnz,
-                                                    const double *__restrict__ cnorm, const double *__restrict__ curv,
+                                                    double *__restrict__ phi, const Nrm<double> *__restrict__ cn,
+                                                    const double *__restrict__ curv,
                                                     const int32_t *__restrict__ cells, const int ncell, const Layout L,
                                                     const MpConstFF K, const int mrt,
                                                     const int32_t *__restrict__ nb = nullptr, const int64_t stride = 0) {
@@ -589,8 +588,9 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__r
     const ff inv_den = ff(1.0f) / den;
     const ff ph = (rho1 - rho2) * inv_den;
     phi[L.i4(i, j, k)] = f64_of_ff(ph);
-    const ff cx = ff_from_f64(cnx[w2]), cy = ff_from_f64(cny[w2]), cz = ff_from_f64(cnz[w2]);
-    const ff tmpf = K.half_gamma * ff_from_f64(curv[L.i1(i, j, k)]) * ff_from_f64(cnorm[w2]);
+    const Nrm<double> nr = cn[w2];
+    const ff cx = ff_from_f64(nr.x), cy = ff_from_f64(nr.y), cz = ff_from_f64(nr.z);
+    const ff tmpf = K.half_gamma * ff_from_f64(curv[L.i1(i, j, k)]) * ff_from_f64(nr.n);
     const ff fx = tmpf * cx, fy = tmpf * cy, fz = tmpf * cz + K.force_z;
     const ff visc = (ff(1.0f) + ph) * K.nui1 + (ff(1.0f) - ph) * K.nui2;
     const ff omega = visc / (ff(6.0f) + ff_pow2(visc, 0.5f));
@@ -1160,8 +1160,8 @@ __global__ void k_extrap_phi_c(T *__restrict__ phi, const SolidBndC *__restrict_
 }
 
 template <class T>
-__global__ void MFLBM_EXTRAP_BOUNDS k_extrap_normals_c(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                                   const SolidBndC *__restrict__ sb, int ns, const Layout L) {
+__global__ void MFLBM_EXTRAP_BOUNDS k_extrap_normals_c(Nrm<T> *__restrict__ cn, const SolidBndC *__restrict__ sb, int ns,
+                                                       const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
     const SolidBndC s = sb[t];
@@ -1171,40 +1171,44 @@ __global__ void MFLBM_EXTRAP_BOUNDS k_extrap_normals_c(T *__restrict__ cnx, T *_
     const int64_t id = L.i2(ix, iy, iz);
     T ax = T(0.0), ay = T(0.0), az = T(0.0);
     if constexpr (sizeof(T) == 4) {
-        // FP32: all 54 gathers in flight before the sums
-        T vx[18], vy[18], vz[18];
+        // FP32: the gathers in two groups of nine directions, each group's record loads in
+        // flight together, then the sums in direction order
 #pragma unroll
-        for (int ie = 1; ie <= 18; ++ie) {
-            const bool on = (s.mask >> (ie - 1)) & 1u;
-            const int64_t nb = id + EX(ie) + L.h2x * EY(ie) + L.h2xy * EZ(ie);
-            vx[ie - 1] = on ? cnx[nb] : T(0.0);
-            vy[ie - 1] = on ? cny[nb] : T(0.0);
-            vz[ie - 1] = on ? cnz[nb] : T(0.0);
-        }
+        for (int h = 0; h < 2; ++h) {
+            Nrm<T> v[9];
 #pragma unroll
-        for (int ie = 1; ie <= 18; ++ie) {
-            if ((s.mask >> (ie - 1)) & 1u) {
-                const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
-                ax = ax + vx[ie - 1] * w;
-                ay = ay + vy[ie - 1] * w;
-                az = az + vz[ie - 1] * w;
+            for (int e = 0; e < 9; ++e) {
+                const int ie = 1 + 9 * h + e;
+                const bool on = (s.mask >> (ie - 1)) & 1u;
+                const int64_t nb = id + EX(ie) + L.h2x * EY(ie) + L.h2xy * EZ(ie);
+                v[e] = on ? cn[nb] : Nrm<T>{T(0.0), T(0.0), T(0.0), T(0.0)};
+            }
+#pragma unroll
+            for (int e = 0; e < 9; ++e) {
+                const int ie = 1 + 9 * h + e;
+                if ((s.mask >> (ie - 1)) & 1u) {
+                    const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
+                    ax = ax + v[e].x * w;
+                    ay = ay + v[e].y * w;
+                    az = az + v[e].z * w;
+                }
             }
         }
     } else {
-        // FP64: 54 preloaded doubles would cost occupancy; gather direction by direction
+        // FP64: gather direction by direction (preloaded records would cost occupancy)
         for (uint32_t m = s.mask; m; m &= m - 1u) {
             const int ie = __ffs((int)m);
             const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
-            const int64_t nb = L.i2(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie]);
-            ax = ax + cnx[nb] * w;
-            ay = ay + cny[nb] * w;
-            az = az + cnz[nb] * w;
+            const Nrm<T> v = cn[L.i2(ix + c_ex[ie], iy + c_ey[ie], iz + c_ez[ie])];
+            ax = ax + v.x * w;
+            ay = ay + v.y * w;
+            az = az + v.z * w;
         }
     }
     const T lw = T(s.la_weight);
-    cnx[id] = ax / lw;
-    cny[id] = ay / lw;
-    cnz[id] = az / lw;
+    cn[id].x = ax / lw;
+    cn[id].y = ay / lw;
+    cn[id].z = az / lw;
 }
 
 // ISO4 gradient and unit normal from a phi accessor P(a, b, c) = phi at offset (a, b, c)
@@ -1234,29 +1238,27 @@ __device__ __forceinline__ void normals_of(PA P, T &gx, T &gy, T &gz, T &cn) {
 // ISO4 gradient and unit normal of one cell from global memory
 template <class T>
 __device__ __forceinline__ void normals_at(const T *__restrict__ phi, int i, int j, int k, int64_t id,
-                                           T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                                           T *__restrict__ cnorm, const Layout &L) {
+                                           Nrm<T> *__restrict__ out, const Layout &L) {
     auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
     T gx, gy, gz, cn;
     normals_of<T>(P, gx, gy, gz, cn);
-    cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
+    out[id] = Nrm<T>{gx, gy, gz, cn};
 }
 
 // over [1-2, n+2]^3, every cell
 template <class T>
 __global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, const int8_t *__restrict__ walls,
-                                                 T *__restrict__ cnx, T *__restrict__ cny,
-                                                 T *__restrict__ cnz, T *__restrict__ cnorm, const Layout L) {
+                                                 Nrm<T> *__restrict__ cn, const Layout L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
     if (i > L.nx + 2 || j > L.ny + 2) return;
     const int64_t id = L.i2(i, j, k);
     if (walls[id] == 1) {  // the reference zeroes normals at wall nodes (Phase_gradient.F90:65-69)
-        cnx[id] = T(0.0); cny[id] = T(0.0); cnz[id] = T(0.0); cnorm[id] = T(0.0);
+        cn[id] = Nrm<T>{T(0.0), T(0.0), T(0.0), T(0.0)};
         return;
     }
-    normals_at<T>(phi, i, j, k, id, cnx, cny, cnz, cnorm, L);
+    normals_at<T>(phi, i, j, k, id, cn, L);
 }
 
 // Fluid-cell forms of k_normals / k_curvature (default build): one thread per entry of a
@@ -1268,13 +1270,12 @@ __global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, cons
 
 template <class T>
 __global__ void MFLBM_GRAD_BOUNDS k_normals_list(const T *__restrict__ phi, const uint32_t *__restrict__ cl, int n,
-                                                      T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                                                      T *__restrict__ cnorm, const Layout L) {
+                                                      Nrm<T> *__restrict__ cn, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
-    normals_at<T>(phi, i, j, k, L.i2(i, j, k), cnx, cny, cnz, cnorm, L);
+    normals_at<T>(phi, i, j, k, L.i2(i, j, k), cn, L);
 }
 
 // The two stencils of the double-word form (MFLBM_FP64FF, multiphase): FP64 fields split on
@@ -1282,8 +1283,7 @@ __global__ void MFLBM_GRAD_BOUNDS k_normals_list(const T *__restrict__ phi, cons
 // results.  Fluid-cell lists only; without them the form uses the FP64 kernels.
 template <int DUMMY = 0>
 __global__ void __launch_bounds__(256) k_normals_list_ff(const double *__restrict__ phi, const uint32_t *__restrict__ cl,
-                                                         int n, double *__restrict__ cnx, double *__restrict__ cny,
-                                                         double *__restrict__ cnz, double *__restrict__ cnorm,
+                                                         int n, Nrm<double> *__restrict__ out,
                                                          const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -1300,28 +1300,24 @@ __global__ void __launch_bounds__(256) k_normals_list_ff(const double *__restric
             c2 * (P(1, 0, 1) - P(-1, 0, -1) + P(-1, 0, 1) - P(1, 0, -1) + P(0, 1, 1) - P(0, -1, -1) + P(0, -1, 1) - P(0, 1, -1));
     ff cn = ff_sqrt(gx * gx + gy * gy + gz * gz);
     if (ff_less(cn, ff_const(1e-6))) {
-        cnx[id] = 0.0; cny[id] = 0.0; cnz[id] = 0.0; cnorm[id] = 0.0;
+        out[id] = Nrm<double>{0.0, 0.0, 0.0, 0.0};
         return;
     }
     const ff inv = ff(1.0f) / cn;
-    cnx[id] = f64_of_ff(gx * inv);
-    cny[id] = f64_of_ff(gy * inv);
-    cnz[id] = f64_of_ff(gz * inv);
-    cnorm[id] = f64_of_ff(cn);
+    out[id] = Nrm<double>{f64_of_ff(gx * inv), f64_of_ff(gy * inv), f64_of_ff(gz * inv), f64_of_ff(cn)};
 }
 
 template <int DUMMY = 0>
-__global__ void __launch_bounds__(256) k_curvature_list_ff(const double *__restrict__ cnx, const double *__restrict__ cny,
-                                                           const double *__restrict__ cnz, double *__restrict__ curv,
+__global__ void __launch_bounds__(256) k_curvature_list_ff(const Nrm<double> *__restrict__ cn, double *__restrict__ curv,
                                                            const uint32_t *__restrict__ cl, int n, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
     constexpr ff c1 = ff_const(ISO4_1), c2 = ff_const(ISO4_2);
-    auto X = [&](int a, int b, int c) { return ff_from_f64(cnx[L.i2(i + a, j + b, k + c)]); };
-    auto Y = [&](int a, int b, int c) { return ff_from_f64(cny[L.i2(i + a, j + b, k + c)]); };
-    auto Z = [&](int a, int b, int c) { return ff_from_f64(cnz[L.i2(i + a, j + b, k + c)]); };
+    auto X = [&](int a, int b, int c) { return ff_from_f64(cn[L.i2(i + a, j + b, k + c)].x); };
+    auto Y = [&](int a, int b, int c) { return ff_from_f64(cn[L.i2(i + a, j + b, k + c)].y); };
+    auto Z = [&](int a, int b, int c) { return ff_from_f64(cn[L.i2(i + a, j + b, k + c)].z); };
     const ff kxx = c1 * (X(1, 0, 0) - X(-1, 0, 0)) +
                    c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));
     const ff kyy = c1 * (Y(0, 1, 0) - Y(0, -1, 0)) +
@@ -1350,23 +1346,23 @@ __global__ void __launch_bounds__(256) k_curvature_list_ff(const double *__restr
 #include "wetting.cuh"
 
 template <class T>
-__global__ void k_wetting(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
-                          const T *__restrict__ cnorm, const FluidBnd *__restrict__ fb, int nf, const Layout L,
+__global__ void k_wetting(Nrm<T> *__restrict__ cn, const FluidBnd *__restrict__ fb, int nf, const Layout L,
                           const T min_one_m) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nf) return;
     const FluidBnd b = fb[t];
     const int64_t id = L.i2(b.ix, b.iy, b.iz);
-    if (cnorm[id] > T(1e-6)) {
-        T n[3] = {cnx[id], cny[id], cnz[id]};
+    const Nrm<T> v = cn[id];
+    if (v.n > T(1e-6)) {
+        T n[3] = {v.x, v.y, v.z};
         wetting_normal<T>(n, T(b.nwx), T(b.nwy), T(b.nwz), T(b.cos_t), T(b.sin_t), min_one_m);
-        cnx[id] = n[0]; cny[id] = n[1]; cnz[id] = n[2];
+        cn[id] = Nrm<T>{n[0], n[1], n[2], v.n};
     }
 }
 
 // normal extrapolation to solid-boundary nodes inside [0, n+1]^3 (:85-110)
 template <class T>
-__global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__restrict__ cnz,
+__global__ void k_extrap_normals(Nrm<T> *__restrict__ cn,
                                  const SolidBnd *__restrict__ sb, int ns, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
@@ -1379,15 +1375,16 @@ __global__ void k_extrap_normals(T *__restrict__ cnx, T *__restrict__ cny, T *__
         const int dx = c_ex[ie], dy = c_ey[ie], dz = c_ez[ie];
         const T w = ie <= 6 ? T(w_equ_1) : T(w_equ_2);
         const int64_t nb = L.i2(s.ix + dx, s.iy + dy, s.iz + dz);
-        ax = ax + cnx[nb] * w;
-        ay = ay + cny[nb] * w;
-        az = az + cnz[nb] * w;
+        const Nrm<T> v = cn[nb];
+        ax = ax + v.x * w;
+        ay = ay + v.y * w;
+        az = az + v.z * w;
     }
     const int64_t id = L.i2(s.ix, s.iy, s.iz);
     const T lw = T(s.la_weight);
-    cnx[id] = ax / lw;
-    cny[id] = ay / lw;
-    cnz[id] = az / lw;
+    cn[id].x = ax / lw;
+    cn[id].y = ay / lw;
+    cn[id].z = az / lw;
 }
 
 // curvature of one cell (:113-201)
@@ -1419,19 +1416,17 @@ __device__ __forceinline__ T curvature_of(FX X, FY Y, FZ Z) {
 }
 
 template <class T>
-__device__ __forceinline__ void curvature_at(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                             const T *__restrict__ cnz, T *__restrict__ curv, int i, int j, int k,
+__device__ __forceinline__ void curvature_at(const Nrm<T> *__restrict__ cn, T *__restrict__ curv, int i, int j, int k,
                                              const Layout &L) {
-    auto X = [&](int a, int b, int c) { return cnx[L.i2(i + a, j + b, k + c)]; };
-    auto Y = [&](int a, int b, int c) { return cny[L.i2(i + a, j + b, k + c)]; };
-    auto Z = [&](int a, int b, int c) { return cnz[L.i2(i + a, j + b, k + c)]; };
+    auto X = [&](int a, int b, int c) { return cn[L.i2(i + a, j + b, k + c)].x; };
+    auto Y = [&](int a, int b, int c) { return cn[L.i2(i + a, j + b, k + c)].y; };
+    auto Z = [&](int a, int b, int c) { return cn[L.i2(i + a, j + b, k + c)].z; };
     curv[L.i1(i, j, k)] = curvature_of<T>(X, Y, Z);
 }
 
 // over [1, n]^3, every cell
 template <class T>
-__global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                                   const T *__restrict__ cnz, T *__restrict__ curv,
+__global__ void __launch_bounds__(256) k_curvature(const Nrm<T> *__restrict__ cn, T *__restrict__ curv,
                                                    const int8_t *__restrict__ walls, const Layout L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -1445,18 +1440,17 @@ __global__ void __launch_bounds__(256) k_curvature(const T *__restrict__ cnx, co
         return;
     }
 #endif
-    curvature_at<T>(cnx, cny, cnz, curv, i, j, k, L);
+    curvature_at<T>(cn, curv, i, j, k, L);
 }
 
 template <class T>
-__global__ void MFLBM_GRAD_BOUNDS k_curvature_list(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                                        const T *__restrict__ cnz, T *__restrict__ curv,
+__global__ void MFLBM_GRAD_BOUNDS k_curvature_list(const Nrm<T> *__restrict__ cn, T *__restrict__ curv,
                                                         const uint32_t *__restrict__ cl, int n, const Layout L) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
-    curvature_at<T>(cnx, cny, cnz, curv, i, j, k, L);
+    curvature_at<T>(cn, curv, i, j, k, L);
 }
 
 // Shared-memory forms of the two stencils (default build): a block of 32 x 8 threads owns
@@ -1478,6 +1472,7 @@ template <class T, int NF>
 struct GradPlanes {
     const T *src[NF];
     int64_t hx, hxy, o;
+    int es;                 // elements between consecutive cells (1: a plain field, 4: a Nrm record component)
     int imax, jmax, kmax;   // largest valid index per axis
     __device__ __forceinline__ void fetch(T (&r)[NF][GRAD_LD], int i0, int j0, int k, int tid) const {
 #pragma unroll
@@ -1488,7 +1483,7 @@ struct GradPlanes {
             const bool ok = idx < GRAD_PN && i <= imax && j <= jmax && k <= kmax;
             const int64_t a = o + i + hx * j + hxy * k;
 #pragma unroll
-            for (int f = 0; f < NF; ++f) r[f][l] = ok ? src[f][a] : T(0.0);
+            for (int f = 0; f < NF; ++f) r[f][l] = ok ? src[f][a * es] : T(0.0);
         }
     }
     __device__ __forceinline__ void put(T (*sm)[3][GRAD_PN], const T (&r)[NF][GRAD_LD], int slot, int tid) const {
@@ -1506,9 +1501,7 @@ struct GradPlanes {
 template <class T>
 __global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_normals_tile(const T *__restrict__ phi,
                                                                     const int8_t *__restrict__ walls,
-                                                                    T *__restrict__ cnx, T *__restrict__ cny,
-                                                                    T *__restrict__ cnz, T *__restrict__ cnorm,
-                                                                    const Layout L) {
+                                                                    Nrm<T> *__restrict__ out, const Layout L) {
     __shared__ T sm[1][3][GRAD_PN];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + GRAD_TX * ty;
     const int i0 = -1 + (int)blockIdx.x * GRAD_TX, j0 = -1 + (int)blockIdx.y * GRAD_TY;
@@ -1516,6 +1509,7 @@ __global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_normals_tile(const T *__re
     const int ke = min(kb + GRAD_KCH - 1, L.nz + 2);
     GradPlanes<T, 1> g;
     g.src[0] = phi;
+    g.es = 1;
     g.hx = L.h4x; g.hxy = L.h4xy; g.o = 3 + 3 * L.h4x + 3 * L.h4xy;
     g.imax = L.nx + 4; g.jmax = L.ny + 4; g.kmax = L.nz + 4;
     T r[1][GRAD_LD];
@@ -1536,7 +1530,7 @@ __global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_normals_tile(const T *__re
                 auto P = [&](int a, int b, int c) { return sm[0][(k + c + 3) % 3][(tx + 1 + a) + GRAD_PW * (ty + 1 + b)]; };
                 T gx, gy, gz, cn;
                 normals_of<T>(P, gx, gy, gz, cn);
-                cnx[id] = gx; cny[id] = gy; cnz[id] = gz; cnorm[id] = cn;
+                out[id] = Nrm<T>{gx, gy, gz, cn};
             }
         }
         __syncthreads();
@@ -1544,8 +1538,7 @@ __global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_normals_tile(const T *__re
 }
 
 template <class T>
-__global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_curvature_tile(const T *__restrict__ cnx, const T *__restrict__ cny,
-                                                                      const T *__restrict__ cnz, T *__restrict__ curv,
+__global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_curvature_tile(const Nrm<T> *__restrict__ cn, T *__restrict__ curv,
                                                                       const int8_t *__restrict__ walls, const Layout L) {
     __shared__ T sm[3][3][GRAD_PN];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + GRAD_TX * ty;
@@ -1553,7 +1546,8 @@ __global__ void __launch_bounds__(GRAD_TX *GRAD_TY) k_curvature_tile(const T *__
     const int kb = 1 + (int)blockIdx.z * GRAD_KCH;
     const int ke = min(kb + GRAD_KCH - 1, L.nz);
     GradPlanes<T, 3> g;
-    g.src[0] = cnx; g.src[1] = cny; g.src[2] = cnz;
+    g.src[0] = &cn[0].x; g.src[1] = &cn[0].y; g.src[2] = &cn[0].z;
+    g.es = 4;
     g.hx = L.h2x; g.hxy = L.h2xy; g.o = 1 + L.h2x + L.h2xy;
     g.imax = L.nx + 2; g.jmax = L.ny + 2; g.kmax = L.nz + 2;
     T r[3][GRAD_LD];
@@ -1592,8 +1586,7 @@ constexpr int MON_NQ = 10;  // fl1 fl2 vol1 vol2 mass1 mass2 pre | umax usq1 usq
 template <class S>
 __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f, const S *__restrict__ g,
                                                          typename Store<S>::R *__restrict__ phi, const int8_t *__restrict__ walls,
-                                                         const typename Store<S>::R *__restrict__ cnx, const typename Store<S>::R *__restrict__ cny,
-                                                         const typename Store<S>::R *__restrict__ cnz, const typename Store<S>::R *__restrict__ cnorm,
+                                                         const Nrm<typename Store<S>::R> *__restrict__ cn,
                                                          const typename Store<S>::R *__restrict__ curv, double *__restrict__ u,
                                                          double *__restrict__ v, double *__restrict__ w, double *__restrict__ rho,
                                                          double *__restrict__ out, const Layout L, const PdfAt pa,
@@ -1625,10 +1618,11 @@ __global__ void __launch_bounds__(MON_THREADS) k_monitor(const S *__restrict__ f
         const int64_t i1 = L.i1(i, j, k);
         if (multiphase) {
             const int64_t i2 = L.i2(i, j, k);
-            const double tmp = 0.5 * P.gamma * (double)curv[i1] * (double)cnorm[i2];
-            fx = tmp * (double)cnx[i2];
-            fy = tmp * (double)cny[i2];
-            fz = tmp * (double)cnz[i2] + P.force_z;
+            const Nrm<typename Store<S>::R> nr = cn[i2];
+            const double tmp = 0.5 * P.gamma * (double)curv[i1] * (double)nr.n;
+            fx = tmp * (double)nr.x;
+            fy = tmp * (double)nr.y;
+            fz = tmp * (double)nr.z + P.force_z;
         }
         const double uu = (ft[1] - ft[2] + ft[7] - ft[8] + ft[9] - ft[10] + ft[11] - ft[12] + ft[13] - ft[14] - 0.5 * fx) * m;
         const double vv = (ft[3] - ft[4] + ft[7] + ft[8] - ft[9] - ft[10] + ft[15] - ft[16] + ft[17] - ft[18] - 0.5 * fy) * m;
@@ -2505,9 +2499,9 @@ __global__ void k_field_in(T *__restrict__ dst, const double *__restrict__ src, 
 }
 
 template <class T>
-__global__ void k_field_out(double *__restrict__ dst, const T *__restrict__ src, int64_t n) {
+__global__ void k_field_out(double *__restrict__ dst, const T *__restrict__ src, int64_t n, int stride) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) dst[t] = (double)src[t];
+    if (t < n) dst[t] = (double)src[t * stride];
 }
 
 }  // namespace MFLBM_NS

@@ -22,7 +22,7 @@ struct DevState {
     // phase field and colour-gradient fields: double, or float in the multiphase
     // FP32 form (element size felt)
     void *phi;             // halo 4
-    void *cnx, *cny, *cnz, *cnorm;    // halo 2
+    void *cn;                         // halo 2: Nrm<T> records (cn_x, cn_y, cn_z, c_norm)
     void *curv;            // halo 1
     int felt;
     double *u, *v, *w, *rho;          // halo 1, FP64 in every form
@@ -95,9 +95,10 @@ struct KernelTable {
     // FP64 plane <-> storage plane (q of species s) through st.stage
     int (*convert_in)(const DevState &, int species, int q, cudaStream_t);
     int (*convert_out)(const DevState &, int species, int q, cudaStream_t);
-    // FP64 image in st.stage <-> field array (phi, gradient fields) of n elements
+    // FP64 image in st.stage <-> field array (phi, gradient fields) of n elements; field_out
+    // reads every stride-th element (4: one component of the Nrm records)
     int (*field_in)(const DevState &, void *dst, int64_t n, cudaStream_t);
-    int (*field_out)(const DevState &, const void *src, int64_t n, cudaStream_t);
+    int (*field_out)(const DevState &, const void *src, int64_t n, int stride, cudaStream_t);
     // ensembles (fluid-list arena of many singlephase samples), storage by prec:
     // persistent != 0: one cooperative launch of a.nsteps steps on `grid` blocks;
     // else a.nsteps launches of one step each.  Returns kernels launched, -1 on a

@@ -12,6 +12,7 @@ inline dim3 row_block(int nx) {
 }
 
 template <class S> inline S *fs(const DevState &st) { return reinterpret_cast<S *>(st.f); }
+template <class T> inline Nrm<T> *nrm(const DevState &st) { return reinterpret_cast<Nrm<T> *>(st.cn); }
 template <class S> inline S *gs(const DevState &st) { return reinterpret_cast<S *>(st.g); }
 // field arrays (phi, gradient) of the compute type T
 template <class T> inline T *fld(void *p) { return reinterpret_cast<T *>(p); }
@@ -124,12 +125,10 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
         const unsigned nb = (unsigned)((st.nfl + 127) / 128);
         T *f = fs<T>(st), *gg = gs<T>(st);
         if (odd)
-            k_mp_step<T, true, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny),
-                                                        fld<T>(st.cnz), fld<T>(st.cnorm), fld<T>(st.curv), st.cell1,
+            k_mp_step<T, true, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cell1,
                                                         st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
         else
-            k_mp_step<T, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny),
-                                                         fld<T>(st.cnz), fld<T>(st.cnorm), fld<T>(st.curv), st.cell1,
+            k_mp_step<T, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cell1,
                                                          st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
         return 1;
     }
@@ -137,12 +136,10 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     T *f = fs<T>(st), *gg = gs<T>(st);
     if (odd)
-        k_mp_step<T, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny), fld<T>(st.cnz),
-                                              fld<T>(st.cnorm), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
+        k_mp_step<T, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
                                               st.rk_weight2);
     else
-        k_mp_step<T, false><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), fld<T>(st.cnx), fld<T>(st.cny), fld<T>(st.cnz),
-                                               fld<T>(st.cnorm), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
+        k_mp_step<T, false><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
                                                st.rk_weight2);
     return 1;
 }
@@ -153,14 +150,12 @@ int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
         const unsigned nb = (unsigned)((st.nfl + 127) / 128);
         S *f = fs<S>(st), *gg = gs<S>(st);
         if (odd)
-            k_mp_step_ff<true, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx),
-                                                           fld<double>(st.cny), fld<double>(st.cnz), fld<double>(st.cnorm),
+            k_mp_step_ff<true, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), nrm<double>(st),
                                                            fld<double>(st.curv), st.cell1, st.nfl, st.L, st.mpff, st.P.mrt,
                                                            st.nb, st.lstride);
         else
-            k_mp_step_ff<false, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx),
-                                                            fld<double>(st.cny), fld<double>(st.cnz),
-                                                            fld<double>(st.cnorm), fld<double>(st.curv), st.cell1, st.nfl,
+            k_mp_step_ff<false, S, true><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), nrm<double>(st),
+                                                            fld<double>(st.curv), st.cell1, st.nfl,
                                                             st.L, st.mpff, st.P.mrt, st.nb, st.lstride);
         return 1;
     }
@@ -168,12 +163,10 @@ int collide_mp_ff(const DevState &st, bool odd, cudaStream_t s) {
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     S *f = fs<S>(st), *gg = gs<S>(st);
     if (odd)
-        k_mp_step_ff<true, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
-                                             fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
+        k_mp_step_ff<true, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), nrm<double>(st), fld<double>(st.curv), st.cells,
                                              st.ncell, st.L, st.mpff, st.P.mrt);
     else
-        k_mp_step_ff<false, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), fld<double>(st.cnx), fld<double>(st.cny),
-                                              fld<double>(st.cnz), fld<double>(st.cnorm), fld<double>(st.curv), st.cells,
+        k_mp_step_ff<false, S><<<nb, 128, 0, s>>>(f, gg, fld<double>(st.phi), nrm<double>(st), fld<double>(st.curv), st.cells,
                                               st.ncell, st.L, st.mpff, st.P.mrt);
     return 1;
 }
@@ -320,8 +313,8 @@ int boundary(const DevState &st, bool before_odd, int inlet_bc, int outlet_bc, b
 template <class T>
 int color_gradient_t(const DevState &st, cudaStream_t s) {
     const Layout &L = st.L;
-    T *phi = fld<T>(st.phi), *cnx = fld<T>(st.cnx), *cny = fld<T>(st.cny), *cnz = fld<T>(st.cnz);
-    T *cnorm = fld<T>(st.cnorm), *curv = fld<T>(st.curv);
+    T *phi = fld<T>(st.phi), *curv = fld<T>(st.curv);
+    Nrm<T> *cn = nrm<T>(st);
     int n_launch = 2 + (st.ns > 0 ? 2 : 0) + (st.nf > 0 ? 1 : 0);
     if (st.ns > 0) {
         if (st.sbc) k_extrap_phi_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sbc, st.ns, L);
@@ -332,20 +325,18 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         const dim3 b(GRAD_TX, GRAD_TY);
         const dim3 g((L.nx + 4 + GRAD_TX - 1) / GRAD_TX, (L.ny + 4 + GRAD_TY - 1) / GRAD_TY,
                      (L.nz + 4 + GRAD_KCH - 1) / GRAD_KCH);
-        k_normals_tile<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
+        k_normals_tile<T><<<g, b, 0, s>>>(phi, st.walls, cn, L);
     } else if (st.glist) {
         if (st.n_gcell_n > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {
                 if (dw_grad(st)) {
-                    k_normals_list_ff<<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny,
-                                                                                cnz, cnorm, L);
+                    k_normals_list_ff<<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cn, L);
                     done = true;
                 }
             }
             if (!done)
-                k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cnx, cny,
-                                                                            cnz, cnorm, L);
+                k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cn, L);
         }
     } else
 #endif
@@ -354,33 +345,33 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         const int bx = nxh >= 128 ? 128 : ((nxh + 31) / 32) * 32;
         const dim3 b(bx, 256 / bx > 0 ? (unsigned)(256 / bx) : 1u);
         const dim3 g((nxh + b.x - 1) / b.x, (L.ny + 4 + b.y - 1) / b.y, L.nz + 4);
-        k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cnx, cny, cnz, cnorm, L);
+        k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cn, L);
     }
     if (st.nf > 0) {
         const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (dw_grad(st) ? T(1e-12) : T(0.0));
-        k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, cnorm, st.fb, st.nf, L, min_one_m);
+        k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cn, st.fb, st.nf, L, min_one_m);
     }
     if (st.ns > 0) {
-        if (st.sbc) k_extrap_normals_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sbc, st.ns, L);
-        else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cnx, cny, cnz, st.sb, st.ns, L);
+        if (st.sbc) k_extrap_normals_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cn, st.sbc, st.ns, L);
+        else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cn, st.sb, st.ns, L);
     }
 #ifndef MFLBM_STRICT
     if (st.gtile && !dw_grad(st)) {
         const dim3 b(GRAD_TX, GRAD_TY);
         const dim3 g((L.nx + GRAD_TX - 1) / GRAD_TX, (L.ny + GRAD_TY - 1) / GRAD_TY, (L.nz + GRAD_KCH - 1) / GRAD_KCH);
-        k_curvature_tile<T><<<g, b, 0, s>>>(cnx, cny, cnz, curv, st.walls, L);
+        k_curvature_tile<T><<<g, b, 0, s>>>(cn, curv, st.walls, L);
     } else if (st.glist) {
         if (st.n_gcell_c > 0) {
             bool done = false;
             if constexpr (std::is_same<T, double>::value) {
                 if (dw_grad(st)) {
-                    k_curvature_list_ff<<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
+                    k_curvature_list_ff<<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cn, curv, st.gcell_c,
                                                                                   st.n_gcell_c, L);
                     done = true;
                 }
             }
             if (!done)
-                k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cnx, cny, cnz, curv, st.gcell_c,
+                k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cn, curv, st.gcell_c,
                                                                                st.n_gcell_c, L);
         }
     } else
@@ -389,7 +380,7 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         const int bx = L.nx >= 128 ? 128 : ((L.nx + 31) / 32) * 32;
         const dim3 b(bx, 256 / bx);
         const dim3 g((L.nx + b.x - 1) / b.x, (L.ny + b.y - 1) / b.y, L.nz);
-        k_curvature<T><<<g, b, 0, s>>>(cnx, cny, cnz, curv, st.walls, L);
+        k_curvature<T><<<g, b, 0, s>>>(cn, curv, st.walls, L);
     }
     return n_launch;
 }
@@ -414,7 +405,7 @@ int monitor_t(const DevState &st, cudaStream_t s) {
         return 1;
     }
     k_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.multiphase ? gs<S>(st) : nullptr, fld<FT>(st.phi), st.walls,
-                                                 fld<FT>(st.cnx), fld<FT>(st.cny), fld<FT>(st.cnz), fld<FT>(st.cnorm),
+                                                 nrm<FT>(st),
                                                  fld<FT>(st.curv), st.u, st.v, st.w, st.rho, st.mon, st.L, pdf_at(st),
                                                  st.P, st.multiphase, 1, st.ref, st.scale);
     return 1;
@@ -555,10 +546,10 @@ int field_in(const DevState &st, void *dst, int64_t n, cudaStream_t s) {
     return 1;
 }
 
-int field_out(const DevState &st, const void *src, int64_t n, cudaStream_t s) {
+int field_out(const DevState &st, const void *src, int64_t n, int stride, cudaStream_t s) {
     const unsigned nb = (unsigned)((n + 255) / 256);
-    if (st.felt == 4) k_field_out<float><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const float *>(src), n);
-    else k_field_out<double><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const double *>(src), n);
+    if (st.felt == 4) k_field_out<float><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const float *>(src), n, stride);
+    else k_field_out<double><<<nb, 256, 0, s>>>(st.stage, reinterpret_cast<const double *>(src), n, stride);
     return 1;
 }
 
