@@ -412,12 +412,13 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
     };
 
 // Resident blocks per SM (128 threads each) the compiler must allow for the multiphase
-// collision, i.e. its register cap.  FP32: 5 (at most 102 registers, no spills in the
-// fluid-list odd step that preloads its 18 table entries; the sweep 1/4/5/6 gave 0.579 /
-// 0.646 / 0.691 / 0.689 of the roofline on the C3 packing).  FP64: 3 (FP64-pipe bound; 4
-// and above spill).  Tuning parameters: MFLBM_NVCC_FLAGS=-DMFLBM_MP_MIN_BLOCKS_F32=n.
+// collision, i.e. its register cap.  FP32: 6 (at most 80 registers; the fluid-list odd step,
+// which preloads its 18 table entries, spills 36 bytes).  With the normals read as one
+// record, the sweep 4/5/6 gave 0.648 / 0.678 / 0.701 of the roofline on the C3 packing
+// (without them 1/4/5/6: 0.579 / 0.646 / 0.691 / 0.689).  FP64: 3 (FP64-pipe bound; 4 and
+// above spill).  Tuning parameters: MFLBM_NVCC_FLAGS=-DMFLBM_MP_MIN_BLOCKS_F32=n.
 #ifndef MFLBM_MP_MIN_BLOCKS_F32
-#define MFLBM_MP_MIN_BLOCKS_F32 5
+#define MFLBM_MP_MIN_BLOCKS_F32 6
 #endif
 #ifndef MFLBM_MP_MIN_BLOCKS_F64
 #define MFLBM_MP_MIN_BLOCKS_F64 3
