@@ -3,6 +3,7 @@
 // map entries inside the direction arrays, one slot per (solid cell, array) for the links,
 // boundary-plane cells all resolved to a slot, and the neighbour of a fluid node in a
 // boundary plane equal to the slot a boundary condition addresses for that cell.
+#include <algorithm>
 #include <cstdint>
 #include <set>
 #include <string>
@@ -10,7 +11,35 @@
 
 #include "../mf-lbm_gb300/csrc/listlayout.cpp"
 
+static mflbm::MpListLayout g_layout;
+
 extern "C" {
+
+// Builds a layout and keeps it for mph_get.  info: nf, nplane, nlink, stride, spare, map
+// size, nwrap.  Returns -1 when the layout cannot be built.
+int64_t mph_build(const int8_t *walls, int nx, int ny, int nz, int jper, int kper, const int *planes, int nplanes,
+                  const int *ghost_planes, int nghost, int64_t *info) {
+    std::vector<int> pl(planes, planes + nplanes), gp(ghost_planes, ghost_planes + nghost);
+    std::string why;
+    if (!mflbm::build_mp_list_layout(walls, nx, ny, nz, jper, kper, pl, gp, g_layout, why)) return -1;
+    info[0] = g_layout.nf;
+    info[1] = g_layout.nplane;
+    info[2] = g_layout.nlink;
+    info[3] = g_layout.stride;
+    info[4] = g_layout.spare;
+    info[5] = (int64_t)g_layout.map.size();
+    info[6] = g_layout.nwrap;
+    return 0;
+}
+
+// Copies the tables of the last mph_build (sizes from its info).
+void mph_get(int32_t *map, int32_t *nb, int32_t *link, int32_t *cell1, int32_t *wrap) {
+    std::copy(g_layout.map.begin(), g_layout.map.end(), map);
+    std::copy(g_layout.nb.begin(), g_layout.nb.end(), nb);
+    std::copy(g_layout.link.begin(), g_layout.link.end(), link);
+    std::copy(g_layout.cell1.begin(), g_layout.cell1.end(), cell1);
+    std::copy(g_layout.wrap.begin(), g_layout.wrap.end(), wrap);
+}
 
 // Returns the number of failed checks, or -1 when the layout cannot be built.
 int64_t mph_check(const int8_t *walls, int nx, int ny, int nz, int jper, int kper, int open_z, int z_pp, int64_t *nf,

@@ -5,38 +5,20 @@ boundary-plane cell resolved, a boundary-plane neighbour equal to the slot the b
 conditions address, the porous-plate planes' private y ghosts and their exchange list),
 for open and periodic z, periodic and walled y, and a porous plate."""
 import ctypes as C
-import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from cases import random_spheres
+from mplist_lib import host_lib
 from mflbm import geometry
 from mflbm.solver import make_params
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-
-
 @pytest.fixture(scope="module")
 def lib():
-    gxx = shutil.which("g++")
-    inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
-    if gxx is None or not os.path.exists(os.path.join(inc, "cuda_runtime.h")):
+    L = host_lib()
+    if L is None:
         pytest.skip("g++ or the CUDA headers not available")
-    build = os.path.join(HERE, "_build")
-    os.makedirs(build, exist_ok=True)
-    out = os.path.join(build, "libmplist_host.so")
-    tmp = out + f".{os.getpid()}"
-    subprocess.run([gxx, "-O2", "-shared", "-fPIC", "-std=c++17", f"-I{inc}", os.path.join(HERE, "mplist_host.cpp"),
-                    "-o", tmp], check=True)
-    os.replace(tmp, out)
-    L = C.CDLL(out)
-    P64 = C.POINTER(C.c_int64)
-    L.mph_check.restype = C.c_int64
-    L.mph_check.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P64, P64, P64,
-                            P64]
     return L
 
 
