@@ -118,3 +118,29 @@ def test_change_inlet_and_checkpoint_round_trip():
     for k in ("f", "g"):
         assert np.array_equal(out[0][k][:, 1:-1, 1:-1, 1:-1][:, fl], out[1][k][:, 1:-1, 1:-1, 1:-1][:, fl]), k
     assert np.array_equal(out[0]["phi"], out[1]["phi"])
+
+
+def test_plate_on_the_first_plane_with_periodic_y_falls_back_to_dense():
+    """The porous plate's lower plane would be the z = 0 ghost plane, whose periodic-y ghosts
+    the list cannot give private slots: AUTO takes the dense planes, an explicit list request
+    is refused when the geometry is set."""
+    from mflbm import MflbmError
+    from mflbm._capi import LAYOUT_AUTO
+    case = mp_case(strict=0, per=(0, 1, 0), inlet=1, outlet=1, plate=1, zplate=1, layout=LAYOUT_AUTO)
+    with Solver(case["params"]) as sim:
+        load_case(sim, case)
+        assert sim.layout == LAYOUT_DENSE
+    p = copy.copy(case["params"])
+    p.layout = LAYOUT_LIST
+    with Solver(p) as sim:
+        with pytest.raises(MflbmError):
+            sim.set_geometry(case["walls"], case["solid"], case["fluid"], case["w_in"])
+
+
+def test_auto_takes_the_list():
+    from mflbm._capi import LAYOUT_AUTO
+    for name in ("periodic_yz", "porous_plate_blocks_fluid1", "walled_pressure_bcs"):
+        case = mp_case(strict=0, layout=LAYOUT_AUTO, **MP_CASES[name])
+        with Solver(case["params"]) as sim:
+            load_case(sim, case)
+            assert sim.layout == LAYOUT_LIST, name
