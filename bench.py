@@ -41,8 +41,11 @@ import numpy as np  # noqa: E402
 METRIC = "MLUPS (% HBM roofline); time-to-converged permeability, mixed vs FP64 plain"
 BYTES_PER_LU = {0: 19 * 8 * 2 + 1, 1: 19 * 4 * 2 + 1, 2: 19 * 2 * 2 + 1, 3: 19 * 8 * 2 + 1, 4: 19 * 8 * 2 + 1}
 # multiphase collision: 2x19 PDFs read and written, phi written, cn_x/y/z + c_norm + curv read, wall
-BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 5 * 4 + 1,
+BYTES_PER_LU_MP = {0: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 1: 2 * 19 * 4 * 2 + 4 + 4 * 4 + 1,
                    3: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1, 4: 2 * 19 * 8 * 2 + 8 + 5 * 8 + 1}
+# 1: the FP32 collision computes the node's curvature from the normal records around it
+# (the workloads here use the fluid-cell gradient lists), so it reads its own 16-byte
+# record and no curv value; the neighbours' records are other nodes' own records
 # 3: FP64 storage, collision in double-word (two-FP32) arithmetic on the FP32 pipe;
 # 4: double-word storage (hi + lo FP32 pair, 8 bytes) and the double-word collision
 DTYPE = {0: "f64", 1: "f32", 2: "f16", 3: "f64ff", 4: "ff"}
@@ -761,7 +764,9 @@ def main():
     layout = {1: "dense", 2: "list"}.get(sim.layout, "dense")
     sim.close()
     roof = roofline_of(prof, pore, args.precision, bool(p.multiphase), layout, hbm, peak_src)
-    roof["kernel"] = "k_mp_step" if p.multiphase else ("k_sp_list" if layout == "list" else "k_sp_step")
+    mp_kernel = {1: "k_mp_step (curvature fused in)", 3: "k_mp_step_ff", 4: "k_mp_step_ff"}.get(args.precision,
+                                                                                              "k_mp_step")
+    roof["kernel"] = mp_kernel if p.multiphase else ("k_sp_list" if layout == "list" else "k_sp_step")
 
     # ---- every other storage form of the singlephase workload, measured the same way
     forms = None

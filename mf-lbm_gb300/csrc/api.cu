@@ -1119,6 +1119,10 @@ int32_t mflbm_get_gradient(mflbm_ctx *c, double *cn_x, double *cn_y, double *cn_
     if (!c->p.multiphase) return fail(c, MFLBM_EINVAL, "multiphase only");
     const mflbm_params &p = c->p;
     CK(c, cudaSetDevice(c->dev));
+    if (curv) {
+        c->kt->curvature_field(c->st, c->stream);
+        CK(c, cudaPeekAtLastError());
+    }
     CK(c, cudaStreamSynchronize(c->stream));
     double *const dst[5] = {cn_x, cn_y, cn_z, c_norm, curv};
     for (int a = 0; a < 5; ++a) {

@@ -426,7 +426,14 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
 template <class T> struct MpOcc { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F64; };
 template <> struct MpOcc<float> { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F32; };
 
-template <class T, bool ODD, bool LIST = false>
+// curvature of one cell from accessors of cn_x, cn_y, cn_z (defined with the gradient kernels)
+template <class T, class FX, class FY, class FZ>
+__device__ __forceinline__ T curvature_of(FX X, FY Y, FZ Z);
+
+// FUSE: the node's curvature is computed here from the 19 normal records around it (the
+// expression of the curvature kernels, so the same value) instead of read from curv, which
+// the colour-gradient pass then leaves unwritten
+template <class T, bool ODD, bool LIST = false, bool FUSE = false>
 __global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
                                                  const Nrm<T> *__restrict__ cn,
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
@@ -460,7 +467,16 @@ __global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__rest
     phi[L.i4(i, j, k)] = ph;
     const Nrm<T> nr = cn[w2];
     const T cx = nr.x, cy = nr.y, cz = nr.z;
-    T tmp = T(0.5) * T(P.gamma) * curv[L.i1(i, j, k)] * nr.n;
+    T kap;
+    if constexpr (FUSE) {
+        auto X = [&](int a, int b, int c) { return cn[w2 + a + L.h2x * b + L.h2xy * c].x; };
+        auto Y = [&](int a, int b, int c) { return cn[w2 + a + L.h2x * b + L.h2xy * c].y; };
+        auto Z = [&](int a, int b, int c) { return cn[w2 + a + L.h2x * b + L.h2xy * c].z; };
+        kap = curvature_of<T>(X, Y, Z);
+    } else {
+        kap = curv[L.i1(i, j, k)];
+    }
+    T tmp = T(0.5) * T(P.gamma) * kap * nr.n;
     const T fx = tmp * cx;
     const T fy = tmp * cy;
     const T fz = tmp * cz + T(P.force_z);

@@ -117,6 +117,9 @@ struct KernelTable {
     int (*steady)(const DevState &, void *phi_old, double *out, int obs_z, int copy_old, cudaStream_t);
     // change_inlet_fluid_phase over the halo-1 planes k = 0..kmax (cmd 1: into f, 2: into g)
     int (*change_inlet_phase)(const DevState &, int cmd, int kmax, cudaStream_t);
+    // writes the curv field when the collision computes each node's curvature itself
+    // (before get_gradient reads it; the monitor does this on its own); 0 otherwise
+    int (*curvature_field)(const DevState &, cudaStream_t);
 };
 
 const KernelTable *kernels_fast();

@@ -24,6 +24,17 @@ inline bool mp_fp32(const DevState &st) { return st.multiphase && st.prec == MFL
 inline bool dw_grad(const DevState &st) {
     return st.multiphase && (st.prec == MFLBM_FP64FF || st.prec == MFLBM_FF);
 }
+// the FP32 multiphase collision computes each node's curvature from the normal records
+// (default build, fluid-cell gradient lists): the colour-gradient pass skips the curvature
+// kernel, which then runs only before a reader of the curv field (monitor, get_gradient)
+inline bool fused_curvature(const DevState &st) {
+#ifdef MFLBM_STRICT
+    (void)st;
+    return false;
+#else
+    return mp_fp32(st) && st.glist && !st.gtile && st.n_gcell_c > 0;
+#endif
+}
 
 // where the cell-addressed kernels find a population: dense planes, or a fluid list with
 // boundary-plane slots (multiphase; singlephase with an inlet or outlet) through its slot map
@@ -124,17 +135,38 @@ int collide_mp(const DevState &st, bool odd, cudaStream_t s) {
     if (st.mplist) {
         const unsigned nb = (unsigned)((st.nfl + 127) / 128);
         T *f = fs<T>(st), *gg = gs<T>(st);
+        auto *phi = fld<T>(st.phi);
+        auto *cn = nrm<T>(st);
+        auto *curv = fld<T>(st.curv);
+        if (fused_curvature(st)) {
+            if (odd)
+                k_mp_step<T, true, true, true><<<nb, 128, 0, s>>>(f, gg, phi, cn, curv, st.cell1, st.nfl, st.L, st.P,
+                                                                  st.rk_weight2, st.nb, st.lstride);
+            else
+                k_mp_step<T, false, true, true><<<nb, 128, 0, s>>>(f, gg, phi, cn, curv, st.cell1, st.nfl, st.L, st.P,
+                                                                   st.rk_weight2, st.nb, st.lstride);
+            return 1;
+        }
         if (odd)
-            k_mp_step<T, true, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cell1,
-                                                        st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
+            k_mp_step<T, true, true><<<nb, 128, 0, s>>>(f, gg, phi, cn, curv, st.cell1, st.nfl, st.L, st.P,
+                                                        st.rk_weight2, st.nb, st.lstride);
         else
-            k_mp_step<T, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cell1,
-                                                         st.nfl, st.L, st.P, st.rk_weight2, st.nb, st.lstride);
+            k_mp_step<T, false, true><<<nb, 128, 0, s>>>(f, gg, phi, cn, curv, st.cell1, st.nfl, st.L, st.P,
+                                                         st.rk_weight2, st.nb, st.lstride);
         return 1;
     }
     if (st.ncell == 0) return 0;
     const unsigned nb = (unsigned)((st.ncell + 127) / 128);
     T *f = fs<T>(st), *gg = gs<T>(st);
+    if (fused_curvature(st)) {
+        if (odd)
+            k_mp_step<T, true, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv),
+                                                               st.cells, st.ncell, st.L, st.P, st.rk_weight2);
+        else
+            k_mp_step<T, false, false, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv),
+                                                                st.cells, st.ncell, st.L, st.P, st.rk_weight2);
+        return 1;
+    }
     if (odd)
         k_mp_step<T, true><<<nb, 128, 0, s>>>(f, gg, fld<T>(st.phi), nrm<T>(st), fld<T>(st.curv), st.cells, st.ncell, st.L, st.P,
                                               st.rk_weight2);
@@ -370,6 +402,10 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
                     done = true;
                 }
             }
+            if (!done && fused_curvature(st)) {
+                done = true;   // each node's curvature is computed by the next collision
+                --n_launch;
+            }
             if (!done)
                 k_curvature_list<T><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(cn, curv, st.gcell_c,
                                                                                st.n_gcell_c, L);
@@ -383,6 +419,15 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         k_curvature<T><<<g, b, 0, s>>>(cn, curv, st.walls, L);
     }
     return n_launch;
+}
+
+// the curv field for a reader other than the collision, when the collision computes the
+// curvature itself (the colour-gradient pass then leaves curv unwritten)
+int curvature_field(const DevState &st, cudaStream_t s) {
+    if (!fused_curvature(st)) return 0;
+    k_curvature_list<float><<<(st.n_gcell_c + 255) / 256, 256, 0, s>>>(nrm<float>(st), fld<float>(st.curv), st.gcell_c,
+                                                                       st.n_gcell_c, st.L);
+    return 1;
 }
 
 int color_gradient(const DevState &st, cudaStream_t s) {
@@ -404,11 +449,12 @@ int monitor_t(const DevState &st, cudaStream_t s) {
                                                           st.w, st.rho, st.mon, st.P, 1, st.scale);
         return 1;
     }
+    const int nc = st.multiphase ? curvature_field(st, s) : 0;
     k_monitor<S><<<st.L.nz, MON_THREADS, 0, s>>>(fs<S>(st), st.multiphase ? gs<S>(st) : nullptr, fld<FT>(st.phi), st.walls,
                                                  nrm<FT>(st),
                                                  fld<FT>(st.curv), st.u, st.v, st.w, st.rho, st.mon, st.L, pdf_at(st),
                                                  st.P, st.multiphase, 1, st.ref, st.scale);
-    return 1;
+    return 1 + nc;
 }
 
 int monitor(const DevState &st, cudaStream_t s) {
@@ -707,7 +753,7 @@ int change_inlet_phase(const DevState &st, int cmd, int kmax, cudaStream_t s) {
 const KernelTable table = {collide,          wrap,        boundary,   color_gradient, monitor, saturation,
                            init_equilibrium, convert_in,  convert_out, field_in,      field_out,
                            ens_run,          ens_monitor, ens_init,   ens_max_grid,   init_velocity,
-                           steady,           change_inlet_phase};
+                           steady,           change_inlet_phase, curvature_field};
 
 #endif  // MFLBM_PART == 3
 
