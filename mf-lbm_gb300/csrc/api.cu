@@ -491,7 +491,8 @@ void mflbm_destroy(mflbm_ctx *c) {
     delete c;
 }
 
-static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid);
+static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid,
+                          const mflbm_fluid_bnd *fluid, int32_t n_fluid);
 
 int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid,
                            const mflbm_fluid_bnd *fluid, int32_t n_fluid, const double *w_in) {
@@ -706,7 +707,7 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
     c->st.ns = n_solid;
     c->st.nf = n_fluid;
     if (p.multiphase) {
-        int r = gradient_lists(c, walls, solid, n_solid);
+        int r = gradient_lists(c, walls, solid, n_solid, fluid, n_fluid);
         if (r) return r;
     }
     CK(c, cudaDeviceSynchronize());
@@ -720,13 +721,15 @@ int32_t mflbm_set_geometry(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_
 // neighbour list is ascending (the order of the sums is then the set-bit order).  The
 // gradient fields are zeroed: cells the lists skip keep those zeros, as the full-box
 // kernels would write them.
-static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid) {
+static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_bnd *solid, int32_t n_solid,
+                          const mflbm_fluid_bnd *fluid, int32_t n_fluid) {
     const mflbm_params &p = c->p;
     const Layout &L = c->st.L;
     const size_t fe = (size_t)c->st.felt;
     CK(c, cudaMemsetAsync(c->st.cn, 0, 4 * fe * n2(p), c->stream));
     CK(c, cudaMemsetAsync(c->st.curv, 0, fe * n1(p), c->stream));
     c->st.glist = 0;
+    c->st.gwet = 0;
     c->st.n_gcell_n = 0;
     c->st.n_gcell_c = 0;
     c->st.sbc = nullptr;
@@ -747,14 +750,35 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
         else c->st.gtile = frac > kGradientTileFraction ? 1 : 0;
     }
     if (!cell_packable(p.nx, p.ny, p.nz)) return MFLBM_OK;  // the full-box kernels serve
-    std::vector<uint32_t> gn, gc;
+    // The normals list starts with the fluid-boundary nodes in record order when their cells
+    // are distinct fluid cells (the normals kernel then applies the wetting of record t at
+    // entry t); the other cells follow in cell order.
+    std::vector<uint32_t> gn, gc, fbs;
+    bool wet = n_fluid > 0;
+    for (int32_t t = 0; t < n_fluid && wet; ++t) {
+        const mflbm_fluid_bnd &f = fluid[t];
+        if (walls[L.i2(f.ix, f.iy, f.iz)] == 1) wet = false;
+        fbs.push_back(pack_cell(f.ix, f.iy, f.iz));
+    }
+    if (wet) {
+        gn = fbs;
+        std::sort(fbs.begin(), fbs.end());
+        wet = std::adjacent_find(fbs.begin(), fbs.end()) == fbs.end();
+        if (!wet) gn.clear();
+    }
+    if (!wet) fbs.clear();
+    size_t pos = 0;
     for (int k = -1; k <= p.nz + 2; ++k)
         for (int j = -1; j <= p.ny + 2; ++j)
             for (int i = -1; i <= p.nx + 2; ++i) {
                 const int8_t w = walls[L.i2(i, j, k)];
-                if (w != 1) gn.push_back(pack_cell(i, j, k));
+                const uint32_t pc = pack_cell(i, j, k);   // ascending in this loop order
+                if (w != 1) {
+                    while (pos < fbs.size() && fbs[pos] < pc) ++pos;
+                    if (!(pos < fbs.size() && fbs[pos] == pc)) gn.push_back(pc);
+                }
                 if (w == 0 && i >= 1 && i <= p.nx && j >= 1 && j <= p.ny && k >= 1 && k <= p.nz)
-                    gc.push_back(pack_cell(i, j, k));
+                    gc.push_back(pc);
             }
     auto put = [&](const std::vector<uint32_t> &v, const uint32_t **dst, int64_t &cap) -> int {
         if (v.empty()) return MFLBM_OK;
@@ -774,6 +798,7 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     c->st.n_gcell_n = (int)gn.size();
     c->st.n_gcell_c = (int)gc.size();
     c->st.glist = 1;
+    c->st.gwet = wet ? 1 : 0;
     std::vector<SolidBndC> sc((size_t)n_solid);
     for (int32_t t = 0; t < n_solid; ++t) {
         const mflbm_solid_bnd &s = solid[t];

@@ -399,14 +399,18 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
         (void)nbr;                                                                                  \
     }                                                                                               \
     auto src = [&](int q) -> int64_t {                                                              \
-        if constexpr (LIST)                                                                         \
-            return ODD ? (q == 0 ? c : (int64_t)q * stride + nbr[OPP(q) - 1]) : (int64_t)OPP(q) * stride + c; \
+        if constexpr (LIST && ODD)                                                                  \
+            return q == 0 ? c : (int64_t)q * stride + nbr[OPP(q) - 1];                             \
+        else if constexpr (LIST)                                                                    \
+            return (int64_t)OPP(q) * stride + c;                                                    \
         else                                                                                        \
             return ODD ? (int64_t)q * L.qs + c - qoff(L, q) : (int64_t)OPP(q) * L.qs + c;           \
     };                                                                                              \
     auto dst = [&](int q) -> int64_t {                                                              \
-        if constexpr (LIST)                                                                         \
-            return ODD ? (int64_t)OPP(q) * stride + nbr[q - 1] : (int64_t)q * stride + c;           \
+        if constexpr (LIST && ODD)                                                                  \
+            return (int64_t)OPP(q) * stride + nbr[q - 1];                                           \
+        else if constexpr (LIST)                                                                    \
+            return (int64_t)q * stride + c;                                                         \
         else                                                                                        \
             return ODD ? (int64_t)OPP(q) * L.qs + c + qoff(L, q) : (int64_t)q * L.qs + c;           \
     };
@@ -1228,6 +1232,8 @@ __global__ void MFLBM_EXTRAP_BOUNDS k_extrap_normals_c(Nrm<T> *__restrict__ cn, 
     cn[id].z = az / lw;
 }
 
+#include "wetting.cuh"
+
 // ISO4 gradient and unit normal from a phi accessor P(a, b, c) = phi at offset (a, b, c)
 // (:33-79); shared by the global-memory and shared-memory forms
 template <class T, class PA>
@@ -1285,14 +1291,34 @@ __global__ void __launch_bounds__(256) k_normals(const T *__restrict__ phi, cons
 // and solid-boundary cells receive their extrapolated normals as before.  At porosity 0.22
 // this skips about two thirds of the cells, and every lane of a warp does work.
 
-template <class T>
+// WET: the list starts with the nwet fluid-boundary nodes in record order; entry t < nwet
+// applies the geometric wetting of record fb[t] to the normal it has just computed (the
+// wetting kernel's operations on the same values, so it is not launched)
+template <class T, bool WET = false>
 __global__ void MFLBM_GRAD_BOUNDS k_normals_list(const T *__restrict__ phi, const uint32_t *__restrict__ cl, int n,
-                                                      Nrm<T> *__restrict__ cn, const Layout L) {
+                                                      Nrm<T> *__restrict__ cn, const Layout L,
+                                                      const FluidBnd *__restrict__ fb = nullptr, int nwet = 0,
+                                                      T min_one_m = T(0.0)) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i, j, k;
     unpack_cell(cl[t], i, j, k);
-    normals_at<T>(phi, i, j, k, L.i2(i, j, k), cn, L);
+    if constexpr (WET) {
+        auto P = [&](int a, int b, int c) { return phi[L.i4(i + a, j + b, k + c)]; };
+        T gx, gy, gz, c;
+        normals_of<T>(P, gx, gy, gz, c);
+        if (t < nwet && c > T(1e-6)) {
+            const FluidBnd b = fb[t];
+            T nn[3] = {gx, gy, gz};
+            wetting_normal<T>(nn, T(b.nwx), T(b.nwy), T(b.nwz), T(b.cos_t), T(b.sin_t), min_one_m);
+            gx = nn[0];
+            gy = nn[1];
+            gz = nn[2];
+        }
+        cn[L.i2(i, j, k)] = Nrm<T>{gx, gy, gz, c};
+    } else {
+        normals_at<T>(phi, i, j, k, L.i2(i, j, k), cn, L);
+    }
 }
 
 // The two stencils of the double-word form (MFLBM_FP64FF, multiphase): FP64 fields split on
@@ -1360,7 +1386,6 @@ __global__ void __launch_bounds__(256) k_curvature_list_ff(const Nrm<double> *__
 }
 
 // geometric wetting at fluid-boundary nodes (alter_color_gradient_solid_surface, :210-265)
-#include "wetting.cuh"
 
 template <class T>
 __global__ void k_wetting(Nrm<T> *__restrict__ cn, const FluidBnd *__restrict__ fb, int nf, const Layout L,

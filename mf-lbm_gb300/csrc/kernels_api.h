@@ -38,6 +38,9 @@ struct DevState {
     int n_gcell_n;
     const uint32_t *gcell_c;  // fluid cells of [1, n]^3 (walls == 0), packed: curvature
     int n_gcell_c;
+    int gwet;                 // 1: gcell_n starts with the fluid-boundary nodes in record
+                              // order (entry t < nf is record t), so the normals kernel applies
+                              // the wetting itself; 0: the separate wetting kernel
     int ns;
     const FluidBnd *fb;
     int nf;

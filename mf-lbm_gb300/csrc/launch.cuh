@@ -348,6 +348,8 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
     T *phi = fld<T>(st.phi), *curv = fld<T>(st.curv);
     Nrm<T> *cn = nrm<T>(st);
     int n_launch = 2 + (st.ns > 0 ? 2 : 0) + (st.nf > 0 ? 1 : 0);
+    const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (dw_grad(st) ? T(1e-12) : T(0.0));
+    bool wet_done = false;   // the normals kernel applied the wetting
     if (st.ns > 0) {
         if (st.sbc) k_extrap_phi_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sbc, st.ns, L);
         else k_extrap_phi<T><<<(st.ns + 127) / 128, 128, 0, s>>>(phi, st.sb, st.ns, L);
@@ -367,6 +369,11 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
                     done = true;
                 }
             }
+            if (!done && st.gwet) {
+                k_normals_list<T, true><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cn, L,
+                                                                                   st.fb, st.nf, min_one_m);
+                done = wet_done = true;
+            }
             if (!done)
                 k_normals_list<T><<<(st.n_gcell_n + 255) / 256, 256, 0, s>>>(phi, st.gcell_n, st.n_gcell_n, cn, L);
         }
@@ -379,10 +386,8 @@ int color_gradient_t(const DevState &st, cudaStream_t s) {
         const dim3 g((nxh + b.x - 1) / b.x, (L.ny + 4 + b.y - 1) / b.y, L.nz + 4);
         k_normals<T><<<g, b, 0, s>>>(phi, st.walls, cn, L);
     }
-    if (st.nf > 0) {
-        const T min_one_m = sizeof(T) == 4 ? T(1e-6) : (dw_grad(st) ? T(1e-12) : T(0.0));
-        k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cn, st.fb, st.nf, L, min_one_m);
-    }
+    if (st.nf > 0 && !wet_done) k_wetting<T><<<(st.nf + 127) / 128, 128, 0, s>>>(cn, st.fb, st.nf, L, min_one_m);
+    if (wet_done) --n_launch;
     if (st.ns > 0) {
         if (st.sbc) k_extrap_normals_c<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cn, st.sbc, st.ns, L);
         else k_extrap_normals<T><<<(st.ns + 127) / 128, 128, 0, s>>>(cn, st.sb, st.ns, L);
