@@ -730,6 +730,12 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     CK(c, cudaMemsetAsync(c->st.curv, 0, fe * n1(p), c->stream));
     c->st.glist = 0;
     c->st.gwet = 0;
+    // MFLBM_SPLIT_GRADIENT=1 (a diagnostic switch, for comparisons): curvature and wetting in
+    // their own kernels instead of inside the collision and the normals kernel
+    {
+        const char *sp = std::getenv("MFLBM_SPLIT_GRADIENT");
+        c->st.gsplit = (sp && *sp && std::strcmp(sp, "0") != 0) ? 1 : 0;
+    }
     c->st.n_gcell_n = 0;
     c->st.n_gcell_c = 0;
     c->st.sbc = nullptr;
@@ -754,7 +760,7 @@ static int gradient_lists(mflbm_ctx *c, const int8_t *walls, const mflbm_solid_b
     // are distinct fluid cells (the normals kernel then applies the wetting of record t at
     // entry t); the other cells follow in cell order.
     std::vector<uint32_t> gn, gc, fbs;
-    bool wet = n_fluid > 0;
+    bool wet = n_fluid > 0 && !c->st.gsplit;
     for (int32_t t = 0; t < n_fluid && wet; ++t) {
         const mflbm_fluid_bnd &f = fluid[t];
         if (walls[L.i2(f.ix, f.iy, f.iz)] == 1) wet = false;

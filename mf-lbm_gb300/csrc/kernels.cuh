@@ -1429,10 +1429,37 @@ __global__ void k_extrap_normals(Nrm<T> *__restrict__ cn,
     cn[id].z = az / lw;
 }
 
-// curvature of one cell (:113-201)
+// FP32 arithmetic with every operation rounded on its own (never contracted into an FMA), so
+// an expression gives the same bits in every kernel it is inlined into: the curvature is
+// computed both inside the FP32 collision and by its own kernel (for the monitor and
+// get_gradient), and the value a reader sees is the one the collision used
+struct rnf {
+    float v;
+    __device__ __forceinline__ rnf(float f) : v(f) {}
+    __device__ __forceinline__ explicit rnf(double d) : v((float)d) {}
+};
+__device__ __forceinline__ rnf operator+(rnf a, rnf b) { return rnf(__fadd_rn(a.v, b.v)); }
+__device__ __forceinline__ rnf operator-(rnf a, rnf b) { return rnf(__fsub_rn(a.v, b.v)); }
+__device__ __forceinline__ rnf operator*(rnf a, rnf b) { return rnf(__fmul_rn(a.v, b.v)); }
+
 // curvature from accessors X, Y, Z of cn_x, cn_y, cn_z at offset (a, b, c) (:113-201)
 template <class T, class FX, class FY, class FZ>
+__device__ __forceinline__ T curvature_expr(FX X, FY Y, FZ Z);
+
+template <class T, class FX, class FY, class FZ>
 __device__ __forceinline__ T curvature_of(FX X, FY Y, FZ Z) {
+    if constexpr (std::is_same<T, float>::value) {
+        auto Xr = [&](int a, int b, int c) { return rnf(X(a, b, c)); };
+        auto Yr = [&](int a, int b, int c) { return rnf(Y(a, b, c)); };
+        auto Zr = [&](int a, int b, int c) { return rnf(Z(a, b, c)); };
+        return curvature_expr<rnf>(Xr, Yr, Zr).v;
+    } else {
+        return curvature_expr<T>(X, Y, Z);
+    }
+}
+
+template <class T, class FX, class FY, class FZ>
+__device__ __forceinline__ T curvature_expr(FX X, FY Y, FZ Z) {
     const T c1 = T(ISO4_1), c2 = T(ISO4_2);
     const T kxx = c1 * (X(1, 0, 0) - X(-1, 0, 0)) +
                        c2 * (X(1, 1, 0) - X(-1, -1, 0) + X(1, -1, 0) - X(-1, 1, 0) + X(1, 0, 1) - X(-1, 0, -1) + X(1, 0, -1) - X(-1, 0, 1));

@@ -32,6 +32,7 @@ struct DevState {
     const SolidBnd *sb;
     const SolidBndC *sbc;     // compact form of sb (nullptr: a neighbour list is not ascending)
     int glist;                // 1: the packed fluid-cell lists below are valid
+    int gsplit;               // 1: curvature and wetting in their own kernels (MFLBM_SPLIT_GRADIENT)
     int gtile;                // 1: normals and curvature by the shared-memory plane-marching
                               //    kernels (default build; the double-word form keeps the lists)
     const uint32_t *gcell_n;  // fluid cells of [-1, n+2]^3 (walls != 1), packed: normals

@@ -32,7 +32,7 @@ inline bool fused_curvature(const DevState &st) {
     (void)st;
     return false;
 #else
-    return mp_fp32(st) && st.glist && !st.gtile && st.n_gcell_c > 0;
+    return mp_fp32(st) && st.glist && !st.gtile && !st.gsplit && st.n_gcell_c > 0;
 #endif
 }
 
