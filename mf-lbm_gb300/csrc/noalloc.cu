@@ -34,7 +34,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxDevices = 64;
 
-__device__ __align__(256) double g_noalloc_slices[2 * MFLBM_NOALLOC_MAX_NZ];
+static __device__ __align__(256) double g_noalloc_slices[2 * MFLBM_NOALLOC_MAX_NZ];
 
 // per-slice sums of 0.5(1+phi)(1-w) and 0.5(1-phi)(1-w) (Monitor.F90:526-538)
 __global__ void __launch_bounds__(kThreads) k_sat_slices(const double *__restrict__ phi, const int8_t *__restrict__ walls,
