@@ -179,7 +179,7 @@ int32_t mflbm_ensemble_create(const mflbm_params *common, int32_t nsamples, cons
     e->dims.assign(dims, dims + 3 * nsamples);
     e->active.assign((size_t)nsamples, 1);
     e->elt = common->precision == MFLBM_FP32 ? 4 : (common->precision == MFLBM_FP16 ? 2 : 8);
-    e->kt = kernels_fast();
+    e->kt = common->strict_fp ? kernels_strict() : kernels_fast();   // strict: no FMA contraction
     int r = MFLBM_OK;
     // arena: fluid nodes of all samples, then the link slots of all samples per direction
     std::vector<int64_t> lbase((size_t)19 * nsamples, 0);

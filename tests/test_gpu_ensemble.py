@@ -1,5 +1,5 @@
 """Ensembles: samples of uneven sizes in one arena against independent single-sample
-runs of the same geometry.
+runs of the same geometry, on the GPU and on the oracle.
 
 Same arithmetic as the single-sample fluid-list sweep, so the per-sample flow sums agree
 to summation order (rtol 1e-12); persistent and per-step launch shapes agree exactly;
@@ -45,6 +45,34 @@ def test_flux_matches_single_sample_runs():
     assert st == 0
     for s in range(len(case["samples"])):
         np.testing.assert_allclose(w[s], _single_flux(case, s, 24), rtol=1e-12)
+
+
+@pytest.mark.parametrize("strict", [1, 0])
+def test_flux_matches_oracle(strict):
+    """Every sample of one arena against the oracle's run of that sample alone: strict build
+    (no FMA contraction, the populations bit-identical to the oracle's) to summation order,
+    rtol 1e-12; default build within 1e-10."""
+    import copy
+    from pyoracle import Oracle
+    case = _ens()
+    p = copy.copy(case["params"])
+    p.strict_fp = strict
+    with Ensemble(p, case["samples"]) as ens:
+        ens.init()
+        ens.run(1, 24)
+        w, _, st = ens.flux()
+    assert st == 0
+    for s, (nx, ny, nz, walls) in enumerate(case["samples"]):
+        ps = copy.copy(p)
+        ps.nx, ps.ny, ps.nz = nx, ny, nz
+        orc = Oracle(ps)
+        orc.set_geometry(walls)
+        orc.init_equilibrium()
+        orc.run(1, 24)
+        prof, _, ost = orc.monitor()
+        orc.close()
+        assert ost == 0
+        np.testing.assert_allclose(w[s], prof[0].sum(), rtol=1e-12 if strict else 1e-10)
 
 
 @pytest.mark.parametrize("precision", [0, 1, 3, 4])
