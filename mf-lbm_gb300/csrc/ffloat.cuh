@@ -138,6 +138,27 @@ __device__ __forceinline__ ff ff_from_f64(double d) {
     return ff{__uint_as_float(hb | sgn), __uint_as_float(__float_as_uint(lo) | sgn)};
 }
 
+// ff_from_f64 without its range selects, for |d| in [2^-103, 2^128) (biased FP64
+// exponents 920..1150), where it returns the same hi and lo.  `span` collects
+// max(biased exponent - 920) over the values split: a span above kFfInRangeSpan means one
+// of them lay outside the range and its result is meaningless (split it again with
+// ff_from_f64).  Populations of a running simulation always lie inside, so a collision
+// sweep splits its 19 loads this way and takes the general split only on that rare span.
+constexpr unsigned kFfInRangeSpan = 230u;
+__device__ __forceinline__ ff ff_from_f64_in_range(double d, unsigned &span) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const unsigned sgn = hw & 0x80000000u;
+    const unsigned a = hw & 0x7fffffffu;
+    const unsigned ed = a >> 20;
+    span = span > ed - 920u ? span : ed - 920u;
+    const unsigned hb = __funnelshift_l(lw, a - (896u << 20), 3);
+    const unsigned m = ((lw >> 6) & 0x7fffffu) + ((lw >> 5) & 1u);
+    const unsigned eb = (ed - 919u) << 23;
+    const float lo = __fsub_rn(__uint_as_float(eb + m), __uint_as_float(eb));
+    return ff{__uint_as_float(hb | sgn), __uint_as_float(__float_as_uint(lo) | sgn)};
+}
+
 // FP32 -> FP64 exactly on the integer pipe (selects only): normal numbers exactly, zero and
 // FP32 subnormals (below 2^-126) as a signed zero, infinities and NaN kept
 __device__ __forceinline__ double f64_of_f32(float x) {

@@ -195,6 +195,31 @@ __device__ __forceinline__ void st_sweep(S *p, int64_t o, int q, typename Store<
     else Store<S>::st(p, o, v, R(WREST(q)), sc);
 }
 
+// the 19 loads of one node's collision, slot of population q at addr(q).  FP64 storage
+// split for the double-word collision (f64ff): the select-free split of the common range,
+// and, if any population lies outside it, all 19 read again and split by the general
+// form (nothing has been written yet, so the second read sees the same values).
+template <class S, class Addr>
+__device__ __forceinline__ void ld_node(typename Store<S>::RS (&ft)[19], const S *p, Addr addr,
+                                        typename Store<S>::RS inv) {
+    if constexpr (std::is_same<S, f64ff>::value) {
+        unsigned span = 0u;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = ff_from_f64_in_range(p[addr(q)].v, span);
+        if (__builtin_expect(span > kFfInRangeSpan, 0)) {
+            // a pointer the compiler cannot equate with p, so the first loads are not kept
+            // live for this path
+            const S *p2 = p;
+            asm volatile("" : "+l"(p2) : "r"(span));
+#pragma unroll
+            for (int q = 0; q < 19; ++q) ft[q] = ff_from_f64(p2[addr(q)].v);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(p, addr(q), q, inv);
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // MRT collision, the "MRT kernel, repeated part" of the reference
 // (multiphase_3D/0.src/Kernel_multiphase.F90:158-267, singlephase Kernel.F90:60-169),
@@ -333,13 +358,9 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
     const int64_t c = cells[t];
     const R inv_scale = R(1.0f / scale);
     R ft[19];
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-        if (ODD)
-            ft[q] = ld_sweep<S>(f, (int64_t)q * L.qs + c - qoff(L, q), q, inv_scale);
-        else
-            ft[q] = ld_sweep<S>(f, (int64_t)OPP(q) * L.qs + c, q, inv_scale);
-    }
+    ld_node<S>(ft, f, [&](int q) -> int64_t {
+        return ODD ? (int64_t)q * L.qs + c - qoff(L, q) : (int64_t)OPP(q) * L.qs + c;
+    }, inv_scale);
     if constexpr (std::is_same<R, ff>::value) {
         mrt_collide_ff<UNIT>(ft, cf);
     } else {
@@ -420,15 +441,23 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
 // which preloads its 18 table entries, spills 36 bytes).  With the normals read as one
 // record, the sweep 4/5/6 gave 0.648 / 0.678 / 0.701 of the roofline on the C3 packing
 // (without them 1/4/5/6: 0.579 / 0.646 / 0.691 / 0.689).  FP64: 3 (FP64-pipe bound; 4 and
-// above spill).  Tuning parameters: MFLBM_NVCC_FLAGS=-DMFLBM_MP_MIN_BLOCKS_F32=n.
+// above spill).  The FP32 even step, which computes the curvature from the normal records
+// (fused) and has no neighbour table, takes its own cap: 5 blocks (96 registers) against
+// 4 / 6 / 7 gave C3 256^2 x 320 FP32 8,841 against 8,739 / 8,722 / 8,704 MLUPS with the odd
+// step at 6.  Tuning parameters: MFLBM_NVCC_FLAGS=-DMFLBM_MP_MIN_BLOCKS_F32=n (odd step),
+// -DMFLBM_MP_MIN_BLOCKS_F32_EVEN=n.
 #ifndef MFLBM_MP_MIN_BLOCKS_F32
 #define MFLBM_MP_MIN_BLOCKS_F32 6
 #endif
 #ifndef MFLBM_MP_MIN_BLOCKS_F64
 #define MFLBM_MP_MIN_BLOCKS_F64 3
 #endif
-template <class T> struct MpOcc { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F64; };
-template <> struct MpOcc<float> { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F32; };
+#ifndef MFLBM_MP_MIN_BLOCKS_F32_EVEN
+#define MFLBM_MP_MIN_BLOCKS_F32_EVEN 5
+#endif
+template <class T, bool ODD> struct MpOcc { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F64; };
+template <> struct MpOcc<float, true> { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F32; };
+template <> struct MpOcc<float, false> { static constexpr int kMinBlocks = MFLBM_MP_MIN_BLOCKS_F32_EVEN; };
 
 // curvature of one cell from accessors of cn_x, cn_y, cn_z (defined with the gradient kernels)
 template <class T, class FX, class FY, class FZ>
@@ -438,7 +467,7 @@ __device__ __forceinline__ T curvature_of(FX X, FY Y, FZ Z);
 // expression of the curvature kernels, so the same value) instead of read from curv, which
 // the colour-gradient pass then leaves unwritten
 template <class T, bool ODD, bool LIST = false, bool FUSE = false>
-__global__ void __launch_bounds__(128, MpOcc<T>::kMinBlocks) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
+__global__ void __launch_bounds__(128, MpOcc<T, ODD>::kMinBlocks) k_mp_step(T *__restrict__ f, T *__restrict__ g, T *__restrict__ phi,
                                                  const Nrm<T> *__restrict__ cn,
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
                                                  const int ncell, const Layout L, const StepParams P, const double rk_weight2,
@@ -1895,9 +1924,8 @@ __device__ __forceinline__ void sp_list_odd_node(S *__restrict__ A, const int64_
     using R = typename Store<S>::RS;
     const R inv_scale = R(1.0f / scale);
     R ft[19];
-    ft[0] = ld_sweep<S>(A, t, 0, inv_scale);
-#pragma unroll
-    for (int q = 1; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)q * stride + nbr[OPP(q) - 1], q, inv_scale);
+    ld_node<S>(ft, A, [&](int q) -> int64_t { return q == 0 ? t : (int64_t)q * stride + nbr[OPP(q) - 1]; },
+               inv_scale);
     sp_collide<S, UNIT>(ft, P, cf);
     const R sc = R(scale);
     st_sweep<S>(A, t, 0, ft[0], sc);
@@ -1919,8 +1947,7 @@ __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t st
         using R = typename Store<S>::RS;
         const R inv_scale = R(1.0f / scale);
         R ft[19];
-#pragma unroll
-        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(A, (int64_t)OPP(q) * stride + t, q, inv_scale);
+        ld_node<S>(ft, A, [&](int q) -> int64_t { return (int64_t)OPP(q) * stride + t; }, inv_scale);
         sp_collide<S, UNIT>(ft, P, cf);
         const R sc = R(scale);
 #pragma unroll
@@ -2032,8 +2059,7 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
             break;
         }
         R ft[19];
-#pragma unroll
-        for (int q = 0; q < 19; ++q) ft[q] = ld_sweep<S>(buf, (int64_t)OPP(q) * kTmaNodes + tid, q, inv_scale);
+        ld_node<S>(ft, buf, [&](int q) -> int64_t { return (int64_t)OPP(q) * kTmaNodes + tid; }, inv_scale);
         sp_collide<S, UNIT>(ft, P, cf);
 #pragma unroll
         for (int q = 0; q < 19; ++q) st_sweep<S>(buf, (int64_t)q * kTmaNodes + tid, q, ft[q], sc);

@@ -16,6 +16,16 @@ void ffh_from_f64(const double *d, float *hi, float *lo, int n) {
         lo[i] = x.lo;
     }
 }
+// the select-free split: per value its (hi, lo) and whether its span passed
+void ffh_from_f64_in_range(const double *d, float *hi, float *lo, int *inside, int n) {
+    for (int i = 0; i < n; ++i) {
+        unsigned span = 0u;
+        const ff x = mflbm::ff_from_f64_in_range(d[i], span);
+        hi[i] = x.hi;
+        lo[i] = x.lo;
+        inside[i] = span <= mflbm::kFfInRangeSpan;
+    }
+}
 void ffh_to_f64(const float *hi, const float *lo, double *d, int n) {
     for (int i = 0; i < n; ++i) d[i] = mflbm::f64_of_ff(ff{hi[i], lo[i]});
 }

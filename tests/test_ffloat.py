@@ -36,6 +36,7 @@ def lib():
     L = C.CDLL(out)
     P = np.ctypeslib.ndpointer
     L.ffh_from_f64.argtypes = [P(np.float64), P(np.float32), P(np.float32), C.c_int]
+    L.ffh_from_f64_in_range.argtypes = [P(np.float64), P(np.float32), P(np.float32), P(np.int32), C.c_int]
     L.ffh_to_f64.argtypes = [P(np.float32), P(np.float32), P(np.float64), C.c_int]
     L.ffh_f32_to_f64.argtypes = [P(np.float32), P(np.float64), C.c_int]
     L.ffh_op.argtypes = [C.c_int] + [P(np.float32)] * 6 + [C.c_int]
@@ -86,6 +87,26 @@ def test_split_special_values(lib):
     assert hi[3] == 0.0 and np.signbit(hi[3])                         # below 2^-126: signed zero
     assert np.isposinf(hi[4]) and np.isposinf(hi[5]) and np.isneginf(hi[6]) and np.isnan(hi[7]) and np.isnan(hi[8])
     assert hi[9] == np.float32(2.0 ** -126) and hi[10] == 0.0
+
+
+def test_in_range_split_matches_general_split(lib):
+    """The select-free split of the sweeps: bit-identical hi and lo for every |d| in
+    [2^-103, 2^128), and every value outside that range reported (zero, subnormals, tiny,
+    huge, infinities, NaN), so the sweep falls back to the general split for it."""
+    rng = np.random.default_rng(7)
+    inside = np.concatenate([rand_doubles(rng, 4000, -30, 30), rng.random(1000) * 0.3, 1 / 3 + 1e-9 * rng.random(500),
+                             [2.0 ** -103, -(2.0 ** -103), np.nextafter(2.0 ** 128, 0), 1.0, -1.0]])
+    outside = np.array([0.0, -0.0, 2.0 ** -103 * (1 - 2.0 ** -52), 1e-35, -1e-40, 5e-324, 2.0 ** 128, 1e300,
+                        np.inf, -np.inf, np.nan, -np.nan])
+    d = np.concatenate([inside, outside])
+    hi, lo = np.empty(d.size, np.float32), np.empty(d.size, np.float32)
+    ok = np.empty(d.size, np.int32)
+    lib.ffh_from_f64_in_range(d, hi, lo, ok, d.size)
+    ghi, glo = split(lib, d)
+    n = inside.size
+    assert ok[:n].all() and not ok[n:].any()
+    assert np.array_equal(hi[:n].view(np.uint32), ghi[:n].view(np.uint32))
+    assert np.array_equal(lo[:n].view(np.uint32), glo[:n].view(np.uint32))
 
 
 def test_f32_to_f64_exact(lib):
