@@ -13,11 +13,12 @@
 // expression left to right exactly as written in the Fortran, so it is bit-identical
 // to any IEEE-754 FP64 implementation that keeps that order (the GPU "strict" build).
 //
-// Parity pinning: the reference ships no golden vectors, tests or fixtures (its
-// test_suites/ hold only input decks).  The oracle is therefore pinned by the
-// restatement itself plus analytic known-answer properties that the reference's own
-// decks are built around (rest state, mass conservation, Poiseuille duct flow,
-// Laplace drop); see tests/test_oracle_*.py.
+// Parity unpinned: the reference ships no golden vectors, tests or fixtures (its
+// test_suites/ hold only input decks), and it cannot be run here to produce outputs.
+// The oracle is therefore pinned only by the restatement itself plus analytic
+// known-answer properties that the reference's own decks are built around (rest state,
+// mass conservation, Poiseuille duct flow, Laplace drop, static contact angle); see
+// tests/test_oracle_*.py and tests/test_kat_oracle.py.
 //
 // Single-rank semantics of the reference's MPI halo exchange: with one rank and a
 // periodic direction the Cartesian communicator sends each halo message to the rank
