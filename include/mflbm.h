@@ -292,7 +292,7 @@ int32_t mflbm_saturation_noalloc(const double *phi, const int8_t *walls, int32_t
  * Ensembles: many singlephase samples of uneven sizes updated together in one
  * fluid-list arena (no counterpart in the reference, which runs one sample per job).
  * The samples share `common` (precision, mrt, la_nu1, force_z, periodic and wall flags,
- * device; nx/ny/nz are ignored) and each has its own dims[3*s..3*s+2] = nx, ny, nz and
+ * strict_fp, device; nx/ny/nz are ignored) and each has its own dims[3*s..3*s+2] = nx, ny, nz and
  * halo-2 wall array walls[s] (Fortran order, 1 = solid).  Every direction must be
  * periodic or walled (no inlet/outlet).  Errors: mflbm_ensemble_last_error.
  * --------------------------------------------------------------------------------- */
