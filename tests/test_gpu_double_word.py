@@ -88,6 +88,38 @@ def test_strict_and_default_builds_identical(name, precision):
     assert np.array_equal(out[0][:, fl], out[1][:, fl])
 
 
+@pytest.mark.parametrize("name", ["list_unit_rates", "dense_unit_rates"])
+def test_fp64_storage_split_of_zero_and_tiny_populations(name):
+    """FP64 storage with the double-word collision splits a node's 19 loads with the
+    select-free split of the range [2^-103, 2^128) and reads them again through the general
+    split when one lies outside it.  Nodes holding an exact zero, a value below 2^-103 and
+    one below the FP32 range take that second path; every node must still track the FP64
+    oracle to rounding noise after one and two steps."""
+    kw = dict(CASES[name])
+    layout = kw.pop("layout")
+    case = sp_case(rest="mrt", precision=MFLBM_FP64FF, strict=0, layout=layout, **kw)
+    fl = _fluid(case)
+    k, j, i = np.nonzero(fl)
+    f = case["f"].copy()
+    for n, (q, v) in enumerate([(3, 0.0), (7, 1e-35), (12, -1e-40), (0, 0.0), (18, 3e-33), (5, -0.0)]):
+        f[q, k[5 * n] + 1, j[5 * n] + 1, i[5 * n] + 1] = v
+    case["f"] = periodic_ghosts(f, kw["per"])
+    for steps in (1, 2):
+        with Solver(case["params"]) as gpu:
+            load_case(gpu, case)
+            gpu.run(1, steps)
+            a = _inner(gpu.download_state()["f"])
+        orc = Oracle(case["params"])
+        load_case(orc, case)
+        orc.run(1, steps)
+        b = _inner(orc.download_state()["f"])
+        orc.close()
+        err = np.abs(a[:, fl] - b[:, fl]).max()
+        print(f"{name} steps {steps}: max |df| {err:.3e}")
+        assert np.isfinite(a[:, fl]).all()
+        assert err <= 2e-14 * (steps + 1)
+
+
 def test_double_word_storage_round_trip():
     """Upload then download without a step: every population back within 2^-46 relative
     (split to 47 bits, joined by one FP64 add)."""
