@@ -391,6 +391,19 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_step(S *__r
 // CSF force, viscosity interpolation in 1/nu, R-K recolouring into f (fluid 1) and
 // g (fluid 2), phi written for the gradient pass.
 // ---------------------------------------------------------------------------------
+// The fluid-list even steps walk the nodes from the last to the first, the odd steps from
+// the first to the last: each sweep starts on the nodes the previous one touched last,
+// whose slots are still in L2.  Only the order of independent node updates changes.
+#ifndef MFLBM_EVEN_REVERSE
+#define MFLBM_EVEN_REVERSE 1
+#endif
+// the list node of this thread: block order reversed on even steps
+template <bool ODD>
+__device__ __forceinline__ int list_node_index() {
+    const int b = (!ODD && MFLBM_EVEN_REVERSE) ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
+    return b * (int)blockDim.x + (int)threadIdx.x;
+}
+
 // T = double: the FP64 drop-in; T = float: the mixed form (FP32 storage of f, g, phi
 // and the gradient fields, FP32 arithmetic).
 // The node of a multiphase collision thread and the slots of its populations: the dense
@@ -472,7 +485,7 @@ __global__ void __launch_bounds__(128, MpOcc<T, ODD>::kMinBlocks) k_mp_step(T *_
                                                  const T *__restrict__ curv, const int32_t *__restrict__ cells,
                                                  const int ncell, const Layout L, const StepParams P, const double rk_weight2,
                                                  const int32_t *__restrict__ nb = nullptr, const int64_t stride = 0) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = LIST ? list_node_index<ODD>() : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= ncell) return;
     MP_NODE_ADDRESSING
     const int64_t w2 = L.i2(i, j, k);
@@ -616,7 +629,7 @@ __global__ void __launch_bounds__(128, 4) k_mp_step_ff(S *__restrict__ f, S *__r
             dst = f64_of_ff(v);
         }
     };
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = LIST ? list_node_index<ODD>() : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= ncell) return;
     MP_NODE_ADDRESSING
     const int64_t w2 = L.i2(i, j, k);
@@ -1975,7 +1988,7 @@ __global__ void __launch_bounds__(128, SweepOcc<S>::kMinBlocks) k_sp_list(S *__r
         if (threadIdx.x < 72 && first < nf)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(nb + (int64_t)(threadIdx.x >> 2) * nf + first));
     }
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = list_node_index<ODD>();
     if (t >= nf) return;
     sp_list_node<S, ODD, UNIT>(A, stride, nb, nf, t, P, cf, scale);
 }
@@ -2022,6 +2035,11 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
     const int tid = threadIdx.x;
     const int ntiles = nf / kTmaNodes;   // whole tiles only
     const int m = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    // the n-th tile of this block (last tile first when the even steps walk backwards)
+    auto tile_of = [&](int n) -> int {
+        const int k = (int)blockIdx.x + n * (int)gridDim.x;
+        return MFLBM_EVEN_REVERSE ? ntiles - 1 - k : k;
+    };
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) {
             bulk::mbar_init(&full[s], 1);
@@ -2046,13 +2064,13 @@ __global__ void __launch_bounds__(kTmaNodes + 32, 4)
                     ok = false;
                     break;
                 }
-                bulk::tma_store_2d(&map, ((int)blockIdx.x + np * (int)gridDim.x) * kTmaNodes, 0, buf);
+                bulk::tma_store_2d(&map, tile_of(np) * kTmaNodes, 0, buf);
                 bulk::bulk_commit();
                 bulk::bulk_wait_read0();
             }
             if (n < m) {
                 bulk::mbar_arrive_expect_tx(&full[s], (uint32_t)TmaTile<S>::bytes);
-                bulk::tma_load_2d(buf, &map, ((int)blockIdx.x + n * (int)gridDim.x) * kTmaNodes, 0, &full[s]);
+                bulk::tma_load_2d(buf, &map, tile_of(n) * kTmaNodes, 0, &full[s]);
                 last_load[s] = n;
             }
         }
