@@ -1954,6 +1954,7 @@ __device__ __forceinline__ void sp_list_odd_node(S *__restrict__ A, const int64_
 template <class S> struct TablePrefetch { static constexpr int kAhead = 0; };
 template <> struct TablePrefetch<__half> { static constexpr int kAhead = 1024; };
 template <> struct TablePrefetch<ffs> { static constexpr int kAhead = 512; };
+
 // one fluid node of the list sweep (shared by the single-sample and ensemble kernels)
 template <class S, bool ODD, bool UNIT>
 __device__ __forceinline__ void sp_list_node(S *__restrict__ A, const int64_t stride, const int32_t *__restrict__ nb,
