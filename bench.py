@@ -102,6 +102,23 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The largest of x over all ranks of the process group (x itself without one): the
+    slowest rank's time is the job's time.  device: "cuda" under NCCL, "cpu" under gloo."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mlups(nodes_per_rank, steps, world, seconds):
+    """Fluid-node updates of all ranks (independent replicas of the same workload) per
+    second of the slowest rank, in millions."""
+    return world * nodes_per_rank * steps / seconds / 1e6
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -738,12 +755,8 @@ def main():
     sim.set_profiling(True)
     sim.run(args.warmup + 1, args.steps)
     prof = sim.get_profile()   # synchronises the context stream
-    total_s = prof["region_ms"] / 1e3
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * pore * args.steps / total_s / 1e6
+    total_s = max_over_ranks(prof["region_ms"] / 1e3, dist, "cuda")
+    value = whole_job_mlups(pore, args.steps, world, total_s)
 
     # ---- graph-replayed region (the production path, no per-kernel events)
     barrier()
@@ -766,10 +779,10 @@ def main():
                              pinned.get("g_convec"), pinned.get("phi_convec"))
             sim.run(1, rs)           # the uploaded state follows an even step
             prof_z, scal, status = sim.monitor()
-        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
         h2d = sum(v.nbytes for k, v in pinned.items() if k != "f_convec" or p.outlet_bc == 1)
         d2h = (7 if p.multiphase else 2) * p.nz * 8 + 3 * 8 + 4
-        e2e = {"value": world * pore * rs * nround / e2e_s / 1e6, "unit": "MLUPS",
+        e2e = {"value": whole_job_mlups(pore, rs * nround, world, e2e_s), "unit": "MLUPS",
                "h2d_bytes_per_step": h2d / rs, "d2h_bytes_per_step": d2h / rs,
                "round": f"upload full state (pinned) + {rs} steps + monitor readback"}
     except Exception as exc:  # keep the device-timed number even if e2e fails
