@@ -165,9 +165,10 @@ template <> struct Store<ffs> {
 // for.  The double-word storage sweep issues about 1,500 instructions per node and waits
 // on memory between them: its natural 96 registers leave 5 blocks per SM; a cap of 72
 // registers gives 7 at about 70 bytes of spill, measured 7 % faster on GB300 (5 / 6 / 7
-// blocks: 14.0 / 14.5 / 15.0 GLUPS on a 256^3 packing).  The FP64-storage double-word
-// sweep is issue-bound (conversions) and gained nothing; the other forms keep the
-// allocator's choice.
+// blocks: 14.0 / 14.5 / 15.0 GLUPS on a 256^3 packing).  Since the even step runs through
+// the TMA kernel, the cap acts on the odd step (and the dense sweep): 5 / 6 / 7 / 8 blocks
+// gave 14,778 / 15,094 / 15,800 / 15,498 MLUPS.  The FP64-storage double-word sweep is
+// issue-bound and gained nothing; the other forms keep the allocator's choice.
 #ifndef MFLBM_FF_MIN_BLOCKS
 #define MFLBM_FF_MIN_BLOCKS 7
 #endif
