@@ -16,7 +16,9 @@ Workload (one bench "step" = one LBM time step over the whole lattice):
   --impl reference : the reference algorithm's CPU implementation (the C++
           restatement, all host threads) on the same workload, bounded sample.
 Under torchrun (N>1) every rank runs an independent replica (the lattice is not
-sharded); value = total fluid-node updates of all ranks / max time over ranks.
+sharded); value = total fluid-node updates of all ranks / max time over ranks.  The
+per-form measurements, the convergence study and the CPU baseline belong to the N=1 line
+and are left out at N>1.
 
 Other forms and workloads: --precision 0-4 (FP64, FP32, FP16 deviations, FP64 storage with
 the double-word collision, double-word storage), --workload c1 (tube drainage), c3
@@ -797,7 +799,7 @@ def main():
 
     # ---- every other storage form of the singlephase workload, measured the same way
     forms = None
-    if rank == 0 and args.workload == "c2" and not args.no_forms and not args.open_z:
+    if rank == 0 and world == 1 and args.workload == "c2" and not args.no_forms and not args.open_z:
         forms = {}
         for prec in (0, 3, 4, 1, 2):
             if prec == args.precision:
@@ -809,7 +811,7 @@ def main():
     clk.__exit__(None, None, None)
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:   # the CPU baseline: N = 1 only
         try:
             cpu = cpu_baseline(case, args.cpu_sample_steps)
         except Exception as exc:
@@ -833,7 +835,7 @@ def main():
         }
         if forms is not None:
             line["forms"] = forms
-    if rank == 0 and args.workload == "c2" and not args.no_convergence and not args.open_z:
+    if rank == 0 and world == 1 and args.workload == "c2" and not args.no_convergence and not args.open_z:
         try:
             line["convergence"] = convergence_study(args, case, local)
         except Exception as exc:
