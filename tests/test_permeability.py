@@ -37,3 +37,39 @@ def test_channel_permeability_is_analytic():
 def test_check_interval_must_be_even():
     with pytest.raises(ValueError):
         run_to_steady(None, make_params(multiphase=0), check_every=101)
+
+
+class _FakeSim:
+    """run() advances a scripted mean velocity; monitor() reports it as one slice sum."""
+
+    def __init__(self, us, status_at=None, nx=2, ny=2, nz=1):
+        self.us, self.i, self.status_at, self.n = list(us), 0, status_at, nx * ny * nz
+        self.calls = []
+
+    def run(self, ntime0, nsteps):
+        self.calls.append((ntime0, nsteps))
+        self.i += 1
+
+    def monitor(self):
+        u = self.us[min(self.i, len(self.us)) - 1]
+        st = 3 if self.status_at is not None and self.i >= self.status_at else 0
+        return np.array([[u * self.n], [0.0]]), np.zeros(3), st
+
+
+def test_stopping_rule_and_failure_paths():
+    p = make_params(multiphase=0, nx=2, ny=2, nz=1, la_nu1=1.0 / 6.0, force_z=1e-6)
+    # relative change below tol between two checks: stops at the third check
+    sim = _FakeSim([1.0, 1.1, 1.1 + 1e-9, 9.0])
+    r = run_to_steady(sim, p, check_every=100, tol=1e-7, max_steps=10000)
+    assert r.converged and r.steps == 300 and r.status == 0
+    assert sim.calls == [(1, 100), (101, 100), (201, 100)]
+    assert r.k == permeability(1.1 + 1e-9, 1.0 / 6.0, 1e-6)
+    # the instability status of the monitor (NaN or |u| > 0.5) ends the run unconverged
+    r = run_to_steady(_FakeSim([1.0, 2.0, 3.0], status_at=2), p, check_every=100, tol=1e-7, max_steps=10000)
+    assert not r.converged and r.status == 3 and r.steps == 200
+    # a NaN mean velocity ends it too
+    r = run_to_steady(_FakeSim([1.0, float("nan")]), p, check_every=100, tol=1e-7, max_steps=10000)
+    assert not r.converged and r.steps == 200
+    # the step cap
+    r = run_to_steady(_FakeSim([1.0, 2.0, 4.0, 8.0, 16.0]), p, check_every=100, tol=1e-7, max_steps=400)
+    assert not r.converged and r.steps == 400 and len(r.history) == 4
