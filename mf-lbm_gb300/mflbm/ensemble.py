@@ -157,14 +157,16 @@ def run_to_steady(ens, nf, check_every=100, tol=1e-7, max_steps=200000, clock=ti
         if status != 0:
             break
         cur = w / ens.volume
+        left = False
         for s in np.nonzero(active)[0]:
             u[s] = cur[s]
             steps[s] = done
             if np.isfinite(prev[s]) and cur[s] != 0.0 and abs(cur[s] - prev[s]) / abs(cur[s]) < tol:
                 conv[s] = True
                 active[s] = 0
+                left = True
             prev[s] = cur[s]
-        if not active.all():
+        if left:   # the device's tile table changes only when a sample has left it
             ens.set_active(active)
     secs = clock() - t0
     k = ens.p.la_nu1 * u / ens.p.force_z
